@@ -1,0 +1,136 @@
+"""Generate the golden vectors in tests/golden/ from the compiled reference.
+
+Run here (where the reference sources are mounted) with
+``python tests/golden/make_golden.py``.  It builds the reference drivers and
+the golden tools (oracle/Makefile, target ``ref``) and, for each case:
+
+* writes the seeded inputs with this package's generators (Hamiltonian MPO,
+  exciton-density MPOs, random right-canonical MPS) in the reference's binary
+  formats, so the reference and the GPU library read identical bytes;
+* runs ``kv_ref_ops`` (reference primitives on those inputs -> ``*.kvt``);
+* runs ``kv_ref_tdvp`` (the reference TDVP driver, per-sweep norm / energy /
+  populations / max bond -> ``traj_*.txt``);
+* runs ``kln-holstein`` on the same model's text input and records
+  <psi|H_ref|psi> so the MPO builder is pinned to the reference's own
+  Hamiltonian construction.
+
+Small cases keep every input and output; the config-sized case keeps only the
+trajectory and an input checksum (its inputs are regenerated from the seed).
+"""
+from __future__ import annotations
+
+import importlib.util
+import json
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+REF_BIN = os.path.join(ROOT, "oracle", "_ref")
+
+
+def _pkg():
+    if "kylin_v_gb300" not in sys.modules:
+        d = os.path.join(ROOT, "kylin-v_gb300")
+        spec = importlib.util.spec_from_file_location("kylin_v_gb300", os.path.join(d, "__init__.py"),
+                                                      submodule_search_locations=[d])
+        m = importlib.util.module_from_spec(spec)
+        sys.modules["kylin_v_gb300"] = m
+        spec.loader.exec_module(m)
+    return sys.modules["kylin_v_gb300"]
+
+
+def cases():
+    from kylin_v_gb300.holstein import HolsteinChain
+
+    return {
+        # 3 molecules x 1 mode, cutoff 4: 9 sites
+        "tiny1": dict(chain=HolsteinChain(3, [1.0], [[1.0], [0.8], [1.2]], cutoff=4, eps=[0.1, -0.2, 0.3]),
+                      D=8, seed=11, ops_sites=[1, 4], traj=[("[0,0,0,4]", 8, 1e-8), ("[0,3,0,0]", 8, 1e-8)],
+                      keep_inputs=True),
+        # 2 molecules x 2 modes, cutoff 3: 10 sites
+        "tiny2m": dict(chain=HolsteinChain(2, [1.0, 0.4], [[1.0, 0.6], [0.9, 0.5]], cutoff=3),
+                       D=10, seed=12, ops_sites=[2, 6], traj=[("[0,0,0,3]", 10, 1e-8), ("[0,3,0,0]", 10, 1e-8)],
+                       keep_inputs=True),
+        # the 1-site benchmark shape: L=8, 1 mode, cutoff 8, D=32, 20 steps
+        "l8c8d32": dict(chain=HolsteinChain(8, [1.0], [[1.0]] * 8, cutoff=8), D=32, seed=1234, ops_sites=[7],
+                        traj=[("[0,0,0,20]", 32, 1e-8)], keep_inputs=False),
+    }
+
+
+def run(cmd, cwd):
+    r = subprocess.run(cmd, cwd=cwd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"{cmd}: {r.stdout}\n{r.stderr}")
+    return r.stdout
+
+
+def main():
+    _pkg()
+    from kylin_v_gb300 import holstein as H
+    from kylin_v_gb300 import kvio
+
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", "-j4"], check=True,
+                   stdout=subprocess.DEVNULL)
+    manifest = {}
+    for name, c in cases().items():
+        ch = c["chain"]
+        out = os.path.join(HERE, name)
+        os.makedirs(out, exist_ok=True)
+        work = tempfile.mkdtemp(prefix="kvgold_")
+        os.makedirs(os.path.join(work, "State"))
+        os.makedirs(os.path.join(work, "Op"))
+        mps = H.random_mps(ch, c["D"], seed=c["seed"])
+        mpo = H.hamiltonian_mpo(ch)
+        kvio.write_mps(os.path.join(work, "in.mps"), mps)
+        kvio.write_mpo(os.path.join(work, "H.mpo"), mpo)
+        dens = []
+        for j in ch.exciton_sites():
+            p = os.path.join(work, f"D{j}.mpo")
+            kvio.write_mpo(p, H.density_mpo(ch, j))
+            dens.append(p)
+        entry = {"D": c["D"], "seed": c["seed"], "n_sites": ch.n_sites,
+                 "site_norms2": [float(sum(np.vdot(a, a).real for _, a in t.blocks)) for t in mps]}
+        # reference-built Hamiltonian on the same model
+        with open(os.path.join(work, "chain.inp"), "w") as f:
+            f.write(ch.reference_input())
+        run([os.path.join(REF_BIN, "kln-holstein"), "-i", "chain.inp", "-t", "1e-14"], work)
+        e_ref = run([os.path.join(REF_BIN, "kln-join"), "-a", "in.mps", "-b", "in.mps", "-o", "Op/H_tot"], work)
+        e_mine = run([os.path.join(REF_BIN, "kln-join"), "-a", "in.mps", "-b", "in.mps", "-o", "H.mpo"], work)
+        entry["energy_ref_mpo"] = float(e_ref.strip().strip("()").split(",")[0])
+        entry["energy_own_mpo"] = float(e_mine.strip().strip("()").split(",")[0])
+        if c["keep_inputs"]:
+            for f in ("in.mps", "H.mpo"):
+                shutil.copy(os.path.join(work, f), os.path.join(out, f))
+            shutil.copy(os.path.join(work, "Op", "H_tot"), os.path.join(out, "H_ref.mpo"))
+            for site in c["ops_sites"]:
+                od = os.path.join(out, f"ops_site{site}")
+                os.makedirs(od, exist_ok=True)
+                run([os.path.join(REF_BIN, "kv_ref_ops"), "-w", "in.mps", "-o", "H.mpo", "-i", str(site),
+                     "-v", "0.05", "-k", "11", "-e", "1e-8", "-t", "1e-8", "-D", str(c["D"]), "-O", od], work)
+        trajs = []
+        for stage, maxd, tol in c["traj"]:
+            for f in os.listdir(os.path.join(work, "State")):
+                os.remove(os.path.join(work, "State", f))
+            txt = run([os.path.join(REF_BIN, "kv_ref_tdvp"), "-w", "in.mps", "-o", "H.mpo", "-s", stage,
+                       "-v", "0.05", "-D", str(maxd), "-t", str(tol), "-k", "11", "-e", "1e-8",
+                       "-d", ",".join(os.path.basename(p) for p in dens)], work)
+            tag = stage.strip("[]").replace(",", "_")
+            with open(os.path.join(out, f"traj_{tag}.txt"), "w") as f:
+                f.write(f"# stage {stage} dt 0.05 maxD {maxd} tolSVD {tol} maxIter 11 tolExp 1e-8\n")
+                f.write(txt)
+            trajs.append({"stage": stage, "maxD": maxd, "tol_svd": tol, "file": f"traj_{tag}.txt"})
+        entry["trajectories"] = trajs
+        manifest[name] = entry
+        shutil.rmtree(work)
+    with open(os.path.join(HERE, "manifest.json"), "w") as f:
+        json.dump(manifest, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,67 @@
+"""Shared helpers for the test-suite: package loading and tensor comparison."""
+from __future__ import annotations
+
+import importlib.util
+import json
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def load_package():
+    if "kylin_v_gb300" not in sys.modules:
+        d = os.path.join(ROOT, "kylin-v_gb300")
+        spec = importlib.util.spec_from_file_location("kylin_v_gb300", os.path.join(d, "__init__.py"),
+                                                      submodule_search_locations=[d])
+        m = importlib.util.module_from_spec(spec)
+        sys.modules["kylin_v_gb300"] = m
+        spec.loader.exec_module(m)
+    return sys.modules["kylin_v_gb300"]
+
+
+def load_oracle():
+    if os.path.join(ROOT, "oracle") not in sys.path:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # noqa: E402
+
+    return oracle
+
+
+def manifest():
+    with open(os.path.join(GOLDEN, "manifest.json")) as f:
+        return json.load(f)
+
+
+def tensor_diff(a, b) -> float:
+    """Max abs difference of two block tensors compared block-by-block by
+    (charges, shape); a block missing on one side counts as zeros."""
+    da, db = a.as_dict(), b.as_dict()
+    m = 0.0
+    for k in set(da) | set(db):
+        x = da.get(k)
+        y = db.get(k)
+        if x is None:
+            m = max(m, float(np.abs(y).max(initial=0.0)))
+        elif y is None:
+            m = max(m, float(np.abs(x).max(initial=0.0)))
+        else:
+            m = max(m, float(np.abs(x - y).max(initial=0.0)))
+    return m
+
+
+def tensor_scale(a) -> float:
+    return max((float(np.abs(x).max(initial=0.0)) for _, x in a.blocks), default=0.0)
+
+
+def read_traj(path):
+    rows = []
+    with open(path) as f:
+        for line in f:
+            if line.startswith("#"):
+                continue
+            rows.append([float(x) for x in line.split()])
+    return np.array(rows)
