@@ -1,0 +1,146 @@
+/*
+ * kvgpu.h -- C ABI of the GB300-native Holstein TDVP library (libkvgpu.so).
+ *
+ * The reference (Kylin-V) has no FFI: its operator surface is the C++
+ * template API of holstein/*.h, called by src/kln-tdvp.cpp:73-78.  Each entry
+ * point below replaces one function of that surface; the citation on each
+ * declaration names the reference function (file:line) whose arguments,
+ * results and error behaviour it mirrors.
+ *
+ * Conventions
+ *  - Tensors are U(1) block-sparse, complex128 at the boundary.  A tensor is
+ *    passed as (rank, dirs[rank], nblocks, shapes[nblocks*rank],
+ *    qns[nblocks*rank], data): the reference's Tensor<Rank>/Block<Rank>
+ *    (holstein/tensor.h:16-209, holstein/block.h:23-166) -- leg directions,
+ *    then per block its shape and per-leg charges, block data row-major and
+ *    blocks concatenated in order (the same order as the .mps/.mpo files,
+ *    holstein/state.h:107-128).  `data` is interleaved (re, im) doubles.
+ *  - Device-resident tensors are opaque kv_tensor handles owned by the caller
+ *    (kv_tensor_free).  Nothing in the ABI exposes torch or CUDA types.
+ *  - Every function returns KV_OK (0) or a negative KV_E* code; it never
+ *    exits the process (the reference prints and calls exit(1)).
+ *    kv_last_error() returns a message for the calling thread's last error.
+ *  - All work is issued on the library's CUDA stream of the current device;
+ *    calls are synchronous with respect to the host unless stated otherwise.
+ */
+#ifndef KVGPU_H
+#define KVGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------- status codes */
+#define KV_OK          0
+#define KV_EINVAL     -1  /* bad argument (rank, shapes, directions, mode)   */
+#define KV_ECUDA      -2  /* CUDA runtime error                             */
+#define KV_ENOMEM     -3  /* device allocation failed                       */
+#define KV_ENONFINITE -4  /* NaN/Inf in a Lanczos norm or singular value    */
+#define KV_ETIMEOUT   -5  /* a bounded device wait gave up                  */
+#define KV_ENOTINIT   -6  /* kv_init not called                            */
+#define KV_EMISMATCH  -7  /* contracted legs' directions mismatch           */
+
+/* ------------------------------------------------------- arithmetic modes */
+/* KV_FP64: every contraction in complex128 on the CUDA cores.
+ * KV_MIXED_TF32: block contractions as 3M (Gauss) real GEMMs on the tcgen05
+ *   tensor cores with TF32 hi/lo split operands (hi*hi + hi*lo + lo*hi) and
+ *   FP32 accumulation in tensor memory; Lanczos, norms, the tridiagonal
+ *   exponential, MPO mixing and SVD stay FP64. */
+#define KV_FP64        0
+#define KV_MIXED_TF32  1
+
+/* contraction operand modes (numerically the CBLAS ones the reference uses) */
+#define KV_OP_N 111
+#define KV_OP_T 112
+#define KV_OP_C 113
+
+typedef struct kv_tensor_s *kv_tensor;
+typedef struct kv_tdvp_s *kv_tdvp;
+
+/* Library lifetime: select the device and create the stream / pools. */
+int kv_init(int device);
+int kv_shutdown(void);
+const char *kv_last_error(void);
+int kv_version(void);
+
+/* -------------------------------------------------------------- tensors */
+/* Upload a block tensor to the device.  data may be NULL (zero blocks).
+ * Replaces constructing Tensor<Rank> from Blocks (holstein/tensor.h:55-77,
+ * holstein/state.h:130-157 for the file order). */
+int kv_tensor_create(int rank, const int *dirs, int nblocks, const int *shapes, const int *qns,
+                     const double *data, kv_tensor *out);
+/* rank, block count and total complex elements */
+int kv_tensor_info(kv_tensor t, int *rank, int *nblocks, long long *nelem);
+/* Download: dirs[rank], shapes/qns[nblocks*rank], data[2*nelem]. */
+int kv_tensor_download(kv_tensor t, int *dirs, int *shapes, int *qns, double *data);
+int kv_tensor_free(kv_tensor t);
+
+/* -------------------------------------------------------- primitives */
+/* product<N1,N2,nc>(A, B, opA, opB): contract the last nc legs of op(A) with
+ * the first nc legs of op(B); opA in {N, C}, opB in {N, T}.
+ * holstein/product.h:61-201 */
+int kv_product(kv_tensor A, kv_tensor B, int nc, int opA, int opB, int precision, kv_tensor *out);
+
+/* H_eff . psi for nsite = 0 (apply_zero, holstein/product.h:540-545; W1, W2
+ * unused), 1 (apply_single, holstein/product.h:547-553; W2 unused) or 2
+ * (apply_double, holstein/product.h:478-486).  Result scaled by `scale`. */
+int kv_heff_apply(int nsite, kv_tensor L, kv_tensor psi, kv_tensor W1, kv_tensor W2, kv_tensor R,
+                  double scale, int precision, kv_tensor *out);
+
+/* Environment update env_sweep(env, A, W, l2r) (holstein/product.h:488-503). */
+int kv_env_update(int l2r, kv_tensor env, kv_tensor A, kv_tensor W, int precision, kv_tensor *out);
+
+/* local_krylov<Rank> (holstein/exponential.h:92-190): psi <- exp(-+i H_eff dt/2) psi
+ * (normalised first), Lanczos while k < max_iter-1 and the product of Lanczos
+ * norms exceeds tol; reverse selects exp(+i ...).  psi is replaced by a new
+ * device tensor (the old handle stays valid and unchanged).  iters receives
+ * the Krylov dimension used. */
+int kv_lanczos_expm(int nsite, kv_tensor L, kv_tensor psi, kv_tensor W1, kv_tensor W2, kv_tensor R,
+                    double dt, int max_iter, double tol, int reverse, int precision, kv_tensor *out,
+                    int *iters);
+
+/* svd_impl<R1,R2>(A, cfg, -1) (holstein/svd.h:296-440): block SVD per charge
+ * sector with the reference's global truncation (keep while index < max_dim
+ * and s > tol, never fewer than one).  l2r folds S into V (S.Vt), else into U.
+ * n_kept / n_total receive the kept and total singular-value counts. */
+int kv_svd_truncate(kv_tensor A, int r1, int l2r, double tol, int max_dim, kv_tensor *U, kv_tensor *V,
+                    int *n_kept, int *n_total);
+
+/* ---------------------------------------------------- sweep driver */
+/* TDVP(State, Operator, tolSVD, tolExp, maxDim, maxIter, dt) followed by the
+ * environment set-up of total_start (holstein/tdvp.h:60-76, 303-316).
+ * mps/mpo are arrays of nsites tensor handles (copied). */
+int kv_tdvp_create(int nsites, const kv_tensor *mps, const kv_tensor *mpo, double tol_svd, double tol_exp,
+                   int max_dim, int max_iter, double dt, int precision, kv_tdvp *out);
+/* One time step: mode 1 = TDVP::one_site (holstein/tdvp.h:78-141),
+ * mode 2 = TDVP::two_site (holstein/tdvp.h:144-227). */
+int kv_tdvp_sweep(kv_tdvp s, int mode);
+/* New handle with a copy of the current site tensor i. */
+int kv_tdvp_site(kv_tdvp s, int i, kv_tensor *out);
+/* Timings of the last sweep: per-module device time in ms in the order
+ * Evl-0, Evl-1, Evl-2, SVD, Update, Sweep (the reference's Timer modules,
+ * util/timer.h:19-66, holstein/tdvp.h:85-106), the whole sweep's device
+ * time, the algorithmic flop count (8*M*N*K summed over every zgemm the
+ * reference issues for the same sweep, Lanczos iterations as actually run)
+ * and the part of it in product<> block pairs (the grouped GEMM kernel). */
+int kv_tdvp_stats(kv_tdvp s, double *module_ms, double *sweep_ms, double *ref_flops, double *gemm_ref_flops);
+int kv_tdvp_free(kv_tdvp s);
+
+/* ------------------------------------------------------ instrumentation */
+/* No reference counterpart (the reference only has its Timer table).
+ * kv_profile(1) brackets every grouped-GEMM launch with CUDA events;
+ * kv_profile_read returns (and resets) their summed device time, the
+ * reference flops of the block pairs they multiplied and the launch count.
+ * kv_counters returns the number of kernels launched since kv_init. */
+int kv_profile(int enable);
+int kv_profile_read(double *gemm_ms, double *gemm_ref_flops, long long *gemm_launches);
+int kv_counters(long long *launches);
+
+/* <a|W|b> (Operator::join, holstein/operator.h:178-198) over nsites. */
+int kv_expectation(int nsites, const kv_tensor *bra, const kv_tensor *mpo, const kv_tensor *ket, double *re,
+                   double *im);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* KVGPU_H */

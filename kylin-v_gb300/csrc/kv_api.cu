@@ -1,0 +1,275 @@
+// C ABI of libkvgpu (include/kvgpu.h).  Every entry point converts C++
+// exceptions into status codes; nothing here exits the process.
+#include <cstdio>
+#include <cstring>
+#include <memory>
+
+#include "kv_engine.h"
+
+struct kv_tensor_s {
+    kv::TensorP t;
+};
+struct kv_tdvp_s {
+    std::unique_ptr<kv::Tdvp> s;
+};
+
+namespace {
+thread_local std::string g_err;
+
+template <class F>
+int guard(F &&f) {
+    try {
+        f();
+        return KV_OK;
+    } catch (const kv::Error &e) {
+        g_err = e.what();
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        g_err = "host allocation failed";
+        return KV_ENOMEM;
+    } catch (const std::exception &e) {
+        g_err = e.what();
+        return KV_EINVAL;
+    }
+}
+
+kv::DTensor *T(kv_tensor h) {
+    KV_REQUIRE(h && h->t, KV_EINVAL, "null tensor handle");
+    return h->t.get();
+}
+kv::DTensor *Topt(kv_tensor h) { return (h && h->t) ? h->t.get() : nullptr; }
+
+kv_tensor wrap(kv::TensorP t) {
+    auto *h = new kv_tensor_s;
+    h->t = std::move(t);
+    return h;
+}
+
+void sync() { KV_CUDA(cudaStreamSynchronize(kv::ctx().stream)); }
+}  // namespace
+
+extern "C" {
+
+int kv_version(void) { return 1; }
+
+const char *kv_last_error(void) { return g_err.c_str(); }
+
+int kv_init(int device) {
+    return guard([&] {
+        auto &c = kv::ctx();
+        if (c.device == device && c.stream) return;
+        KV_REQUIRE(c.device < 0, KV_EINVAL, "kv_init already called for another device");
+        int n = 0;
+        KV_CUDA(cudaGetDeviceCount(&n));
+        KV_REQUIRE(device >= 0 && device < n, KV_EINVAL, "no such CUDA device");
+        KV_CUDA(cudaSetDevice(device));
+        KV_CUDA(cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, device));
+        KV_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+        cudaMemPool_t pool;
+        KV_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+        uint64_t thr = ~0ull;  // keep freed blocks cached in the pool
+        KV_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+        c.device = device;
+    });
+}
+
+int kv_shutdown(void) {
+    return guard([&] {
+        auto &c = kv::ctx();
+        if (c.device < 0) return;
+        KV_CUDA(cudaStreamSynchronize(c.stream));
+        KV_CUDA(cudaStreamDestroy(c.stream));
+        c.stream = nullptr;
+        c.device = -1;
+    });
+}
+
+int kv_tensor_create(int rank, const int *dirs, int nblocks, const int *shapes, const int *qns, const double *data,
+                     kv_tensor *out) {
+    return guard([&] {
+        kv::require_init();
+        KV_REQUIRE(out && dirs && (nblocks == 0 || (shapes && qns)), KV_EINVAL, "null argument");
+        *out = wrap(kv::upload_tensor(rank, dirs, nblocks, shapes, qns, data));
+        sync();
+    });
+}
+
+int kv_tensor_info(kv_tensor t, int *rank, int *nblocks, long long *nelem) {
+    return guard([&] {
+        kv::DTensor *x = T(t);
+        if (rank) *rank = x->meta.rank;
+        if (nblocks) *nblocks = (int)x->meta.blocks.size();
+        if (nelem) *nelem = x->meta.nelem;
+    });
+}
+
+int kv_tensor_download(kv_tensor t, int *dirs, int *shapes, int *qns, double *data) {
+    return guard([&] {
+        kv::require_init();
+        kv::download_tensor(*T(t), dirs, shapes, qns, data);
+    });
+}
+
+int kv_tensor_free(kv_tensor t) {
+    return guard([&] { delete t; });
+}
+
+int kv_product(kv_tensor A, kv_tensor B, int nc, int opA, int opB, int precision, kv_tensor *out) {
+    return guard([&] {
+        kv::require_init();
+        *out = wrap(kv::op_product(*T(A), *T(B), nc, opA, opB, precision));
+        sync();
+    });
+}
+
+int kv_heff_apply(int nsite, kv_tensor L, kv_tensor psi, kv_tensor W1, kv_tensor W2, kv_tensor R, double scale,
+                  int precision, kv_tensor *out) {
+    return guard([&] {
+        kv::require_init();
+        KV_REQUIRE(nsite >= 0 && nsite <= 2, KV_EINVAL, "nsite must be 0, 1 or 2");
+        KV_REQUIRE(nsite < 1 || Topt(W1), KV_EINVAL, "W1 required");
+        KV_REQUIRE(nsite < 2 || Topt(W2), KV_EINVAL, "W2 required");
+        *out = wrap(kv::op_heff(nsite, *T(L), *T(psi), Topt(W1), Topt(W2), *T(R), scale, precision));
+        sync();
+    });
+}
+
+int kv_env_update(int l2r, kv_tensor env, kv_tensor A, kv_tensor W, int precision, kv_tensor *out) {
+    return guard([&] {
+        kv::require_init();
+        *out = wrap(kv::op_env(l2r != 0, *T(env), *T(A), *T(W), nullptr, precision, nullptr));
+        sync();
+    });
+}
+
+int kv_lanczos_expm(int nsite, kv_tensor L, kv_tensor psi, kv_tensor W1, kv_tensor W2, kv_tensor R, double dt,
+                    int max_iter, double tol, int reverse, int precision, kv_tensor *out, int *iters) {
+    return guard([&] {
+        kv::require_init();
+        KV_REQUIRE(nsite >= 0 && nsite <= 2, KV_EINVAL, "nsite must be 0, 1 or 2");
+        KV_REQUIRE(nsite < 1 || Topt(W1), KV_EINVAL, "W1 required");
+        KV_REQUIRE(nsite < 2 || Topt(W2), KV_EINVAL, "W2 required");
+        kv::DevBuf st(sizeof(kv::KrylovState));
+        kv::TensorP r = kv::op_lanczos(nsite, *T(L), *T(psi), Topt(W1), Topt(W2), *T(R), dt, max_iter, tol,
+                                       reverse != 0, precision, st.as<kv::KrylovState>(), nullptr);
+        kv::KrylovState h;
+        KV_CUDA(cudaMemcpyAsync(&h, st.p, sizeof(h), cudaMemcpyDeviceToHost, kv::ctx().stream));
+        sync();
+        KV_REQUIRE(h.status == KV_OK, h.status, "non-finite norm in the Lanczos recurrence");
+        if (iters) *iters = h.iters;
+        *out = wrap(r);
+    });
+}
+
+int kv_svd_truncate(kv_tensor A, int r1, int l2r, double tol, int max_dim, kv_tensor *U, kv_tensor *V, int *n_kept,
+                    int *n_total) {
+    return guard([&] {
+        kv::require_init();
+        kv::SvdOut r = kv::op_svd(*T(A), r1, l2r != 0, tol, max_dim);
+        sync();
+        *U = wrap(r.U);
+        *V = wrap(r.V);
+        if (n_kept) *n_kept = r.n_kept;
+        if (n_total) *n_total = r.n_total;
+    });
+}
+
+int kv_tdvp_create(int nsites, const kv_tensor *mps, const kv_tensor *mpo, double tol_svd, double tol_exp,
+                   int max_dim, int max_iter, double dt, int precision, kv_tdvp *out) {
+    return guard([&] {
+        kv::require_init();
+        KV_REQUIRE(nsites >= 2 && mps && mpo, KV_EINVAL, "need >= 2 sites");
+        std::vector<kv::TensorP> a, w;
+        for (int i = 0; i < nsites; ++i) {
+            T(mps[i]);
+            T(mpo[i]);
+            a.push_back(mps[i]->t);
+            w.push_back(mpo[i]->t);
+        }
+        auto *h = new kv_tdvp_s;
+        try {
+            h->s.reset(new kv::Tdvp(a, w, tol_svd, tol_exp, max_dim, max_iter, dt, precision));
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *out = h;
+    });
+}
+
+int kv_tdvp_sweep(kv_tdvp s, int mode) {
+    return guard([&] {
+        kv::require_init();
+        KV_REQUIRE(s && s->s, KV_EINVAL, "null TDVP handle");
+        if (mode == 1) s->s->one_site();
+        else if (mode == 2) s->s->two_site();
+        else throw kv::Error(KV_EINVAL, "mode must be 1 or 2");
+    });
+}
+
+int kv_tdvp_site(kv_tdvp s, int i, kv_tensor *out) {
+    return guard([&] {
+        KV_REQUIRE(s && s->s && i >= 0 && i < (int)s->s->mps.size(), KV_EINVAL, "bad site index");
+        *out = wrap(kv::clone(*s->s->mps[i]));
+        sync();
+    });
+}
+
+int kv_tdvp_stats(kv_tdvp s, double *module_ms, double *sweep_ms, double *ref_flops, double *gemm_ref_flops) {
+    return guard([&] {
+        KV_REQUIRE(s && s->s, KV_EINVAL, "null TDVP handle");
+        if (module_ms)
+            for (int i = 0; i < kv::MOD_COUNT; ++i) module_ms[i] = s->s->module_ms[i];
+        if (sweep_ms) *sweep_ms = s->s->sweep_ms;
+        if (ref_flops) *ref_flops = s->s->last_ref_flops;
+        if (gemm_ref_flops) *gemm_ref_flops = s->s->last_gemm_flops;
+    });
+}
+
+int kv_profile(int enable) {
+    return guard([&] {
+        kv::require_init();
+        kv::ctx().prof = enable != 0;
+    });
+}
+
+int kv_profile_read(double *gemm_ms, double *gemm_ref_flops, long long *gemm_launches) {
+    return guard([&] {
+        kv::require_init();
+        kv::prof_resolve(nullptr, nullptr);
+        auto &c = kv::ctx();
+        if (gemm_ms) *gemm_ms = c.prof_ms;
+        if (gemm_ref_flops) *gemm_ref_flops = c.prof_flops;
+        if (gemm_launches) *gemm_launches = c.prof_launches;
+        c.prof_ms = c.prof_flops = 0.0;
+        c.prof_launches = 0;
+    });
+}
+
+int kv_counters(long long *launches) {
+    return guard([&] {
+        if (launches) *launches = kv::ctx().launches;
+    });
+}
+
+int kv_tdvp_free(kv_tdvp s) {
+    return guard([&] { delete s; });
+}
+
+int kv_expectation(int nsites, const kv_tensor *bra, const kv_tensor *mpo, const kv_tensor *ket, double *re,
+                   double *im) {
+    return guard([&] {
+        kv::require_init();
+        std::vector<kv::DTensor *> a, w, b;
+        for (int i = 0; i < nsites; ++i) {
+            a.push_back(T(bra[i]));
+            w.push_back(T(mpo[i]));
+            b.push_back(T(ket[i]));
+        }
+        kv::cplx r = kv::op_expectation(a, w, b);
+        *re = r.real();
+        *im = r.imag();
+    });
+}
+
+}  // extern "C"

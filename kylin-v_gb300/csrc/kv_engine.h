@@ -1,0 +1,104 @@
+// Host-side engine declarations: plans, operations, TDVP driver.
+#pragma once
+#include "kv_internal.h"
+
+namespace kv {
+
+// Output tile shape of the grouped GEMM for a precision mode.
+inline int kTileM(int precision) { return precision == KV_MIXED_TF32 ? 128 : 32; }
+inline int kTileN(int precision) { return precision == KV_MIXED_TF32 ? 64 : 32; }
+
+// reference flop count split by who executes it here: the grouped GEMM
+// (product<> pairs) or the MPO mixing kernel (env_mps_mpo zgemms)
+struct Flops {
+    double gemm = 0.0, mix = 0.0;
+};
+
+struct ProductPlan {
+    Meta out;
+    GemmPlan gemm;
+    std::vector<std::vector<GemmSeg>> per_out;  // segments per output block
+    std::vector<std::pair<int, int>> mn;        // (M, N) per output block
+};
+
+struct MixPlanFull {
+    Meta out;       // merged output structure (what is computed)
+    Meta unmerged;  // one block per matched pair (the reference's structure)
+    MixPlan mix;
+    double ref_flops = 0.0;
+};
+
+struct HeffPlan {
+    int nsite = 1;
+    Meta klayout;  // Krylov layout (closure of psi's blocks under H_eff)
+    ProductPlan p1, p2;
+    MixPlanFull m1, m2;
+    DevBuf t1, t2, t3;  // intermediates
+    double ref_flops = 0.0;   // reference flops of one H_eff application
+    double gemm_flops = 0.0;  // of which executed by the grouped GEMM
+};
+
+struct SvdOut {
+    TensorP U, V;
+    int n_kept = 0, n_total = 0;
+    std::vector<double> kept_s;
+};
+
+ProductPlan plan_product(const Meta &A, const Meta &B, int nc, int opA, int opB);
+void build_tiles(ProductPlan &P, const std::vector<int64_t> &target_off, int tile_m, int tile_n);
+MixPlanFull plan_mix(const Meta &lm, const Meta &W, int lead);
+HeffPlan plan_heff(int nsite, const Meta &L, const Meta &psi, const Meta *W1, const Meta *W2, const Meta &R,
+                   int precision);
+
+TensorP op_product(const DTensor &A, const DTensor &B, int nc, int opA, int opB, int precision,
+                   Flops *fl = nullptr);
+TensorP op_heff(int nsite, const DTensor &L, const DTensor &psi, const DTensor *W1, const DTensor *W2,
+                const DTensor &R, double scale, int precision);
+TensorP op_lanczos(int nsite, const DTensor &L, const DTensor &psi, const DTensor *W1, const DTensor *W2,
+                   const DTensor &R, double dt, int max_iter, double tol, bool reverse, int precision,
+                   KrylovState *st_dev, Flops *per_iter);
+SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim);
+TensorP op_env(bool l2r, const DTensor &env, const DTensor &A, const DTensor &W, const DTensor *Wt, int precision,
+               Flops *fl);
+TensorP op_permute(const DTensor &t, const std::vector<int> &ax);
+cplx op_expectation(const std::vector<DTensor *> &a, const std::vector<DTensor *> &w, const std::vector<DTensor *> &b);
+
+enum Module { MOD_EVL0 = 0, MOD_EVL1, MOD_EVL2, MOD_SVD, MOD_UPDATE, MOD_SWEEP, MOD_COUNT };
+
+class Tdvp {
+  public:
+    Tdvp(const std::vector<TensorP> &mps, const std::vector<TensorP> &mpo, double tol_svd, double tol_exp,
+         int max_dim, int max_iter, double dt, int precision);
+    ~Tdvp();
+    void one_site();
+    void two_site();
+    std::vector<TensorP> mps, mpo, mpo_t;
+    std::vector<TensorP> envL, envR;
+    double tol_svd, tol_exp;
+    int max_dim, max_iter;
+    double dt;
+    int precision;
+    double module_ms[MOD_COUNT] = {};
+    double sweep_ms = 0.0;
+    double last_ref_flops = 0.0;   // all reference zgemm flops of the last sweep
+    double last_gemm_flops = 0.0;  // of which in product<> pairs (grouped GEMM)
+
+  private:
+    static constexpr int kStateSlots = 8192;
+    static constexpr int kMaxEvents = 16384;
+    TensorP krylov(int nsite, const DTensor &L, const DTensor &psi, const DTensor *W1, const DTensor *W2,
+                   const DTensor &R, bool reverse, int module);
+    void mark(int module, bool start);
+    KrylovState *next_state();
+    void begin_sweep();
+    void end_sweep();
+    DevBuf kstate;
+    std::vector<cudaEvent_t> events;
+    int mark_module[kMaxEvents] = {};
+    int n_marks = 0, n_krylov = 0;
+    std::vector<std::pair<KrylovState *, Flops>> krylov_flops;
+    Flops other;
+    cudaEvent_t sweep_ev[2] = {};
+};
+
+}  // namespace kv

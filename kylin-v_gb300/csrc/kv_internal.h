@@ -1,0 +1,225 @@
+// Internal runtime of libkvgpu: device block tensors, contraction plans,
+// kernel launch wrappers.  Not part of the public ABI (include/kvgpu.h).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <array>
+#include <complex>
+#include <cstdint>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/kvgpu.h"
+
+namespace kv {
+
+constexpr int kMaxRank = 6;
+using cplx = std::complex<double>;
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+#define KV_CUDA(expr)                                                                           \
+    do {                                                                                        \
+        cudaError_t e_ = (expr);                                                                \
+        if (e_ != cudaSuccess)                                                                  \
+            throw ::kv::Error(e_ == cudaErrorMemoryAllocation ? KV_ENOMEM : KV_ECUDA,            \
+                              std::string(#expr) + ": " + cudaGetErrorString(e_));              \
+    } while (0)
+
+#define KV_REQUIRE(cond, code, msg)                          \
+    do {                                                     \
+        if (!(cond)) throw ::kv::Error((code), (msg));       \
+    } while (0)
+
+// ------------------------------------------------------------------ context
+struct KrylovState;
+
+// One profiled grouped-GEMM launch: its events, the reference flops of the
+// block pairs it multiplies, and (for Lanczos applies) the Krylov state and
+// iteration whose stop flag may have skipped it.
+struct ProfRec {
+    cudaEvent_t a, b;
+    double flops;
+    const KrylovState *st;
+    int k;
+};
+
+struct Context {
+    int device = -1;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    long long launches = 0;  // kernels launched by this library since kv_init
+    bool prof = false;       // bracket grouped-GEMM launches with events
+    std::vector<ProfRec> prof_pending;
+    std::vector<cudaEvent_t> ev_free;
+    double prof_ms = 0.0, prof_flops = 0.0;
+    long long prof_launches = 0;
+};
+Context &ctx();
+void require_init();
+inline void counted(int n = 1) { ctx().launches += n; }
+cudaEvent_t prof_event();
+// resolve pending profiled launches; iters_of(st) gives the Krylov dimension
+// reached by a state (launches at iteration k >= that were skipped)
+void prof_resolve(int (*iters_of)(const KrylovState *, void *), void *arg);
+
+// Stream-ordered device buffer (cudaMallocAsync on the library stream).
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    explicit DevBuf(size_t b) { alloc(b); }
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    DevBuf(DevBuf &&o) noexcept : p(o.p), bytes(o.bytes) { o.p = nullptr; o.bytes = 0; }
+    DevBuf &operator=(DevBuf &&o) noexcept {
+        if (this != &o) { release(); p = o.p; bytes = o.bytes; o.p = nullptr; o.bytes = 0; }
+        return *this;
+    }
+    ~DevBuf() { release(); }
+    void alloc(size_t b);
+    void release();
+    template <class T> T *as() const { return static_cast<T *>(p); }
+};
+
+// Upload a host vector into a fresh device buffer (async on the stream; the
+// host vector must stay alive until the stream reaches the copy -- callers
+// keep plans alive for that reason).
+template <class T>
+DevBuf upload_vec(const std::vector<T> &v) {
+    DevBuf b(std::max<size_t>(1, v.size()) * sizeof(T));
+    if (!v.empty())
+        KV_CUDA(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, ctx().stream));
+    return b;
+}
+
+// ------------------------------------------------------------ block tensors
+struct BlockMeta {
+    std::array<int, kMaxRank> shape{}, qn{};
+    int64_t off = 0;   // complex elements from the start of the tensor buffer
+    int64_t size = 0;  // complex elements
+};
+
+struct Meta {
+    int rank = 0;
+    std::array<int, kMaxRank> dirs{};
+    std::vector<BlockMeta> blocks;
+    int64_t nelem = 0;
+    void layout();  // contiguous offsets in block order
+    bool same_key(const BlockMeta &a, const BlockMeta &b) const {
+        for (int i = 0; i < rank; ++i)
+            if (a.shape[i] != b.shape[i] || a.qn[i] != b.qn[i]) return false;
+        return true;
+    }
+    int find(const BlockMeta &b) const {
+        for (size_t i = 0; i < blocks.size(); ++i)
+            if (same_key(blocks[i], b)) return (int)i;
+        return -1;
+    }
+};
+
+// A device tensor: host metadata + one contiguous complex128 device buffer.
+struct DTensor {
+    Meta meta;
+    DevBuf buf;
+    double2 *data() const { return buf.as<double2>(); }
+    static std::shared_ptr<DTensor> make(const Meta &m, bool zero);
+};
+using TensorP = std::shared_ptr<DTensor>;
+
+TensorP upload_tensor(int rank, const int *dirs, int nb, const int *shapes, const int *qns, const double *data);
+TensorP clone(const DTensor &t);
+void download_tensor(const DTensor &t, int *dirs, int *shapes, int *qns, double *data);
+
+// ------------------------------------------------------------ GEMM plans
+// One output tile of a grouped complex GEMM and the contributions summed into
+// it.  C[m, n] = alpha * sum_seg opA(A_seg)[m, k] opB(B_seg)[k, n].
+struct GemmSeg {
+    int64_t a_off, b_off;  // complex elements into the A / B buffers
+    int K, lda, ldb;
+    int opa;  // 0: A[m*lda + k]; 1: conj(A[k*lda + m])
+    int opb;  // 0: B[k*ldb + n]; 1: B[n*ldb + k]
+};
+struct GemmTile {
+    int64_t c_off;
+    int ldc, M, N, m0, n0;
+    int seg_begin, seg_end;
+};
+struct GemmPlan {
+    std::vector<GemmTile> tiles;
+    std::vector<GemmSeg> segs;
+    DevBuf d_tiles, d_segs;
+    double ref_flops = 0.0;  // sum of 8*M*N*K over the reference's zgemm pairs
+    int max_k = 0;
+    void upload() { d_tiles = upload_vec(tiles); d_segs = upload_vec(segs); }
+};
+
+// MPO mixing (env_mps_mpo family) with merging of equal output blocks.
+struct MixTerm {
+    int64_t in_off, w_off;
+    int K;  // contracted extent (w_l sector dim * sigma dim)
+};
+struct MixJob {
+    int64_t out_off, count;    // output block and its element count
+    int nk_unused, so, wr, rest;
+    int term_begin, term_end;
+};
+struct MixItem {  // a chunk of one job handled by one CTA
+    int job;
+    int64_t start;
+};
+struct MixPlan {
+    std::vector<MixTerm> terms;
+    std::vector<MixJob> jobs;
+    std::vector<MixItem> items;
+    DevBuf d_terms, d_jobs, d_items;
+    void upload() { d_terms = upload_vec(terms); d_jobs = upload_vec(jobs); d_items = upload_vec(items); }
+};
+
+// ------------------------------------------------------- kernel wrappers
+void launch_gemm_fp64(const GemmPlan &p, const double2 *A, const double2 *B, double2 *C, double alpha,
+                      const int *skip);
+// dispatch by precision; st/k identify a Lanczos apply for profiling
+void run_gemm(const GemmPlan &g, const double2 *A, const double2 *B, double2 *C, double alpha, int precision,
+              const int *skip, const KrylovState *st = nullptr, int k = -1);
+void launch_gemm_mixed(const GemmPlan &p, const double2 *A, const double2 *B, double2 *C, double alpha,
+                       const int *skip);
+void launch_mix(const MixPlan &p, const double2 *in, const double2 *W, double2 *out, const int *skip);
+void launch_permute(const double2 *in, double2 *out, const std::vector<int64_t> &desc, int nblocks);
+void launch_zero(double2 *p, int64_t n);
+void launch_copy(double2 *dst, const double2 *src, int64_t n);
+
+// Krylov (FP64) state kept on the device for one local_krylov call.  The
+// loop is launched without host synchronisation: every kernel of an
+// iteration returns immediately once `done` is set.
+constexpr int kMaxKrylov = 32;
+struct KrylovState {
+    double2 alpha[kMaxKrylov];  // overlap(V_k, hv) as the reference stores it
+    double2 beta[kMaxKrylov];   // overlap(V_{k-1}, hv): the upper off-diagonal
+    double err[kMaxKrylov + 1]; // running product of Lanczos norms, err[0] = 1
+    double2 coef[kMaxKrylov];   // c = Z exp(-+i Lambda) Z^H e0
+    double psi_norm;
+    int done;
+    int iters;                  // number of alphas (Krylov dimension)
+    int status;                 // KV_OK or KV_ENONFINITE
+};
+
+int reduce_parts();  // number of partial sums used by the vector kernels
+// v0 = psi / |psi|; resets the state (err[0] = 1)
+void krylov_start(KrylovState *st, const double2 *psi, double2 *v0, int64_t n, double2 *parts);
+// after hv = (dt/2) H v_k: Gram-Schmidt against v_{k-1} (k > 0) and v_k,
+// norm, stop test, v_{k+1} = hv / |hv|
+void krylov_step(KrylovState *st, int k, double2 *hv, const double2 *vprev, const double2 *vk, double2 *vnext,
+                 int64_t n, double2 *parts, double tol, int max_iter);
+// coefficients from the tridiagonal exponential, then out = sum_i c_i v_i
+void krylov_finish(KrylovState *st, double2 *const *dV, double2 *out, int64_t n, int reverse);
+// sum |x|^2 into a device double (deterministic)
+void vec_norm2(const double2 *x, int64_t n, double2 *parts, double *result);
+
+}  // namespace kv

@@ -1,0 +1,234 @@
+// FP64 Lanczos kernels for local_krylov (holstein/exponential.h:92-190).
+//
+// All Krylov vectors share one block layout, so overlaps and updates are flat
+// vector operations.  Reductions are two-level and deterministic: each kernel
+// writes one partial per CTA (fixed grid, fixed order) and the next kernel
+// reduces those partials in a fixed order before using the value, fused with
+// the update that needs it (classical Gram-Schmidt in the reference's order:
+// beta against v_{k-1} first, then alpha against v_k, then the norm).
+#include "kv_internal.h"
+#include "kv_jacobi.cuh"
+
+namespace kv {
+
+namespace {
+
+constexpr int KT = 256;
+
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+
+// conj(x) * y
+__device__ __forceinline__ double2 cdotc(double2 x, double2 y) {
+    return make_double2(x.x * y.x + x.y * y.y, x.x * y.y - x.y * y.x);
+}
+
+__device__ double2 block_sum(double2 v) {
+    __shared__ double2 red[KT / 32];
+    for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[w] = v;
+    __syncthreads();
+    double2 s = make_double2(0.0, 0.0);
+    if (threadIdx.x == 0)
+        for (int i = 0; i < KT / 32; ++i) s = cadd(s, red[i]);
+    __shared__ double2 out;
+    if (threadIdx.x == 0) out = s;
+    __syncthreads();
+    return out;
+}
+
+// every CTA reduces the same partial array in the same order
+__device__ double2 reduce_partials(const double2 *parts, int nparts) {
+    double2 v = make_double2(0.0, 0.0);
+    for (int i = threadIdx.x; i < nparts; i += KT) v = cadd(v, parts[i]);
+    return block_sum(v);
+}
+
+__global__ void __launch_bounds__(KT) k_norm_part(const double2 *x, int64_t n, double2 *parts) {
+    double s = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)KT + threadIdx.x; i < n; i += (int64_t)gridDim.x * KT)
+        s += x[i].x * x[i].x + x[i].y * x[i].y;
+    double2 r = block_sum(make_double2(s, 0.0));
+    if (threadIdx.x == 0) parts[blockIdx.x] = r;
+}
+
+__global__ void __launch_bounds__(KT) k_start(KrylovState *st, const double2 *psi, double2 *v0, int64_t n,
+                                              const double2 *parts, int nparts) {
+    const double nrm = sqrt(reduce_partials(parts, nparts).x);
+    const bool bad = !isfinite(nrm) || nrm == 0.0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        st->psi_norm = nrm;
+        st->err[0] = 1.0;
+        st->done = bad ? 1 : 0;
+        st->iters = 0;
+        st->status = bad ? KV_ENONFINITE : KV_OK;
+    }
+    const double inv = bad ? 0.0 : 1.0 / nrm;
+    for (int64_t i = blockIdx.x * (int64_t)KT + threadIdx.x; i < n; i += (int64_t)gridDim.x * KT)
+        v0[i] = make_double2(psi[i].x * inv, psi[i].y * inv);
+}
+
+// parts[b] = sum conj(x) y
+__global__ void __launch_bounds__(KT) k_dot_part(const KrylovState *st, const double2 *x, const double2 *y,
+                                                 int64_t n, double2 *parts) {
+    if (st->done) return;
+    double2 s = make_double2(0.0, 0.0);
+    for (int64_t i = blockIdx.x * (int64_t)KT + threadIdx.x; i < n; i += (int64_t)gridDim.x * KT)
+        s = cadd(s, cdotc(x[i], y[i]));
+    double2 r = block_sum(s);
+    if (threadIdx.x == 0) parts[blockIdx.x] = r;
+}
+
+// c = reduce(pin) (= overlap(v, hv) = <hv|v>);  hv -= c v;  pout[b] = sum conj(hv) w
+// (w == nullptr: pout[b] = sum |hv|^2).  slot receives c.
+__global__ void __launch_bounds__(KT) k_sub(KrylovState *st, double2 *hv, const double2 *v, const double2 *w,
+                                            int64_t n, const double2 *pin, double2 *pout, int nparts,
+                                            double2 *slot) {
+    if (st->done) return;
+    const double2 c = reduce_partials(pin, nparts);
+    if (blockIdx.x == 0 && threadIdx.x == 0) *slot = c;
+    double2 s = make_double2(0.0, 0.0);
+    for (int64_t i = blockIdx.x * (int64_t)KT + threadIdx.x; i < n; i += (int64_t)gridDim.x * KT) {
+        double2 h = hv[i], x = v[i];
+        h.x -= c.x * x.x - c.y * x.y;
+        h.y -= c.x * x.y + c.y * x.x;
+        hv[i] = h;
+        if (w) s = cadd(s, cdotc(h, w[i]));
+        else s.x += h.x * h.x + h.y * h.y;
+    }
+    double2 r = block_sum(s);
+    if (threadIdx.x == 0) pout[blockIdx.x] = r;
+}
+
+// nrm = sqrt(reduce(pin)); err[k+1] = err[k] nrm; stop test; vnext = hv / nrm
+__global__ void __launch_bounds__(KT) k_normalize(KrylovState *st, const double2 *hv, double2 *vnext, int64_t n,
+                                                  const double2 *pin, int nparts, int k, double tol, int max_iter) {
+    if (st->done) return;
+    const double nrm = sqrt(reduce_partials(pin, nparts).x);
+    const double e = st->err[k] * nrm;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        st->err[k + 1] = e;
+        if (!isfinite(nrm)) {
+            st->status = KV_ENONFINITE;
+            st->done = 1;
+            st->iters = k + 1;
+        } else if (e <= tol || k + 1 >= max_iter - 1) {
+            st->done = 1;
+            st->iters = k + 1;
+        }
+    }
+    if (!(nrm > 0.0) || !isfinite(nrm)) return;
+    const double inv = 1.0 / nrm;
+    for (int64_t i = blockIdx.x * (int64_t)KT + threadIdx.x; i < n; i += (int64_t)gridDim.x * KT)
+        vnext[i] = make_double2(hv[i].x * inv, hv[i].y * inv);
+}
+
+// T = tridiag(Re alpha, beta upper); c = Z exp(img Lambda) Z^H e0 with
+// img = -i (forward) or +i (reverse): holstein/exponential.h:163-183.
+__global__ void k_tridiag_exp(KrylovState *st, int reverse) {
+    __shared__ double H[2 * kMaxKrylov * kMaxKrylov];
+    __shared__ double Z[2 * kMaxKrylov * kMaxKrylov];
+    if (threadIdx.x != 0) return;
+    const int n = st->iters;
+    if (n <= 0) return;
+    for (int i = 0; i < 2 * n * n; ++i) H[i] = 0.0;
+    for (int i = 0; i < n; ++i) {
+        H[2 * (i * n + i)] = st->alpha[i].x;
+        if (i + 1 < n) {
+            H[2 * (i * n + i + 1)] = st->beta[i].x;
+            H[2 * (i * n + i + 1) + 1] = st->beta[i].y;
+            H[2 * ((i + 1) * n + i)] = st->beta[i].x;
+            H[2 * ((i + 1) * n + i) + 1] = -st->beta[i].y;
+        }
+    }
+    kvj::hermitian_jacobi<double>(n, H, Z, 60);
+    const double sg = reverse ? 1.0 : -1.0;
+    for (int i = 0; i < n; ++i) {
+        double cr = 0.0, ci = 0.0;
+        for (int j = 0; j < n; ++j) {
+            double lam = H[2 * (j * n + j)];
+            double er = cos(lam), ei = sg * sin(lam);              // exp(img lam)
+            double zr = Z[2 * (i * n + j)], zi = Z[2 * (i * n + j) + 1];
+            double z0r = Z[2 * j], z0i = -Z[2 * j + 1];             // conj(Z[0, j])
+            double pr = zr * er - zi * ei, pi = zr * ei + zi * er;
+            cr += pr * z0r - pi * z0i;
+            ci += pr * z0i + pi * z0r;
+        }
+        st->coef[i] = make_double2(cr, ci);
+    }
+}
+
+__global__ void __launch_bounds__(KT) k_combine(const KrylovState *st, double2 *const *V, double2 *out, int64_t n) {
+    const int m = st->iters;
+    for (int64_t i = blockIdx.x * (int64_t)KT + threadIdx.x; i < n; i += (int64_t)gridDim.x * KT) {
+        double2 acc = make_double2(0.0, 0.0);
+        for (int j = 0; j < m; ++j) {
+            const double2 c = st->coef[j], v = V[j][i];
+            acc.x += c.x * v.x - c.y * v.y;
+            acc.y += c.x * v.y + c.y * v.x;
+        }
+        out[i] = acc;
+    }
+}
+
+__global__ void k_store_norm2(const double2 *parts, int nparts, double *result) {
+    double2 s = reduce_partials(parts, nparts);
+    if (threadIdx.x == 0) *result = s.x;
+}
+
+}  // namespace
+
+int reduce_parts() { return std::max(1, std::min(512, 2 * ctx().num_sms)); }
+
+void krylov_start(KrylovState *st, const double2 *psi, double2 *v0, int64_t n, double2 *parts) {
+    const int np = reduce_parts();
+    k_norm_part<<<np, KT, 0, ctx().stream>>>(psi, n, parts);
+    counted();
+    k_start<<<np, KT, 0, ctx().stream>>>(st, psi, v0, n, parts, np);
+    counted();
+    KV_CUDA(cudaGetLastError());
+}
+
+void krylov_step(KrylovState *st, int k, double2 *hv, const double2 *vprev, const double2 *vk, double2 *vnext,
+                 int64_t n, double2 *parts, double tol, int max_iter) {
+    const int np = reduce_parts();
+    double2 *P0 = parts, *P1 = parts + np;
+    cudaStream_t s = ctx().stream;
+    if (k > 0) {
+        k_dot_part<<<np, KT, 0, s>>>(st, hv, vprev, n, P0);
+    counted();
+        k_sub<<<np, KT, 0, s>>>(st, hv, vprev, vk, n, P0, P1, np, &st->beta[k - 1]);
+    counted();
+    } else {
+        k_dot_part<<<np, KT, 0, s>>>(st, hv, vk, n, P1);
+    counted();
+    }
+    k_sub<<<np, KT, 0, s>>>(st, hv, vk, nullptr, n, P1, P0, np, &st->alpha[k]);
+    counted();
+    k_normalize<<<np, KT, 0, s>>>(st, hv, vnext, n, P0, np, k, tol, max_iter);
+    counted();
+    KV_CUDA(cudaGetLastError());
+}
+
+void krylov_finish(KrylovState *st, double2 *const *dV, double2 *out, int64_t n, int reverse) {
+    k_tridiag_exp<<<1, 32, 0, ctx().stream>>>(st, reverse);
+    counted();
+    k_combine<<<reduce_parts(), KT, 0, ctx().stream>>>(st, dV, out, n);
+    counted();
+    KV_CUDA(cudaGetLastError());
+}
+
+void vec_norm2(const double2 *x, int64_t n, double2 *parts, double *result) {
+    const int np = reduce_parts();
+    k_norm_part<<<np, KT, 0, ctx().stream>>>(x, n, parts);
+    counted();
+    k_store_norm2<<<1, KT, 0, ctx().stream>>>(parts, np, result);
+    counted();
+    KV_CUDA(cudaGetLastError());
+}
+
+}  // namespace kv

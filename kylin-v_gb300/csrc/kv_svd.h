@@ -1,0 +1,42 @@
+// Block SVD plan structures shared by the host planner (kv_engine.cu) and the
+// device kernels (kv_svd.cu).
+#pragma once
+#include "kv_internal.h"
+
+namespace kv {
+
+struct SvdSector {
+    int64_t t_off;  // T (p x q, column-major) and its sorted U copy
+    int64_t v_off;  // V (q x q, column-major) and its sorted copy
+    int64_t s_off;  // q singular values
+    int p, q;       // tall orientation, p >= q
+    int transposed; // 0: T = A (m = p, n = q); 1: T = A^H (m = q, n = p)
+    int m, n;       // sector matrix of A (rows x cols)
+};
+
+struct SvdGather {  // one block of A into its sector matrix
+    int64_t blk_off;
+    int sector, row_off, col_off, nrows, ncols;
+};
+
+struct SvdScatter {  // one output block of U (side 0) or S.V^H / V^H (side 1)
+    int64_t out_off;
+    int sector, side, pos, len, kept, scale_s;
+};
+
+struct SvdPlan {
+    std::vector<SvdSector> secs;
+    std::vector<SvdGather> gathers;
+    int64_t t_elems = 0, v_elems = 0, s_elems = 0;
+    int max_q = 0;
+    DevBuf d_secs, d_gathers;
+    void upload() { d_secs = upload_vec(secs); d_gathers = upload_vec(gathers); }
+};
+
+void svd_gather(const SvdPlan &p, const double2 *A, double2 *T);
+void svd_jacobi(const SvdPlan &p, double2 *T, double2 *V, int *status, int max_sweeps, double tol);
+void svd_finalize(const SvdPlan &p, const double2 *T, const double2 *V, double2 *Us, double2 *Vs, double *S);
+void svd_scatter(const std::vector<SvdScatter> &sc, const SvdPlan &p, const double2 *Us, const double2 *Vs,
+                 const double *S, double2 *out);
+
+}  // namespace kv

@@ -143,10 +143,14 @@ Tensor transpose(const Tensor &t, const std::vector<int> &ax) {
     return r;
 }
 
+// algorithmic flop counter: 8*M*N*K per complex GEMM the reference issues
+double g_flops = 0.0;
+
 // row-major complex GEMM with the reference's zdot conventions
 // (util/allocation.h:186-205)
 void zdot(const cplx *a, const cplx *b, int m, int n, int k, cplx *c, Op ta, Op tb) {
     const cplx one(1.0, 0.0), zero(0.0, 0.0);
+    g_flops += 8.0 * m * (double)n * k;
     int lda = (ta == OP_N) ? k : m;
     int ldb = (tb == OP_N) ? n : k;
     scipy_cblas_zgemm(kRowMajor, ta, tb, m, n, k, &one, a, lda, b, ldb, &zero, c, n);
@@ -620,6 +624,13 @@ int guarded(F &&f) {
 extern "C" {
 
 const char *kvo_last_error() { return g_err.c_str(); }
+
+// complex-GEMM flops (8*M*N*K) issued since the last reset
+double kvo_flops(int reset) {
+    double f = g_flops;
+    if (reset) g_flops = 0.0;
+    return f;
+}
 
 int kvo_tensor_new(int rank, const int *dirs, int nblocks, const int *shapes, const int *qns,
                    const double *data, void **out) {

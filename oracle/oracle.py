@@ -53,6 +53,8 @@ def lib():
         L.kvo_tdvp_site.argtypes = [vp, ctypes.c_int, ctypes.POINTER(vp)]
         L.kvo_tdvp_free.argtypes = [vp]
         L.kvo_tdvp_free.restype = None
+        L.kvo_flops.argtypes = [ctypes.c_int]
+        L.kvo_flops.restype = ctypes.c_double
         L.kvo_join.argtypes = [ctypes.c_int, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp), dp, dp]
         _lib = L
     return _lib
@@ -189,6 +191,11 @@ class Tdvp:
         if getattr(self, "ptr", None) and _lib is not None:
             _lib.kvo_tdvp_free(self.ptr)
             self.ptr = None
+
+
+def flops(reset=True) -> float:
+    """Complex-GEMM flops (8*M*N*K, the reference's zgemm calls) since the last reset."""
+    return lib().kvo_flops(int(reset))
 
 
 def join(a, w, b) -> complex:
