@@ -1,0 +1,344 @@
+#!/usr/bin/env python3
+"""Benchmark of the Holstein TDVP hot path (one JSON line on rank 0).
+
+A step is one TDVP time step (a full left-to-right plus right-to-left sweep)
+of the configured chain.  Default workload ``holstein-2site-L32``: 32
+molecules x 2 modes (omega 0.2 / 1.2, g 0.5 / 1.0), phonon cutoff 16, J = -1,
+N_ex = 1 charge sectors, seeded random MPS at D = 128, two-site TDVP with
+dt = 0.05, Krylov maxIter 11 (dimension <= 10), tolExp 1e-8, SVD cutoff 1e-8.
+Inputs are synthetic: a seeded random right-canonical U(1) MPS and the
+Holstein Hamiltonian as an MPO, generated on the host.
+
+value      algorithmic TFLOP/s: 8*M*N*K summed over every complex GEMM the
+           reference algorithm issues in the timed sweeps (Lanczos iterations
+           as actually run), divided by the device time of those sweeps
+           (CUDA events on the library's stream), MPS and environments already
+           resident in HBM; L2 is flushed between steps.
+e2e        the same metric through the public C ABI with host buffers: every
+           step uploads the MPS and MPO from pinned host memory, builds the
+           environments, sweeps and downloads the MPS.
+roofline   grouped block-sparse GEMM (the dominant kernel): reference flops
+           of its block pairs / its event-timed duration, against the TF32
+           dense tensor peak (half the measured bf16 peak).
+cpu_baseline  the CPU oracle (restatement of the reference on OpenBLAS, all
+           host threads) on a 3-molecule chain of the same local structure.
+
+--impl reference  runs only the CPU oracle (rank 0) and prints its line.
+N > 1 (torchrun): each rank evolves its own replica chain (a single chain's
+sweep is sequential), value = total flops / max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+METRIC = "TDVP sweep s & H_eff TFLOP/s, mixed vs plain FP64 on GB300 at <=1e-6 pop err"
+CPU_SAMPLE_MOL = 3
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="holstein-2site-L32")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-compare", action="store_true", help="skip the mixed-vs-FP64 comparison leg")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    return ap.parse_args()
+
+
+def dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampler running during the timed region."""
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r for r in csv.reader(io.StringIO(self.f.read())) if len(r) >= 9]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip() == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["bf16_tflops"]), float(d["hbm_gbs"]), "measured"
+    return 1900.0, 6800.0, "fallback"
+
+
+def traffic_per_launch(config: str):
+    """DRAM bytes per grouped-GEMM launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", f"k_gemm_tc_{config}.md")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for line in f:
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
+    return None
+
+
+def build_workload(config: str, seed: int, n_mol: int | None = None):
+    import __graft_entry__ as ge
+
+    ge.load_package()
+    from kylin_v_gb300 import holstein as H
+
+    chain, D, d = H.config_chain(config)
+    if n_mol is not None:
+        chain = H.HolsteinChain(n_mol, chain.omega, chain.g[:n_mol], chain.cutoff, chain.J, chain.eps[:n_mol])
+    return chain, D, d, H.random_mps(chain, D, seed=seed), H.hamiltonian_mpo(chain)
+
+
+def cpu_baseline(config: str, sweeps: int = 1, warm: int = 0):
+    """The CPU oracle (reference restatement, OpenBLAS on all host threads)."""
+    cores = os.cpu_count() or 1
+    os.environ["OPENBLAS_NUM_THREADS"] = str(cores)
+    chain, D, d, mps, mpo = build_workload(config, 1234, n_mol=CPU_SAMPLE_MOL)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O  # CPU baseline leg only
+
+    t = O.Tdvp(mps, mpo, d["tol_svd"], d["tol_exp"], D, d["max_iter"], d["dt"])
+    for _ in range(warm):
+        t.sweep(d["mode"])
+    O.flops(True)
+    times = []
+    for _ in range(sweeps):
+        t0 = time.perf_counter()
+        t.sweep(d["mode"])
+        times.append(time.perf_counter() - t0)
+    f = O.flops(True)
+    tot = sum(times)
+    return {"value": f / tot / 1e12, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+            "sample": f"{sweeps} time step(s) of a {CPU_SAMPLE_MOL}-molecule chain ({chain.n_sites} sites) with the "
+                      f"same modes, cutoff, D and tolerances ({f / 1e9:.1f} GFLOP in {tot:.1f} s)",
+            "ms_per_step": 1e3 * tot / sweeps}
+
+
+def run_reference(args):
+    ws, rank, _ = dist()
+    if rank != 0:
+        return
+    _, _, d, _, _ = build_workload(args.config, 1234, n_mol=1)
+    cb = cpu_baseline(args.config, sweeps=args.steps, warm=args.warmup)
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "TFLOP/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": cb["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": {"workload": args.config, "sample_molecules": CPU_SAMPLE_MOL},
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": cb["value"], "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    ws, rank, local = dist()
+    import numpy as np
+    import torch
+
+    import __graft_entry__ as ge
+
+    ge.load_package()
+    from kylin_v_gb300 import kvgpu as G
+
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as tdist
+
+        tdist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    G.init(local)
+    prec = G.KV_MIXED_TF32 if args.precision == "mixed" else G.KV_FP64
+    chain, D, d, mps, mpo = build_workload(args.config, 1234 + rank)
+    mode = d["mode"]
+    t = G.TDVP(mps, mpo, d["tol_svd"], d["tol_exp"], D, d["max_iter"], d["dt"], prec)
+    sweep = t.two_site if mode == 2 else t.one_site
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > L2 (129 MB)
+    for _ in range(args.warmup):
+        sweep()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+
+    dev_ms, flops, gemm_flops = 0.0, 0.0, 0.0
+    modules = {}
+    barrier()
+    n0 = G.launches()
+    G.profile(True)
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            sweep()
+            st = t.stats()
+            dev_ms += st["sweep_ms"]
+            flops += st["ref_flops"]
+            gemm_flops += st["gemm_ref_flops"]
+            for k, v in st["modules_ms"].items():
+                modules[k] = modules.get(k, 0.0) + v
+    barrier()
+    prof = G.profile_read()
+    G.profile(False)
+    launches = G.launches() - n0
+    clocks = clk.summary()
+    tot_flops, max_ms = flops, dev_ms
+    if ws > 1:
+        x = torch.tensor([flops, dev_ms], dtype=torch.float64, device="cuda")
+        y = x.clone()
+        torch.distributed.all_reduce(x[:1], op=torch.distributed.ReduceOp.SUM)
+        torch.distributed.all_reduce(y[1:], op=torch.distributed.ReduceOp.MAX)
+        tot_flops, max_ms = float(x[0]), float(y[1])
+    value = tot_flops / (max_ms / 1e3) / 1e12
+
+    # ---- end to end through the public API with pinned host buffers
+    e2e = None
+    steps_e2e = max(1, min(args.steps, 2))
+    host = []
+    for tns in mps + mpo:
+        data = np.concatenate([a.ravel() for _, a in tns.blocks]).astype(np.complex128)
+        pin = torch.from_numpy(data.view(np.float64)).pin_memory()
+        host.append((tns, pin))
+    h2d = sum(p.numel() * 8 for _, p in host)
+    d2h = sum(a.size * 16 for tns in mps for _, a in tns.blocks)
+    barrier()
+    t0 = time.perf_counter()
+    e2e_flops = 0.0
+    for _ in range(steps_e2e):
+        dev = []
+        for tns, pin in host:
+            dev.append(G.Tensor.from_pinned(tns, pin.data_ptr()))
+        te = G.TDVP(dev[:len(mps)], dev[len(mps):], d["tol_svd"], d["tol_exp"], D, d["max_iter"], d["dt"], prec)
+        te.two_site() if mode == 2 else te.one_site()
+        e2e_flops += te.stats()["ref_flops"]
+        out = te.sites()
+        _ = [s.to_host() for s in out]
+        del te
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": e2e_flops / e2e_s / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h), "steps": steps_e2e}
+
+    if rank != 0:
+        return
+    bf16, hbm, src = peaks()
+    tf32_peak = bf16 / 2.0
+    achieved = prof["gemm_ref_flops"] / max(1e-9, prof["gemm_ms"]) / 1e9  # TFLOP/s
+    per_launch = prof["gemm_ref_flops"] / max(1, prof["gemm_launches"])
+    tr = traffic_per_launch(args.config)
+    line = {
+        "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "c64 3M TF32x3 contractions + c128 Lanczos/SVD polish" if prec else "c128",
+        "data": "synthetic (seeded random right-canonical U(1) MPS, Holstein FSM MPO)",
+        "config": {"workload": args.config, "n_sites": chain.n_sites, "D": D, "mode": f"{mode}-site TDVP",
+                   "dt": d["dt"], "max_iter": d["max_iter"], "precision": args.precision, "l2_flush": True,
+                   "replicas_per_gpu": 1},
+        "modules_ms_per_step": {k: v / args.steps for k, v in modules.items()},
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": tf32_peak, "unit": "TFLOP/s",
+                     "frac": achieved / tf32_peak, "traffic": tr,
+                     "kernel": "k_gemm_tc" if prec else "k_gemm_fp64",
+                     "flops_per_launch": per_launch, "launches": prof["gemm_launches"],
+                     "peak_source": f"TF32 dense = bf16/2 of {src} ({bf16:.1f} TFLOP/s bf16)"},
+        "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
+    }
+    if not args.no_compare:
+        line["fp64_compare"] = compare_fp64(args, G)
+    if not args.no_cpu:
+        line["cpu_baseline"] = {k: v for k, v in cpu_baseline(args.config).items() if k != "ms_per_step"}
+    print(json.dumps(line), flush=True)
+
+
+def compare_fp64(args, G):
+    """Mixed vs plain FP64 GPU path on a 4-molecule chain of the same local
+    structure: time per step and max population / energy error over 3 steps."""
+    import numpy as np
+
+    import __graft_entry__ as ge
+
+    ge.load_package()
+    from kylin_v_gb300 import holstein as H
+
+    chain, D, d, mps, mpo = build_workload(args.config, 1234, n_mol=4)
+    dens = [[G.Tensor.from_host(x) for x in H.density_mpo(chain, j)] for j in chain.exciton_sites()]
+    hm = [G.Tensor.from_host(x) for x in mpo]
+    runs = {p: G.TDVP(mps, mpo, d["tol_svd"], d["tol_exp"], D, d["max_iter"], d["dt"], p)
+            for p in (G.KV_FP64, G.KV_MIXED_TF32)}
+    ms = {p: 0.0 for p in runs}
+    perr = eerr = 0.0
+    nsteps = 3
+    for _ in range(nsteps):
+        obs = {}
+        for p, t in runs.items():
+            t.two_site() if d["mode"] == 2 else t.one_site()
+            ms[p] += t.stats()["sweep_ms"]
+            s = t.sites()
+            obs[p] = (np.array([G.expectation(s, x, s).real for x in dens]), G.expectation(s, hm, s).real)
+        perr = max(perr, float(np.abs(obs[G.KV_FP64][0] - obs[G.KV_MIXED_TF32][0]).max()))
+        eerr = max(eerr, abs(obs[G.KV_FP64][1] - obs[G.KV_MIXED_TF32][1]))
+    return {"sample": f"4-molecule chain ({chain.n_sites} sites), {nsteps} steps", "fp64_ms_per_step": ms[G.KV_FP64] / nsteps,
+            "mixed_ms_per_step": ms[G.KV_MIXED_TF32] / nsteps,
+            "speedup_mixed_vs_fp64": ms[G.KV_FP64] / max(1e-9, ms[G.KV_MIXED_TF32]),
+            "max_pop_err": perr, "max_energy_err": eerr}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

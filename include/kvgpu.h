@@ -48,6 +48,11 @@ extern "C" {
  *   exponential, MPO mixing and SVD stay FP64. */
 #define KV_FP64        0
 #define KV_MIXED_TF32  1
+/* one part mixed, the other FP64 (to attribute mixed-precision error):
+ * KV_MIXED_GEMM = tensor-core contractions + FP64 SVD,
+ * KV_MIXED_SVD  = FP64 contractions + mixed SVD */
+#define KV_MIXED_GEMM  2
+#define KV_MIXED_SVD   3
 
 /* contraction operand modes (numerically the CBLAS ones the reference uses) */
 #define KV_OP_N 111
@@ -102,9 +107,13 @@ int kv_lanczos_expm(int nsite, kv_tensor L, kv_tensor psi, kv_tensor W1, kv_tens
 /* svd_impl<R1,R2>(A, cfg, -1) (holstein/svd.h:296-440): block SVD per charge
  * sector with the reference's global truncation (keep while index < max_dim
  * and s > tol, never fewer than one).  l2r folds S into V (S.Vt), else into U.
- * n_kept / n_total receive the kept and total singular-value counts. */
-int kv_svd_truncate(kv_tensor A, int r1, int l2r, double tol, int max_dim, kv_tensor *U, kv_tensor *V,
-                    int *n_kept, int *n_total);
+ * n_kept / n_total receive the kept and total singular-value counts.
+ * KV_FP64: FP64 one-sided Jacobi.  KV_MIXED_TF32: FP32 one-sided Jacobi
+ * chooses the kept subspace and the truncation, then the kept factor is made
+ * orthonormal in FP64 (Cholesky-QR) and the other factor is the exact FP64
+ * projection of the sector matrix onto it. */
+int kv_svd_truncate(kv_tensor A, int r1, int l2r, double tol, int max_dim, int precision, kv_tensor *U,
+                    kv_tensor *V, int *n_kept, int *n_total);
 
 /* ---------------------------------------------------- sweep driver */
 /* TDVP(State, Operator, tolSVD, tolExp, maxDim, maxIter, dt) followed by the

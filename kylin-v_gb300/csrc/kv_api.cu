@@ -45,7 +45,11 @@ kv_tensor wrap(kv::TensorP t) {
     return h;
 }
 
-void sync() { KV_CUDA(cudaStreamSynchronize(kv::ctx().stream)); }
+void sync() {
+    KV_CUDA(cudaStreamSynchronize(kv::ctx().stream));
+    const int st = kv::mixed_gemm_status();
+    KV_REQUIRE(st == KV_OK, st, "a tensor-core GEMM wait timed out");
+}
 }  // namespace
 
 extern "C" {
@@ -69,6 +73,9 @@ int kv_init(int device) {
         KV_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
         uint64_t thr = ~0ull;  // keep freed blocks cached in the pool
         KV_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+        KV_CUDA(cudaHostAlloc((void **)&c.ring, (size_t)kv::Context::kRingChunks * kv::Context::kRingChunk,
+                              cudaHostAllocDefault));
+        for (auto &e : c.ring_ev) KV_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         c.device = device;
     });
 }
@@ -78,6 +85,12 @@ int kv_shutdown(void) {
         auto &c = kv::ctx();
         if (c.device < 0) return;
         KV_CUDA(cudaStreamSynchronize(c.stream));
+        kv::clear_plan_cache();
+        for (auto &e : c.ring_ev) cudaEventDestroy(e);
+        cudaFreeHost(c.ring);
+        c.ring = nullptr;
+        for (auto &e : c.ev_free) cudaEventDestroy(e);
+        c.ev_free.clear();
         KV_CUDA(cudaStreamDestroy(c.stream));
         c.stream = nullptr;
         c.device = -1;
@@ -161,11 +174,12 @@ int kv_lanczos_expm(int nsite, kv_tensor L, kv_tensor psi, kv_tensor W1, kv_tens
     });
 }
 
-int kv_svd_truncate(kv_tensor A, int r1, int l2r, double tol, int max_dim, kv_tensor *U, kv_tensor *V, int *n_kept,
-                    int *n_total) {
+int kv_svd_truncate(kv_tensor A, int r1, int l2r, double tol, int max_dim, int precision, kv_tensor *U, kv_tensor *V,
+                    int *n_kept, int *n_total) {
     return guard([&] {
         kv::require_init();
-        kv::SvdOut r = kv::op_svd(*T(A), r1, l2r != 0, tol, max_dim);
+        KV_REQUIRE(precision >= KV_FP64 && precision <= KV_MIXED_SVD, KV_EINVAL, "unknown precision mode");
+        kv::SvdOut r = kv::op_svd(*T(A), r1, l2r != 0, tol, max_dim, precision);
         sync();
         *U = wrap(r.U);
         *V = wrap(r.V);

@@ -11,6 +11,7 @@
 #include <cstring>
 #include <map>
 #include <numeric>
+#include <string>
 
 #include "kv_engine.h"
 #include "kv_svd.h"
@@ -38,14 +39,40 @@ void DevBuf::release() {
     }
 }
 
+void upload_bytes(void *dst, const void *src, size_t n) {
+    auto &c = ctx();
+    if (!c.ring || n > Context::kRingChunk) {
+        KV_CUDA(cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, c.stream));
+        KV_CUDA(cudaStreamSynchronize(c.stream));  // pageable source: keep the copy safe
+        return;
+    }
+    if (c.ring_used + n > Context::kRingChunk) {
+        // leave the chunk: fence its copies, move on, wait for the next chunk's old copies
+        KV_CUDA(cudaEventRecord(c.ring_ev[c.ring_cur], c.stream));
+        c.ring_live[c.ring_cur] = true;
+        c.ring_cur = (c.ring_cur + 1) % Context::kRingChunks;
+        c.ring_used = 0;
+        if (c.ring_live[c.ring_cur]) KV_CUDA(cudaEventSynchronize(c.ring_ev[c.ring_cur]));
+        c.ring_live[c.ring_cur] = false;
+    }
+    char *stage = c.ring + (size_t)c.ring_cur * Context::kRingChunk + c.ring_used;
+    std::memcpy(stage, src, n);
+    c.ring_used += (n + 255) & ~size_t(255);
+    KV_CUDA(cudaMemcpyAsync(dst, stage, n, cudaMemcpyHostToDevice, c.stream));
+}
+
 void Meta::layout() {
     int64_t off = 0;
-    for (auto &b : blocks) {
+    index.clear();
+    index.reserve(blocks.size() * 2);
+    for (size_t j = 0; j < blocks.size(); ++j) {
+        auto &b = blocks[j];
         int64_t s = 1;
         for (int i = 0; i < rank; ++i) s *= b.shape[i];
         b.size = s;
         b.off = off;
         off += s;
+        index.emplace(leg_key(b, 0, rank), (int)j);
     }
     nelem = off;
 }
@@ -136,15 +163,18 @@ ProductPlan plan_product(const Meta &A, const Meta &B, int nc, int opA, int opB)
                    "contracted legs' directions mismatch");
     std::vector<std::vector<GemmSeg>> per_out;
     std::vector<std::pair<int, int>> mn;  // M, N per output block
-    // index B blocks by the charges of their contracted legs for fast matching
+    // B blocks by (shape, charge) of their contracted legs, in block order
+    std::unordered_map<LegKey, std::vector<int>, LegKeyHash> bidx;
+    for (size_t j = 0; j < B.blocks.size(); ++j) bidx[leg_key(B.blocks[j], iax2, iax2 + nc)].push_back((int)j);
+    P.out.index.reserve(A.blocks.size() * 4);
     for (size_t i = 0; i < A.blocks.size(); ++i) {
         const BlockMeta &a = A.blocks[i];
-        for (size_t j = 0; j < B.blocks.size(); ++j) {
+        LegKey ka = leg_key(a, iax1, iax1 + nc);
+        // leg_key packs legs from position 0, so keys of A's and B's contracted legs compare directly
+        auto it = bidx.find(ka);
+        if (it == bidx.end()) continue;
+        for (int j : it->second) {
             const BlockMeta &b = B.blocks[j];
-            bool match = true;
-            for (int ax = 0; ax < nc && match; ++ax)
-                match = a.shape[iax1 + ax] == b.shape[iax2 + ax] && a.qn[iax1 + ax] == b.qn[iax2 + ax];
-            if (!match) continue;
             BlockMeta o;
             int nrow = 1, ncol = 1;
             for (int u = 0; u < n1 - nc; ++u) {
@@ -160,22 +190,21 @@ ProductPlan plan_product(const Meta &A, const Meta &B, int nc, int opA, int opB)
                 ncol *= b.shape[src];
             }
             const int nk = (int)(prod_range(a, 0, n1) / nrow);
-            int pos = P.out.find(o);
-            if (pos < 0) {
-                pos = (int)P.out.blocks.size();
-                P.out.blocks.push_back(o);
+            const int before = (int)P.out.blocks.size();
+            const int pos = P.out.add(o);
+            if (pos == before) {
                 per_out.emplace_back();
                 mn.push_back({nrow, ncol});
             }
-            GemmSeg s;
-            s.a_off = a.off;
-            s.b_off = b.off;
-            s.K = nk;
-            s.opa = (opA == KV_OP_N) ? 0 : 1;
-            s.opb = (opB == KV_OP_N) ? 0 : 1;
-            s.lda = (opA == KV_OP_N) ? nk : nrow;
-            s.ldb = (opB == KV_OP_N) ? ncol : nk;
-            per_out[pos].push_back(s);
+            GemmSeg sg;
+            sg.a_off = a.off;
+            sg.b_off = b.off;
+            sg.K = nk;
+            sg.opa = (opA == KV_OP_N) ? 0 : 1;
+            sg.opb = (opB == KV_OP_N) ? 0 : 1;
+            sg.lda = (opA == KV_OP_N) ? nk : nrow;
+            sg.ldb = (opB == KV_OP_N) ? ncol : nk;
+            per_out[pos].push_back(sg);
             P.gemm.ref_flops += 8.0 * nrow * (double)ncol * nk;
             P.gemm.max_k = std::max(P.gemm.max_k, nk);
         }
@@ -213,19 +242,29 @@ static std::vector<int64_t> own_offsets(const Meta &m) {
     return o;
 }
 
-// Reference flop count of a product<> on a given (unmerged) operand structure.
-double ref_product_flops(const Meta &A, const Meta &B, int nc, int opA, int opB) {
+// Reference flop count of a product<> whose A operand block i stands for
+// multA[i] identical blocks of the reference (unmerged MPO-mixing output).
+double ref_product_flops(const Meta &A, const Meta &B, int nc, int opA, int opB, const std::vector<double> *multA,
+                         const std::vector<double> *multB) {
     const int n1 = A.rank, n2 = B.rank;
     const int iax1 = (opA == KV_OP_N) ? n1 - nc : 0;
     const int iax2 = (opB == KV_OP_N) ? 0 : n2 - nc;
+    std::unordered_map<LegKey, double, LegKeyHash> bsum;  // sum of uncontracted sizes of B per key
+    for (size_t bi = 0; bi < B.blocks.size(); ++bi) {
+        const BlockMeta &b = B.blocks[bi];
+        int64_t sz = 1;
+        for (int i = 0; i < n2; ++i) sz *= b.shape[i];
+        bsum[leg_key(b, iax2, iax2 + nc)] += (multB ? (*multB)[bi] : 1.0) * (double)(sz / prod_range(b, iax2, iax2 + nc));
+    }
     double f = 0.0;
-    for (auto &a : A.blocks)
-        for (auto &b : B.blocks) {
-            bool match = true;
-            for (int ax = 0; ax < nc && match; ++ax)
-                match = a.shape[iax1 + ax] == b.shape[iax2 + ax] && a.qn[iax1 + ax] == b.qn[iax2 + ax];
-            if (match) f += 8.0 * (double)a.size * (double)(b.size / prod_range(b, iax2, iax2 + nc));
-        }
+    for (size_t ai = 0; ai < A.blocks.size(); ++ai) {
+        const BlockMeta &a = A.blocks[ai];
+        auto it = bsum.find(leg_key(a, iax1, iax1 + nc));
+        if (it == bsum.end()) continue;
+        int64_t sz = 1;
+        for (int i = 0; i < n1; ++i) sz *= a.shape[i];
+        f += (multA ? (*multA)[ai] : 1.0) * 8.0 * (double)sz * it->second;
+    }
     return f;
 }
 
@@ -234,41 +273,44 @@ double ref_product_flops(const Meta &A, const Meta &B, int nc, int opA, int opB)
 // legs lead, lead+1 of lm (w_l, sigma) contract with legs 1, 2 of W; W's legs
 // 0, 3 (sigma', w_r) replace them.  Equal output blocks are merged here (the
 // reference keeps them apart and the following product<> sums them).
-MixPlanFull plan_mix(const Meta &lm, const Meta &W, int lead) {
+MixPlanFull plan_mix(const Meta &lm, const Meta &W, int lead, const std::vector<double> *mult_in) {
     MixPlanFull R;
     R.out.rank = lm.rank;
     R.out.dirs = lm.dirs;
     R.out.dirs[lead] = W.dirs[0];
     R.out.dirs[lead + 1] = W.dirs[3];
-    R.unmerged = R.out;
     std::vector<std::vector<MixTerm>> terms;
     std::vector<std::array<int, 3>> geo;  // so, wr, rest
-    for (auto &a : lm.blocks)
-        for (auto &w : W.blocks) {
-            if (!(a.shape[lead] == w.shape[1] && a.shape[lead + 1] == w.shape[2] && a.qn[lead] == w.qn[1] &&
-                  a.qn[lead + 1] == w.qn[2]))
-                continue;
+    std::unordered_map<LegKey, std::vector<int>, LegKeyHash> widx;
+    for (size_t j = 0; j < W.blocks.size(); ++j) widx[leg_key(W.blocks[j], 1, 3)].push_back((int)j);
+    for (size_t ai = 0; ai < lm.blocks.size(); ++ai) {
+        const BlockMeta &a = lm.blocks[ai];
+        const double mi = mult_in ? (*mult_in)[ai] : 1.0;
+        auto wit = widx.find(leg_key(a, lead, lead + 2));
+        if (wit == widx.end()) continue;
+        for (int wj : wit->second) {
+            const BlockMeta &w = W.blocks[wj];
             BlockMeta o = a;
             o.shape[lead] = w.shape[0];
             o.qn[lead] = w.qn[0];
             o.shape[lead + 1] = w.shape[3];
             o.qn[lead + 1] = w.qn[3];
-            R.unmerged.blocks.push_back(o);
-            int pos = R.out.find(o);
             const int rest = (int)prod_range(a, lead + 2, lm.rank);
-            if (pos < 0) {
-                pos = (int)R.out.blocks.size();
-                R.out.blocks.push_back(o);
+            const int before = (int)R.out.blocks.size();
+            const int pos = R.out.add(o);
+            if (pos == before) {
                 terms.emplace_back();
                 geo.push_back({w.shape[0], w.shape[3], rest});
+                R.mult.push_back(0.0);
             }
+            R.mult[pos] += mi;  // the reference keeps each matched pair as its own block
             const int K = a.shape[lead] * a.shape[lead + 1];
             terms[pos].push_back({a.off, w.off, K});
             const double nk = (double)prod_range(a, 0, lead);
-            R.ref_flops += 8.0 * nk * w.shape[0] * (double)w.shape[3] * rest * K;
+            R.ref_flops += mi * 8.0 * nk * w.shape[0] * (double)w.shape[3] * rest * K;
         }
+    }
     R.out.layout();
-    R.unmerged.layout();
     for (size_t b = 0; b < R.out.blocks.size(); ++b) {
         MixJob j;
         j.out_off = R.out.blocks[b].off;
@@ -317,12 +359,13 @@ void prof_resolve(int (*iters_of)(const KrylovState *, void *), void *arg) {
 }
 
 void run_gemm(const GemmPlan &g, const double2 *A, const double2 *B, double2 *C, double alpha, int precision,
-              const int *skip, const KrylovState *st, int k) {
+              const int *skip, const KrylovState *st, int k, double credit_flops) {
+    precision = gemm_mixed(precision) ? KV_MIXED_TF32 : KV_FP64;
     if (g.tiles.empty()) return;
     auto &c = ctx();
     ProfRec rec{};
     if (c.prof) {
-        rec = {prof_event(), prof_event(), g.ref_flops, st, k};
+        rec = {prof_event(), prof_event(), credit_flops >= 0.0 ? credit_flops : g.ref_flops, st, k};
         KV_CUDA(cudaEventRecord(rec.a, c.stream));
     }
     if (precision == KV_FP64) launch_gemm_fp64(g, A, B, C, alpha, skip);
@@ -335,7 +378,7 @@ void run_gemm(const GemmPlan &g, const double2 *A, const double2 *B, double2 *C,
 }
 
 static void check_precision(int precision) {
-    KV_REQUIRE(precision == KV_FP64 || precision == KV_MIXED_TF32, KV_EINVAL, "unknown precision mode");
+    KV_REQUIRE(precision >= KV_FP64 && precision <= KV_MIXED_SVD, KV_EINVAL, "unknown precision mode");
 }
 
 // =========================================================== operations
@@ -351,27 +394,55 @@ TensorP op_product(const DTensor &A, const DTensor &B, int nc, int opA, int opB,
 }
 
 // --------------------------------------------------------- H_eff plans
+// Reference flops of one H_eff application on input structure S, split into
+// product<> pairs and MPO-mixing zgemms, and the output block set.
+static Flops heff_ref_flops(int nsite, const Meta &L, const Meta &S, const Meta *W1, const Meta *W2, const Meta &R,
+                            Meta *out_blocks) {
+    Flops f;
+    ProductPlan P1 = plan_product(L, S, 1, KV_OP_N, KV_OP_N);
+    f.gemm += P1.gemm.ref_flops;
+    Meta merged = P1.out;
+    std::vector<double> mult(P1.out.blocks.size(), 1.0);
+    const Meta *Ws[2] = {W1, W2};
+    for (int st = 0; st < nsite; ++st) {
+        MixPlanFull m = plan_mix(merged, *Ws[st], st + 1, &mult);
+        f.mix += m.ref_flops;
+        merged = std::move(m.out);
+        mult = std::move(m.mult);
+    }
+    f.gemm += ref_product_flops(merged, R, 2, KV_OP_N, KV_OP_T, &mult, nullptr);
+    if (out_blocks) *out_blocks = plan_product(merged, R, 2, KV_OP_N, KV_OP_T).out;
+    return f;
+}
+
 // Krylov layout: the closure of psi's blocks under H_eff (union of input and
 // output block sets until stable), so every Lanczos vector and H_eff . v share
-// one layout; blocks absent from the reference's tensors are zero.
+// one layout; blocks absent from the reference's tensors are zero.  The
+// reference's vectors grow towards that closure one application at a time
+// (hv += V_{k-1} beta, V_k alpha merge block sets, holstein/exponential.h:126-137);
+// iter_flops[k] replays that growth so only the block pairs the reference
+// multiplies at iteration k are credited.
 HeffPlan plan_heff(int nsite, const Meta &L, const Meta &psi, const Meta *W1, const Meta *W2, const Meta &R,
-                   int precision) {
+                   int precision, int max_iter) {
     HeffPlan H;
     H.nsite = nsite;
     Meta K = psi;
     K.layout();
-    for (int iter = 0; iter < 8; ++iter) {
-        ProductPlan P1 = plan_product(L, K, 1, KV_OP_N, KV_OP_N);
-        Meta last = P1.out;
-        if (nsite >= 1) last = plan_mix(last, *W1, 1).out;
-        if (nsite == 2) last = plan_mix(last, *W2, 2).out;
-        ProductPlan P2 = plan_product(last, R, 2, KV_OP_N, KV_OP_T);
+    for (int iter = 0;; ++iter) {
+        KV_REQUIRE(iter < 4096, KV_EINVAL, "H_eff block closure did not converge");
+        Meta out;
+        Flops f = heff_ref_flops(nsite, L, K, W1, W2, R, &out);
+        if (iter < max_iter) H.iter_flops.push_back(f);
         bool grew = false;
-        for (auto &b : P2.out.blocks)
-            if (K.find(b) < 0) { K.blocks.push_back(b); grew = true; }
-        if (!grew) break;
+        for (auto &b : out.blocks) {
+            const size_t before = K.blocks.size();
+            if ((size_t)K.add(b) == before) grew = true;
+        }
         K.layout();
-        KV_REQUIRE(iter < 7, KV_EINVAL, "H_eff block closure did not converge");
+        if (!grew) {
+            while ((int)H.iter_flops.size() < max_iter) H.iter_flops.push_back(f);
+            break;
+        }
     }
     K.layout();
     H.klayout = K;
@@ -379,29 +450,15 @@ HeffPlan plan_heff(int nsite, const Meta &L, const Meta &psi, const Meta *W1, co
     H.p1 = plan_product(L, K, 1, KV_OP_N, KV_OP_N);
     build_tiles(H.p1, own_offsets(H.p1.out), kTileM(precision), kTileN(precision));
     Meta last = H.p1.out;
-    Meta last_unmerged = H.p1.out;
-    H.ref_flops = H.p1.gemm.ref_flops;
-    H.gemm_flops = H.p1.gemm.ref_flops;
     if (nsite >= 1) {
         H.m1 = plan_mix(last, *W1, 1);
-        H.ref_flops += H.m1.ref_flops;
         last = H.m1.out;
-        last_unmerged = H.m1.unmerged;
     }
     if (nsite == 2) {
-        // the reference mixes W2 into every unmerged W1 block; count its flops on that structure
-        MixPlanFull ref2 = plan_mix(last_unmerged, *W2, 2);
         H.m2 = plan_mix(last, *W2, 2);
-        H.ref_flops += ref2.ref_flops;
         last = H.m2.out;
-        last_unmerged = ref2.unmerged;
     }
     H.p2 = plan_product(last, R, 2, KV_OP_N, KV_OP_T);
-    const double f2 = ref_product_flops(last_unmerged, R, 2, KV_OP_N, KV_OP_T);
-    H.ref_flops += f2;
-    H.gemm_flops += f2;
-    // the grouped GEMM is credited with the reference flops of the pairs it replaces
-    H.p2.gemm.ref_flops = f2;
     std::vector<int64_t> tgt;
     std::vector<char> produced(K.blocks.size(), 0);
     for (auto &b : H.p2.out.blocks) {
@@ -423,27 +480,79 @@ HeffPlan plan_heff(int nsite, const Meta &L, const Meta &psi, const Meta *W1, co
     H.p2.gemm.upload();
     if (nsite >= 1) H.m1.mix.upload();
     if (nsite == 2) H.m2.mix.upload();
-    H.t1 = DevBuf(std::max<int64_t>(1, H.p1.out.nelem) * sizeof(double2));
-    if (nsite >= 1) H.t2 = DevBuf(std::max<int64_t>(1, H.m1.out.nelem) * sizeof(double2));
-    if (nsite == 2) H.t3 = DevBuf(std::max<int64_t>(1, H.m2.out.nelem) * sizeof(double2));
     return H;
 }
 
+// ---------------------------------------------------------- plan cache
+// H_eff plans depend only on the block structures (charges, shapes, order) of
+// L, psi, W1, W2, R; in a steady sweep the same structures recur every time
+// step, so plans (host task lists and their device copies, no data) are cached.
+namespace {
+void key_meta(std::vector<int> &v, const Meta *m) {
+    if (!m) { v.push_back(-1); return; }
+    v.push_back(m->rank);
+    v.push_back((int)m->blocks.size());
+    for (int i = 0; i < m->rank; ++i) v.push_back(m->dirs[i]);
+    for (auto &b : m->blocks)
+        for (int i = 0; i < m->rank; ++i) { v.push_back(b.shape[i]); v.push_back(b.qn[i]); }
+}
+struct VecHash {
+    size_t operator()(const std::vector<int> &v) const {
+        uint64_t h = 1469598103934665603ull;
+        for (int x : v) { h ^= (uint64_t)(uint32_t)x; h *= 1099511628211ull; }
+        return (size_t)h;
+    }
+};
+std::unordered_map<std::vector<int>, std::shared_ptr<HeffPlan>, VecHash> g_plan_cache;
+constexpr size_t kPlanCacheMax = 16384;
+}  // namespace
+
+void clear_plan_cache() { g_plan_cache.clear(); }
+
+std::shared_ptr<HeffPlan> get_heff_plan(int nsite, const Meta &L, const Meta &psi, const Meta *W1, const Meta *W2,
+                                        const Meta &R, int precision, int max_iter) {
+    std::vector<int> key = {nsite, precision, max_iter};
+    key_meta(key, &L);
+    key_meta(key, &psi);
+    key_meta(key, W1);
+    key_meta(key, W2);
+    key_meta(key, &R);
+    auto it = g_plan_cache.find(key);
+    if (it != g_plan_cache.end()) return it->second;
+    if (g_plan_cache.size() >= kPlanCacheMax) g_plan_cache.clear();
+    auto p = std::make_shared<HeffPlan>(plan_heff(nsite, L, psi, W1, W2, R, precision, max_iter));
+    g_plan_cache.emplace(std::move(key), p);
+    return p;
+}
+
+// per-call intermediates of an H_eff application
+struct HeffWork {
+    DevBuf t1, t2, t3;
+    explicit HeffWork(const HeffPlan &H) {
+        t1 = DevBuf(std::max<int64_t>(1, H.p1.out.nelem) * sizeof(double2));
+        if (H.nsite >= 1) t2 = DevBuf(std::max<int64_t>(1, H.m1.out.nelem) * sizeof(double2));
+        if (H.nsite == 2) t3 = DevBuf(std::max<int64_t>(1, H.m2.out.nelem) * sizeof(double2));
+    }
+};
+
 // out (Krylov layout) = scale * H_eff . v (Krylov layout)
-void run_heff(HeffPlan &H, const DTensor &L, const double2 *v, const DTensor *W1, const DTensor *W2,
-              const DTensor &R, double2 *out, double scale, int precision, const int *skip,
+void run_heff(const HeffPlan &H, HeffWork &w, const DTensor &L, const double2 *v, const DTensor *W1,
+              const DTensor *W2, const DTensor &R, double2 *out, double scale, int precision, const int *skip,
               const KrylovState *st = nullptr, int k = -1) {
-    run_gemm(H.p1.gemm, L.data(), v, H.t1.as<double2>(), 1.0, precision, skip, st, k);
-    const double2 *last = H.t1.as<double2>();
+    // credit each launch with the reference flops of iteration k (all of the
+    // product<> flops to the first GEMM of the pair; the second gets none)
+    const double credit = (k >= 0 && k < (int)H.iter_flops.size()) ? H.iter_flops[k].gemm : -1.0;
+    run_gemm(H.p1.gemm, L.data(), v, w.t1.as<double2>(), 1.0, precision, skip, st, k, credit);
+    const double2 *last = w.t1.as<double2>();
     if (H.nsite >= 1) {
-        launch_mix(H.m1.mix, last, W1->data(), H.t2.as<double2>(), skip);
-        last = H.t2.as<double2>();
+        launch_mix(H.m1.mix, last, W1->data(), w.t2.as<double2>(), skip);
+        last = w.t2.as<double2>();
     }
     if (H.nsite == 2) {
-        launch_mix(H.m2.mix, last, W2->data(), H.t3.as<double2>(), skip);
-        last = H.t3.as<double2>();
+        launch_mix(H.m2.mix, last, W2->data(), w.t3.as<double2>(), skip);
+        last = w.t3.as<double2>();
     }
-    run_gemm(H.p2.gemm, last, R.data(), out, scale, precision, skip, st, k);
+    run_gemm(H.p2.gemm, last, R.data(), out, scale, precision, skip, st, k, credit >= 0.0 ? 0.0 : -1.0);
 }
 
 // scatter a tensor into a (superset) layout; blocks not present become zero
@@ -469,25 +578,29 @@ void scatter_into(const DTensor &src, const Meta &dst_meta, double2 *dst) {
 TensorP op_heff(int nsite, const DTensor &L, const DTensor &psi, const DTensor *W1, const DTensor *W2,
                 const DTensor &R, double scale, int precision) {
     check_precision(precision);
-    HeffPlan H = plan_heff(nsite, L.meta, psi.meta, W1 ? &W1->meta : nullptr, W2 ? &W2->meta : nullptr, R.meta,
-                           precision);
+    auto Hp = get_heff_plan(nsite, L.meta, psi.meta, W1 ? &W1->meta : nullptr, W2 ? &W2->meta : nullptr, R.meta,
+                            precision, 1);
+    const HeffPlan &H = *Hp;
+    HeffWork w(H);
     DevBuf v(std::max<int64_t>(1, H.klayout.nelem) * sizeof(double2));
     scatter_into(psi, H.klayout, v.as<double2>());
     auto out = DTensor::make(H.klayout, false);
-    run_heff(H, L, v.as<double2>(), W1, W2, R, out->data(), scale, precision, nullptr);
+    run_heff(H, w, L, v.as<double2>(), W1, W2, R, out->data(), scale, precision, nullptr);
     return out;
 }
 
 // ------------------------------------------------------- local_krylov
 TensorP op_lanczos(int nsite, const DTensor &L, const DTensor &psi, const DTensor *W1, const DTensor *W2,
                    const DTensor &R, double dt, int max_iter, double tol, bool reverse, int precision,
-                   KrylovState *st_dev, Flops *per_iter) {
+                   KrylovState *st_dev, std::vector<Flops> *per_iter) {
     check_precision(precision);
     KV_REQUIRE(max_iter >= 2 && max_iter <= kMaxKrylov, KV_EINVAL, "max_iter must be in [2, 32]");
     KV_REQUIRE(tol < 1.0, KV_EINVAL, "Krylov tolerance must be < 1");
-    HeffPlan H = plan_heff(nsite, L.meta, psi.meta, W1 ? &W1->meta : nullptr, W2 ? &W2->meta : nullptr, R.meta,
-                           precision);
-    if (per_iter) { per_iter->gemm = H.gemm_flops; per_iter->mix = H.ref_flops - H.gemm_flops; }
+    auto Hp = get_heff_plan(nsite, L.meta, psi.meta, W1 ? &W1->meta : nullptr, W2 ? &W2->meta : nullptr, R.meta,
+                            precision, max_iter);
+    const HeffPlan &H = *Hp;
+    HeffWork w(H);
+    if (per_iter) *per_iter = H.iter_flops;
     const int64_t n = H.klayout.nelem;
     const int nvec = max_iter;  // V_0 .. V_{max_iter-1}
     DevBuf Vbuf(std::max<int64_t>(1, n) * nvec * sizeof(double2));
@@ -499,7 +612,7 @@ TensorP op_lanczos(int nsite, const DTensor &L, const DTensor &psi, const DTenso
     krylov_start(st_dev, tmp.as<double2>(), V, n, parts.as<double2>());
     const int *skip = &st_dev->done;
     for (int k = 0; k < max_iter - 1; ++k) {
-        run_heff(H, L, V + (int64_t)k * n, W1, W2, R, hv.as<double2>(), dt * 0.5, precision, skip, st_dev, k);
+        run_heff(H, w, L, V + (int64_t)k * n, W1, W2, R, hv.as<double2>(), dt * 0.5, precision, skip, st_dev, k);
         krylov_step(st_dev, k, hv.as<double2>(), k > 0 ? V + (int64_t)(k - 1) * n : nullptr, V + (int64_t)k * n,
                     V + (int64_t)(k + 1) * n, n, parts.as<double2>(), tol, max_iter);
     }
@@ -512,6 +625,12 @@ TensorP op_lanczos(int nsite, const DTensor &L, const DTensor &psi, const DTenso
 }
 
 // ---------------------------------------------------------------- SVD
+// mixed mode: singular values below this fraction of their sector's largest
+// are below the FP32 Jacobi's resolution (exact zeros come out at up to
+// ~1e-5 relative after many FP32 rotations) and are treated as zero; a state
+// dropped by this rule carries at most 1e-8 of the sector's weight
+constexpr double kMixedSvdFloor = 1e-4;
+
 struct Micro {
     std::array<int, kMaxRank> shape{}, qn{};
     int pos = 0, len = 0;
@@ -552,7 +671,7 @@ static void fill_side(std::vector<Macro> &info, int q, const BlockMeta &b, int l
     info.push_back(mac);
 }
 
-SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim) {
+SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int precision) {
     const Meta &M = A.meta;
     KV_REQUIRE(r1 >= 1 && r1 < M.rank, KV_EINVAL, "svd split must be in [1, rank-1]");
     KV_REQUIRE(max_dim >= 1, KV_EINVAL, "max_dim must be >= 1");
@@ -595,13 +714,21 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim) {
             sec_rc.push_back({ri, ci});
         }
     P.upload();
-    DevBuf T(std::max<int64_t>(1, P.t_elems) * sizeof(double2)), Us(std::max<int64_t>(1, P.t_elems) * sizeof(double2));
-    DevBuf V(std::max<int64_t>(1, P.v_elems) * sizeof(double2)), Vs(std::max<int64_t>(1, P.v_elems) * sizeof(double2));
+    const bool mixed = svd_mixed(precision);
+    const size_t cb = mixed ? sizeof(float2) : sizeof(double2);
+    DevBuf T(std::max<int64_t>(1, P.t_elems) * sizeof(double2));
+    DevBuf Us(std::max<int64_t>(1, P.t_elems) * cb), V(std::max<int64_t>(1, P.v_elems) * cb);
+    DevBuf Vs(std::max<int64_t>(1, P.v_elems) * cb), T32(mixed ? std::max<int64_t>(1, P.t_elems) * cb : 16);
     DevBuf S(std::max<int64_t>(1, P.s_elems) * sizeof(double));
     DevBuf status(std::max<size_t>(1, P.secs.size()) * sizeof(int));
     svd_gather(P, A.data(), T.as<double2>());
-    svd_jacobi(P, T.as<double2>(), V.as<double2>(), status.as<int>(), 60, 1e-15);
-    svd_finalize(P, T.as<double2>(), V.as<double2>(), Us.as<double2>(), Vs.as<double2>(), S.as<double>());
+    if (mixed) {
+        svd_jacobi_f32(P, T.as<double2>(), T32.as<float2>(), V.as<float2>(), status.as<int>(), 60, 3e-7f);
+        svd_finalize_f32(P, T32.as<float2>(), V.as<float2>(), Us.as<float2>(), Vs.as<float2>(), S.as<double>());
+    } else {
+        svd_jacobi(P, T.as<double2>(), V.as<double2>(), status.as<int>(), 60, 1e-15);
+        svd_finalize(P, T.as<double2>(), V.as<double2>(), Us.as<double2>(), Vs.as<double2>(), S.as<double>());
+    }
     std::vector<double> sv(P.s_elems);
     std::vector<int> st(P.secs.size());
     if (P.s_elems)
@@ -611,6 +738,15 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim) {
     KV_CUDA(cudaStreamSynchronize(ctx().stream));
     for (int x : st) KV_REQUIRE(x >= 0, KV_ETIMEOUT, "Jacobi SVD did not converge within the sweep limit");
     for (double x : sv) KV_REQUIRE(std::isfinite(x), KV_ENONFINITE, "non-finite singular value");
+    if (mixed) {
+        // FP32 Jacobi resolves singular values only down to ~1e-5 of the
+        // sector's largest: anything below kMixedSvdFloor of it is a zero
+        for (auto &sc : P.secs) {
+            const double smax = sc.q > 0 ? sv[sc.s_off] : 0.0;
+            for (int i = 0; i < sc.q; ++i)
+                if (sv[sc.s_off + i] <= kMixedSvdFloor * smax) sv[sc.s_off + i] = 0.0;
+        }
+    }
     // global ordering and truncation, holstein/svd.h:350-388
     std::vector<std::pair<int, double>> collect;
     for (size_t s = 0; s < P.secs.size(); ++s) {
@@ -664,13 +800,132 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim) {
     }
     out.U = DTensor::make(mu, false);
     out.V = DTensor::make(mv, false);
-    std::vector<SvdScatter> su, svs;
-    for (size_t i = 0; i < pu.size(); ++i)
-        su.push_back({out.U->meta.blocks[i].off, pu[i].sector, 0, pu[i].pos, pu[i].len, pu[i].kept, l2r ? 0 : 1});
-    for (size_t i = 0; i < pv.size(); ++i)
-        svs.push_back({out.V->meta.blocks[i].off, pv[i].sector, 1, pv[i].pos, pv[i].len, pv[i].kept, l2r ? 1 : 0});
-    svd_scatter(su, P, Us.as<double2>(), Vs.as<double2>(), S.as<double>(), out.U->data());
-    svd_scatter(svs, P, Us.as<double2>(), Vs.as<double2>(), S.as<double>(), out.V->data());
+    if (!mixed) {
+        std::vector<SvdScatter> su, svs;
+        for (size_t i = 0; i < pu.size(); ++i)
+            su.push_back({out.U->meta.blocks[i].off, pu[i].sector, 0, pu[i].pos, pu[i].len, pu[i].kept, l2r ? 0 : 1});
+        for (size_t i = 0; i < pv.size(); ++i)
+            svs.push_back({out.V->meta.blocks[i].off, pv[i].sector, 1, pv[i].pos, pv[i].len, pv[i].kept, l2r ? 1 : 0});
+        svd_scatter(su, P, Us.as<double2>(), Vs.as<double2>(), S.as<double>(), out.U->data());
+        svd_scatter(svs, P, Us.as<double2>(), Vs.as<double2>(), S.as<double>(), out.V->data());
+        return out;
+    }
+    // ---- mixed mode: FP64 polish.  The kept factor is rebuilt in FP64 from the
+    // sector matrix and the FP32 singular vectors of the other side,
+    //   L->R: X = A_s V_k   R->L: X = A_s^H U_k,
+    // made orthonormal by shifted Cholesky-QR3, and the other factor is the
+    // exact projection (Y = X^H A_s, or A_s X).  With no truncation the
+    // factorisation is exact to FP64 rounding; the FP32 error only enters the
+    // choice of the discarded directions.
+    const int side = l2r ? 0 : 1;  // which factor is kept orthonormal
+    std::vector<SvdPolish> pol;
+    std::vector<int> pol_of_sector(P.secs.size(), -1);
+    int64_t x_elems = 0, g_elems = 0, y_elems = 0, w_elems = 0;
+    std::vector<int64_t> y_off(P.secs.size(), 0);
+    for (size_t s_ = 0; s_ < P.secs.size(); ++s_) {
+        const int k = rows[sec_rc[s_].first].kept;
+        if (k <= 0 || cols[sec_rc[s_].second].kept <= 0) continue;
+        const SvdSector &sc = P.secs[s_];
+        const int xr = side == 0 ? sc.m : sc.n;  // rows of the kept factor
+        const int wr = side == 0 ? sc.n : sc.m;  // rows of the other side's vectors
+        pol_of_sector[s_] = (int)pol.size();
+        pol.push_back({x_elems, g_elems, w_elems, (int)s_, xr, k, 0});
+        x_elems += (int64_t)xr * k;
+        g_elems += (int64_t)k * k;
+        w_elems += (int64_t)wr * k;
+        y_off[s_] = y_elems;
+        y_elems += (int64_t)k * (side == 0 ? sc.n : sc.m);
+    }
+    DevBuf dpol = upload_vec(pol);
+    DevBuf X(std::max<int64_t>(1, x_elems) * sizeof(double2)), Gm(std::max<int64_t>(1, g_elems) * sizeof(double2));
+    DevBuf Y(std::max<int64_t>(1, y_elems) * sizeof(double2)), Wb(std::max<int64_t>(1, w_elems) * sizeof(double2));
+    DevBuf cst(std::max<size_t>(1, pol.size()) * sizeof(int)), cdiag(std::max<size_t>(1, pol.size()) * sizeof(double));
+    KV_CUDA(cudaMemsetAsync(cst.p, 0, std::max<size_t>(1, pol.size()) * sizeof(int), ctx().stream));
+    svd_extract(dpol, (int)pol.size(), P, Us.as<float2>(), Vs.as<float2>(), Wb.as<double2>(), 1 - side);
+    const int tm = kTileM(KV_FP64), tn = kTileN(KV_FP64);
+    auto add_gemm = [&](GemmPlan &g, int64_t c_off, int M, int N, GemmSeg seg) {
+        const int sb = (int)g.segs.size();
+        g.segs.push_back(seg);
+        for (int m0 = 0; m0 < M; m0 += tm)
+            for (int n0 = 0; n0 < N; n0 += tn) g.tiles.push_back({c_off, N, M, N, m0, n0, sb, sb + 1});
+    };
+    // X = A_s W (L->R, K = n) or A_s^H W (R->L, K = m), A_s from T:
+    // A_s[i, j] = T[i + j p] (T = A_s) or conj(T[j + i p]) (T = A_s^H)
+    GemmPlan build;
+    for (auto &pl : pol) {
+        const SvdSector &sc = P.secs[pl.sector];
+        if (side == 0)
+            add_gemm(build, pl.x_off, sc.m, pl.k, GemmSeg{sc.t_off, pl.w_off, sc.n, sc.p, pl.k, sc.transposed ? 3 : 2, 0});
+        else
+            add_gemm(build, pl.x_off, sc.n, pl.k, GemmSeg{sc.t_off, pl.w_off, sc.m, sc.p, pl.k, sc.transposed ? 2 : 3, 0});
+    }
+    build.upload();
+    launch_gemm_fp64(build, T.as<double2>(), Wb.as<double2>(), X.as<double2>(), 1.0, nullptr);
+    GemmPlan gram;
+    for (auto &pl : pol) add_gemm(gram, pl.g_off, pl.k, pl.k, GemmSeg{pl.x_off, pl.x_off, pl.rows, pl.k, pl.k, 1, 0});
+    gram.upload();
+    std::vector<int> item_pol, item_row0;
+    for (size_t i = 0; i < pol.size(); ++i)
+        for (int r0 = 0; r0 < pol[i].rows; r0 += 64) { item_pol.push_back((int)i); item_row0.push_back(r0); }
+    // shifted CholeskyQR3: the columns of X have norms ~ s_j (condition up to
+    // ~1e5 at the floor); a shifted first pass keeps the factorisation defined,
+    // two plain passes restore FP64 orthonormality; the span never changes
+    for (int pass = 0; pass < 3; ++pass) {
+        launch_gemm_fp64(gram, X.as<double2>(), X.as<double2>(), Gm.as<double2>(), 1.0, nullptr);
+        svd_chol(dpol, (int)pol.size(), Gm.as<double2>(), cst.as<int>(), cdiag.as<double>(), pass == 0 ? 1e-14 : 0.0);
+        svd_trsm(dpol, item_pol, item_row0, Gm.as<double2>(), X.as<double2>());
+    }
+    GemmPlan proj;
+    for (auto &pl : pol) {
+        const SvdSector &sc = P.secs[pl.sector];
+        const int64_t tof = sc.t_off;
+        if (side == 0) {
+            // Y = X^H A_s (k x n)
+            add_gemm(proj, y_off[pl.sector], pl.k, sc.n,
+                     GemmSeg{pl.x_off, tof, sc.m, pl.k, sc.p, 1, sc.transposed ? 3 : 1});
+        } else {
+            // Lef = A_s X (m x k)
+            add_gemm(proj, y_off[pl.sector], sc.m, pl.k,
+                     GemmSeg{tof, pl.x_off, sc.n, sc.p, pl.k, sc.transposed ? 3 : 2, 0});
+        }
+    }
+    proj.upload();
+    if (side == 0) launch_gemm_fp64(proj, X.as<double2>(), T.as<double2>(), Y.as<double2>(), 1.0, nullptr);
+    else launch_gemm_fp64(proj, T.as<double2>(), X.as<double2>(), Y.as<double2>(), 1.0, nullptr);
+    std::vector<SvdDense> du, dv;
+    for (size_t i = 0; i < pu.size(); ++i) {
+        const int s_ = pu[i].sector;
+        const SvdPolish &pl = pol[pol_of_sector[s_]];
+        if (side == 0) du.push_back({out.U->meta.blocks[i].off, pl.x_off, 0, pu[i].pos, pu[i].len, pl.k, pl.k, 0});
+        else du.push_back({out.U->meta.blocks[i].off, y_off[s_], 0, pu[i].pos, pu[i].len, pl.k, pl.k, 0});
+    }
+    for (size_t i = 0; i < pv.size(); ++i) {
+        const int s_ = pv[i].sector;
+        const SvdPolish &pl = pol[pol_of_sector[s_]];
+        if (side == 0)
+            dv.push_back({out.V->meta.blocks[i].off, y_off[s_], 1, pv[i].pos, pv[i].len, pl.k, P.secs[s_].n, 0});
+        else dv.push_back({out.V->meta.blocks[i].off, pl.x_off, 1, pv[i].pos, pv[i].len, pl.k, pl.k, 1});
+    }
+    svd_scatter_dense(du, side == 0 ? X.as<double2>() : Y.as<double2>(), out.U->data());
+    svd_scatter_dense(dv, side == 0 ? Y.as<double2>() : X.as<double2>(), out.V->data());
+    std::vector<int> ch(pol.size());
+    std::vector<double> chd(pol.size());
+    if (!ch.empty()) {
+        KV_CUDA(cudaMemcpyAsync(ch.data(), cst.p, ch.size() * sizeof(int), cudaMemcpyDeviceToHost, ctx().stream));
+        KV_CUDA(cudaMemcpyAsync(chd.data(), cdiag.p, chd.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                ctx().stream));
+        KV_CUDA(cudaStreamSynchronize(ctx().stream));
+        for (size_t i = 0; i < ch.size(); ++i) {
+            if (ch[i] == 0) continue;
+            const SvdSector &sc = P.secs[pol[i].sector];
+            std::string msg = "Cholesky re-orthonormalisation failed: sector m=" + std::to_string(sc.m) +
+                              " n=" + std::to_string(sc.n) + " kept=" + std::to_string(pol[i].k) +
+                              " transposed=" + std::to_string(sc.transposed) + " l2r=" + std::to_string(l2r) +
+                              " pivot=" + std::to_string(ch[i] - 1) + " value=" + std::to_string(chd[i]) + " s=[";
+            for (int j = 0; j < std::min(sc.q, 12); ++j) msg += std::to_string(sv[sc.s_off + j]) + " ";
+            throw Error(KV_ENONFINITE, msg + "]");
+        }
+    }
     return out;
 }
 
@@ -721,7 +976,8 @@ TensorP op_env(bool l2r, const DTensor &env, const DTensor &A, const DTensor &W,
     auto t2 = DTensor::make(M.out, false);
     launch_mix(M.mix, t1->data(), W.data(), t2->data(), nullptr);
     ProductPlan P2 = plan_product(A.meta, t2->meta, 2, KV_OP_C, KV_OP_N);
-    const double f2 = ref_product_flops(A.meta, M.unmerged, 2, KV_OP_C, KV_OP_N);
+    // A's blocks pair with every (reference-unmerged) copy of each mixed block
+    const double f2 = ref_product_flops(A.meta, M.out, 2, KV_OP_C, KV_OP_N, nullptr, &M.mult);
     P2.gemm.ref_flops = f2;
     auto out = DTensor::make(P2.out, false);
     build_tiles(P2, own_offsets(out->meta), kTileM(precision), kTileN(precision));
@@ -791,7 +1047,7 @@ KrylovState *Tdvp::next_state() {
 TensorP Tdvp::krylov(int nsite, const DTensor &L, const DTensor &psi, const DTensor *W1, const DTensor *W2,
                      const DTensor &R, bool reverse, int module) {
     mark(module, true);
-    Flops f;
+    std::vector<Flops> f;
     KrylovState *st = next_state();
     TensorP r = op_lanczos(nsite, L, psi, W1, W2, R, dt, max_iter, tol_exp, reverse, precision, st, &f);
     krylov_flops.push_back({st, f});
@@ -819,6 +1075,10 @@ void Tdvp::end_sweep() {
     float sms = 0.f;
     KV_CUDA(cudaEventElapsedTime(&sms, sweep_ev[0], sweep_ev[1]));
     sweep_ms = sms;
+    {
+        const int st = mixed_gemm_status();
+        KV_REQUIRE(st == KV_OK, st, "a tensor-core GEMM wait timed out");
+    }
     for (auto &m : module_ms) m = 0.0;
     for (int i = 0; i < n_marks; ++i) {
         float ms = 0.f;
@@ -834,8 +1094,10 @@ void Tdvp::end_sweep() {
     for (auto &kf : krylov_flops) {
         const KrylovState &h = host[kf.first - kstate.as<KrylovState>()];
         KV_REQUIRE(h.status == KV_OK, h.status, "non-finite norm in the Lanczos recurrence");
-        f += (kf.second.gemm + kf.second.mix) * h.iters;
-        fg += kf.second.gemm * h.iters;
+        for (int k = 0; k < h.iters && k < (int)kf.second.size(); ++k) {
+            f += kf.second[k].gemm + kf.second[k].mix;
+            fg += kf.second[k].gemm;
+        }
     }
     last_ref_flops = f;
     last_gemm_flops = fg;
@@ -851,7 +1113,7 @@ void Tdvp::one_site() {
         mps[i] = krylov(1, *envL.back(), *mps[i], mpo[i].get(), nullptr, *envR.back(), false, MOD_EVL1);
         if (i < ns - 1) {
             mark(MOD_SVD, true);
-            SvdOut r = op_svd(*mps[i], 2, true, tol_svd, max_dim);
+            SvdOut r = op_svd(*mps[i], 2, true, tol_svd, max_dim, precision);
             mark(MOD_SVD, false);
             mps[i] = r.U;
             mark(MOD_UPDATE, true);
@@ -868,7 +1130,7 @@ void Tdvp::one_site() {
         mps[i] = krylov(1, *envL.back(), *mps[i], mpo[i].get(), nullptr, *envR.back(), false, MOD_EVL1);
         if (i > 0) {
             mark(MOD_SVD, true);
-            SvdOut r = op_svd(*mps[i], 1, false, tol_svd, max_dim);
+            SvdOut r = op_svd(*mps[i], 1, false, tol_svd, max_dim, precision);
             mark(MOD_SVD, false);
             mps[i] = r.V;
             mark(MOD_UPDATE, true);
@@ -895,7 +1157,7 @@ void Tdvp::two_site() {
         mark(MOD_SWEEP, false);
         mm = krylov(2, *envL.back(), *mm, mpo[i].get(), mpo[i + 1].get(), *envR.back(), false, MOD_EVL2);
         mark(MOD_SVD, true);
-        SvdOut r = op_svd(*mm, 2, true, tol_svd, max_dim);
+        SvdOut r = op_svd(*mm, 2, true, tol_svd, max_dim, precision);
         mark(MOD_SVD, false);
         if (i < ns - 2) {
             mps[i] = r.U;
@@ -915,7 +1177,7 @@ void Tdvp::two_site() {
         mark(MOD_SWEEP, false);
         mm = krylov(2, *envL.back(), *mm, mpo[i - 1].get(), mpo[i].get(), *envR.back(), false, MOD_EVL2);
         mark(MOD_SVD, true);
-        SvdOut r = op_svd(*mm, 2, false, tol_svd, max_dim);
+        SvdOut r = op_svd(*mm, 2, false, tol_svd, max_dim, precision);
         mark(MOD_SVD, false);
         if (i > 1) {
             mps[i] = r.V;

@@ -4,9 +4,12 @@
 
 namespace kv {
 
+// precision mode -> which parts run in mixed precision
+inline bool gemm_mixed(int precision) { return precision == KV_MIXED_TF32 || precision == KV_MIXED_GEMM; }
+inline bool svd_mixed(int precision) { return precision == KV_MIXED_TF32 || precision == KV_MIXED_SVD; }
 // Output tile shape of the grouped GEMM for a precision mode.
-inline int kTileM(int precision) { return precision == KV_MIXED_TF32 ? 128 : 32; }
-inline int kTileN(int precision) { return precision == KV_MIXED_TF32 ? 64 : 32; }
+inline int kTileM(int precision) { return gemm_mixed(precision) ? 128 : 32; }
+inline int kTileN(int precision) { return gemm_mixed(precision) ? 64 : 32; }
 
 // reference flop count split by who executes it here: the grouped GEMM
 // (product<> pairs) or the MPO mixing kernel (env_mps_mpo zgemms)
@@ -22,8 +25,8 @@ struct ProductPlan {
 };
 
 struct MixPlanFull {
-    Meta out;       // merged output structure (what is computed)
-    Meta unmerged;  // one block per matched pair (the reference's structure)
+    Meta out;                  // merged output structure (what is computed)
+    std::vector<double> mult;  // reference blocks (matched pairs) merged into each output block
     MixPlan mix;
     double ref_flops = 0.0;
 };
@@ -33,9 +36,7 @@ struct HeffPlan {
     Meta klayout;  // Krylov layout (closure of psi's blocks under H_eff)
     ProductPlan p1, p2;
     MixPlanFull m1, m2;
-    DevBuf t1, t2, t3;  // intermediates
-    double ref_flops = 0.0;   // reference flops of one H_eff application
-    double gemm_flops = 0.0;  // of which executed by the grouped GEMM
+    std::vector<Flops> iter_flops;  // reference flops of the apply at Lanczos iteration k
 };
 
 struct SvdOut {
@@ -46,18 +47,21 @@ struct SvdOut {
 
 ProductPlan plan_product(const Meta &A, const Meta &B, int nc, int opA, int opB);
 void build_tiles(ProductPlan &P, const std::vector<int64_t> &target_off, int tile_m, int tile_n);
-MixPlanFull plan_mix(const Meta &lm, const Meta &W, int lead);
+MixPlanFull plan_mix(const Meta &lm, const Meta &W, int lead, const std::vector<double> *mult_in = nullptr);
+double ref_product_flops(const Meta &A, const Meta &B, int nc, int opA, int opB, const std::vector<double> *multA,
+                         const std::vector<double> *multB);
 HeffPlan plan_heff(int nsite, const Meta &L, const Meta &psi, const Meta *W1, const Meta *W2, const Meta &R,
-                   int precision);
+                   int precision, int max_iter);
 
+void clear_plan_cache();
 TensorP op_product(const DTensor &A, const DTensor &B, int nc, int opA, int opB, int precision,
                    Flops *fl = nullptr);
 TensorP op_heff(int nsite, const DTensor &L, const DTensor &psi, const DTensor *W1, const DTensor *W2,
                 const DTensor &R, double scale, int precision);
 TensorP op_lanczos(int nsite, const DTensor &L, const DTensor &psi, const DTensor *W1, const DTensor *W2,
                    const DTensor &R, double dt, int max_iter, double tol, bool reverse, int precision,
-                   KrylovState *st_dev, Flops *per_iter);
-SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim);
+                   KrylovState *st_dev, std::vector<Flops> *per_iter);
+SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int precision);
 TensorP op_env(bool l2r, const DTensor &env, const DTensor &A, const DTensor &W, const DTensor *Wt, int precision,
                Flops *fl);
 TensorP op_permute(const DTensor &t, const std::vector<int> &ax);
@@ -96,7 +100,7 @@ class Tdvp {
     std::vector<cudaEvent_t> events;
     int mark_module[kMaxEvents] = {};
     int n_marks = 0, n_krylov = 0;
-    std::vector<std::pair<KrylovState *, Flops>> krylov_flops;
+    std::vector<std::pair<KrylovState *, std::vector<Flops>>> krylov_flops;
     Flops other;
     cudaEvent_t sweep_ev[2] = {};
 };

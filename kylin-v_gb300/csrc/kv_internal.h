@@ -10,6 +10,7 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/kvgpu.h"
@@ -60,6 +61,14 @@ struct Context {
     std::vector<cudaEvent_t> ev_free;
     double prof_ms = 0.0, prof_flops = 0.0;
     long long prof_launches = 0;
+    // pinned staging ring for plan uploads: kRingChunks chunks of kRingChunk bytes
+    static constexpr int kRingChunks = 16;
+    static constexpr size_t kRingChunk = 4u << 20;
+    char *ring = nullptr;
+    int ring_cur = 0;
+    size_t ring_used = 0;
+    cudaEvent_t ring_ev[kRingChunks] = {};
+    bool ring_live[kRingChunks] = {};
 };
 Context &ctx();
 void require_init();
@@ -88,14 +97,14 @@ struct DevBuf {
     template <class T> T *as() const { return static_cast<T *>(p); }
 };
 
-// Upload a host vector into a fresh device buffer (async on the stream; the
-// host vector must stay alive until the stream reaches the copy -- callers
-// keep plans alive for that reason).
+// Host-to-device copy of a small host array through a pinned staging ring,
+// so the copy is asynchronous and the source may be freed on return.
+void upload_bytes(void *dst, const void *src, size_t n);
+
 template <class T>
 DevBuf upload_vec(const std::vector<T> &v) {
     DevBuf b(std::max<size_t>(1, v.size()) * sizeof(T));
-    if (!v.empty())
-        KV_CUDA(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, ctx().stream));
+    if (!v.empty()) upload_bytes(b.p, v.data(), v.size() * sizeof(T));
     return b;
 }
 
@@ -106,21 +115,53 @@ struct BlockMeta {
     int64_t size = 0;  // complex elements
 };
 
+// Exact (shape, charge) key of some legs of a block, hashable.
+struct LegKey {
+    std::array<int, 2 * kMaxRank> v{};
+    bool operator==(const LegKey &o) const { return v == o.v; }
+};
+struct LegKeyHash {
+    size_t operator()(const LegKey &k) const {
+        uint64_t h = 1469598103934665603ull;
+        for (int x : k.v) { h ^= (uint64_t)(uint32_t)x; h *= 1099511628211ull; }
+        return (size_t)h;
+    }
+};
+inline LegKey leg_key(const BlockMeta &b, int lo, int hi) {
+    LegKey k;
+    for (int i = lo; i < hi; ++i) { k.v[2 * (i - lo)] = b.shape[i]; k.v[2 * (i - lo) + 1] = b.qn[i]; }
+    return k;
+}
+
 struct Meta {
     int rank = 0;
     std::array<int, kMaxRank> dirs{};
     std::vector<BlockMeta> blocks;
     int64_t nelem = 0;
-    void layout();  // contiguous offsets in block order
+    std::unordered_map<LegKey, int, LegKeyHash> index;  // full (shape, qn) key -> block
+    void layout();  // contiguous offsets in block order, rebuilds the index
     bool same_key(const BlockMeta &a, const BlockMeta &b) const {
         for (int i = 0; i < rank; ++i)
             if (a.shape[i] != b.shape[i] || a.qn[i] != b.qn[i]) return false;
         return true;
     }
     int find(const BlockMeta &b) const {
+        if (index.size() == blocks.size()) {
+            auto it = index.find(leg_key(b, 0, rank));
+            return it == index.end() ? -1 : it->second;
+        }
         for (size_t i = 0; i < blocks.size(); ++i)
             if (same_key(blocks[i], b)) return (int)i;
         return -1;
+    }
+    // append b if its key is new; returns its index
+    int add(const BlockMeta &b) {
+        LegKey k = leg_key(b, 0, rank);
+        auto it = index.find(k);
+        if (it != index.end()) return it->second;
+        blocks.push_back(b);
+        index.emplace(k, (int)blocks.size() - 1);
+        return (int)blocks.size() - 1;
     }
 };
 
@@ -143,8 +184,9 @@ void download_tensor(const DTensor &t, int *dirs, int *shapes, int *qns, double 
 struct GemmSeg {
     int64_t a_off, b_off;  // complex elements into the A / B buffers
     int K, lda, ldb;
-    int opa;  // 0: A[m*lda + k]; 1: conj(A[k*lda + m])
-    int opb;  // 0: B[k*ldb + n]; 1: B[n*ldb + k]
+    int opa;  // 0: A[m*lda + k]; 1: conj(A[k*lda + m]); 2: A[k*lda + m]; 3: conj(A[m*lda + k])
+    int opb;  // 0: B[k*ldb + n]; 1: B[n*ldb + k]; 2: conj(B[n*ldb + k]); 3: conj(B[k*ldb + n])
+              // (the tensor-core kernel implements opa, opb in {0, 1})
 };
 struct GemmTile {
     int64_t c_off;
@@ -187,9 +229,11 @@ void launch_gemm_fp64(const GemmPlan &p, const double2 *A, const double2 *B, dou
                       const int *skip);
 // dispatch by precision; st/k identify a Lanczos apply for profiling
 void run_gemm(const GemmPlan &g, const double2 *A, const double2 *B, double2 *C, double alpha, int precision,
-              const int *skip, const KrylovState *st = nullptr, int k = -1);
+              const int *skip, const KrylovState *st = nullptr, int k = -1, double credit_flops = -1.0);
 void launch_gemm_mixed(const GemmPlan &p, const double2 *A, const double2 *B, double2 *C, double alpha,
                        const int *skip);
+// KV_ETIMEOUT if a tensor-core kernel's bounded wait gave up since the last call
+int mixed_gemm_status();
 void launch_mix(const MixPlan &p, const double2 *in, const double2 *W, double2 *out, const int *skip);
 void launch_permute(const double2 *in, double2 *out, const std::vector<int64_t> &desc, int nblocks);
 void launch_zero(double2 *p, int64_t n);

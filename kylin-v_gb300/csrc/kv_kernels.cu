@@ -42,23 +42,27 @@ __global__ void __launch_bounds__(256) k_gemm_fp64(const GemmTile *__restrict__ 
             for (int r = 0; r < 2; ++r) {
                 int idx = tid + r * 256;
                 int m, k;
-                if (g.opa == 0) { m = idx / TK; k = idx % TK; }
+                const bool a_kc = (g.opa == 0 || g.opa == 3);  // contiguous along k
+                if (a_kc) { m = idx / TK; k = idx % TK; }
                 else { m = idx % TM; k = idx / TM; }
                 int gm = t.m0 + m, gk = k0 + k;
                 double2 v = make_double2(0.0, 0.0);
                 if (gm < t.M && gk < g.K) {
-                    if (g.opa == 0) v = a[(int64_t)gm * g.lda + gk];
-                    else { v = a[(int64_t)gk * g.lda + gm]; v.y = -v.y; }
+                    v = a_kc ? a[(int64_t)gm * g.lda + gk] : a[(int64_t)gk * g.lda + gm];
+                    if (g.opa == 1 || g.opa == 3) v.y = -v.y;
                 }
                 As[k][m] = v;
                 int n;
-                if (g.opb == 0) { n = idx % TN; k = idx / TN; }
+                const bool b_nc = (g.opb == 0 || g.opb == 3);  // contiguous along n
+                if (b_nc) { n = idx % TN; k = idx / TN; }
                 else { k = idx % TK; n = idx / TK; }
                 int gn = t.n0 + n;
                 gk = k0 + k;
                 double2 w = make_double2(0.0, 0.0);
-                if (gn < t.N && gk < g.K)
-                    w = (g.opb == 0) ? b[(int64_t)gk * g.ldb + gn] : b[(int64_t)gn * g.ldb + gk];
+                if (gn < t.N && gk < g.K) {
+                    w = b_nc ? b[(int64_t)gk * g.ldb + gn] : b[(int64_t)gn * g.ldb + gk];
+                    if (g.opb == 2 || g.opb == 3) w.y = -w.y;
+                }
                 Bs[k][n] = w;
             }
             __syncthreads();

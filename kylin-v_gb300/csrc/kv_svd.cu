@@ -30,7 +30,15 @@ __global__ void __launch_bounds__(256) k_svd_gather(const SvdGather *__restrict_
     }
 }
 
-__device__ __forceinline__ void warp_sum3(double &a, double &b, double &cr, double &ci) {
+template <class R>
+struct Cx;
+template <>
+struct Cx<double> { using T = double2; };
+template <>
+struct Cx<float> { using T = float2; };
+
+template <class R>
+__device__ __forceinline__ void warp_sum3(R &a, R &b, R &cr, R &ci) {
     for (int o = 16; o > 0; o >>= 1) {
         a += __shfl_xor_sync(0xffffffffu, a, o);
         b += __shfl_xor_sync(0xffffffffu, b, o);
@@ -39,19 +47,26 @@ __device__ __forceinline__ void warp_sum3(double &a, double &b, double &cr, doub
     }
 }
 
-// One CTA per sector.  status[sector] = sweeps used (negative: no convergence).
-__global__ void __launch_bounds__(ST) k_svd_jacobi(const SvdSector *__restrict__ secs, double2 *__restrict__ T,
-                                                   double2 *__restrict__ V, int *status, int max_sweeps,
-                                                   double tol) {
+// One CTA per sector, NT threads.  status[sector] = sweeps used (negative:
+// no convergence within max_sweeps).
+template <class R, int NT>
+__global__ void __launch_bounds__(NT) k_svd_jacobi(const SvdSector *__restrict__ secs, typename Cx<R>::T *__restrict__ T,
+                                                   typename Cx<R>::T *__restrict__ V, int *status, int max_sweeps,
+                                                   R tol) {
+    using C = typename Cx<R>::T;
     const SvdSector s = secs[blockIdx.x];
     const int p = s.p, q = s.q;
-    double2 *t = T + s.t_off;
-    double2 *v = V + s.v_off;
-    for (int64_t e = threadIdx.x; e < (int64_t)q * q; e += ST)
-        v[e] = make_double2((e % q) == (e / q) ? 1.0 : 0.0, 0.0);
+    C *t = T + s.t_off;
+    C *v = V + s.v_off;
+    for (int64_t e = threadIdx.x; e < (int64_t)q * q; e += NT) {
+        C one;
+        one.x = (e % q) == (e / q) ? R(1) : R(0);
+        one.y = R(0);
+        v[e] = one;
+    }
     __syncthreads();
     const int qe = q + (q & 1);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = ST / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = NT / 32;
     __shared__ int rotated;
     int sweep = 0;
     bool converged = (q < 2);
@@ -63,29 +78,29 @@ __global__ void __launch_bounds__(ST) k_svd_jacobi(const SvdSector *__restrict__
                 int c0, c1;
                 kvj::tournament_pair(qe, r, pi, c0, c1);
                 if (c1 >= q) continue;
-                double2 *x = t + (int64_t)c0 * p, *y = t + (int64_t)c1 * p;
-                double a = 0.0, b = 0.0, cr = 0.0, ci = 0.0;
+                C *x = t + (int64_t)c0 * p, *y = t + (int64_t)c1 * p;
+                R a = 0, b = 0, cr = 0, ci = 0;
                 for (int i = lane; i < p; i += 32) {
-                    double2 xi = x[i], yi = y[i];
+                    C xi = x[i], yi = y[i];
                     a += xi.x * xi.x + xi.y * xi.y;
                     b += yi.x * yi.x + yi.y * yi.y;
                     cr += xi.x * yi.x + xi.y * yi.y;
                     ci += xi.x * yi.y - xi.y * yi.x;
                 }
-                warp_sum3(a, b, cr, ci);
-                kvj::Rot<double> R;
-                if (!kvj::make_rotation<double>(a, b, cr, ci, tol, R)) continue;
+                warp_sum3<R>(a, b, cr, ci);
+                kvj::Rot<R> rot;
+                if (!kvj::make_rotation<R>(a, b, cr, ci, tol, rot)) continue;
                 if (lane == 0) rotated = 1;
                 for (int i = lane; i < p; i += 32) {
-                    double2 xi = x[i], yi = y[i];
-                    kvj::rotate_pair(R, xi.x, xi.y, yi.x, yi.y);
+                    C xi = x[i], yi = y[i];
+                    kvj::rotate_pair(rot, xi.x, xi.y, yi.x, yi.y);
                     x[i] = xi;
                     y[i] = yi;
                 }
-                double2 *vx = v + (int64_t)c0 * q, *vy = v + (int64_t)c1 * q;
+                C *vx = v + (int64_t)c0 * q, *vy = v + (int64_t)c1 * q;
                 for (int i = lane; i < q; i += 32) {
-                    double2 xi = vx[i], yi = vy[i];
-                    kvj::rotate_pair(R, xi.x, xi.y, yi.x, yi.y);
+                    C xi = vx[i], yi = vy[i];
+                    kvj::rotate_pair(rot, xi.x, xi.y, yi.x, yi.y);
                     vx[i] = xi;
                     vy[i] = yi;
                 }
@@ -98,19 +113,23 @@ __global__ void __launch_bounds__(ST) k_svd_jacobi(const SvdSector *__restrict__
     if (threadIdx.x == 0) status[blockIdx.x] = converged ? sweep : -sweep;
 }
 
-// singular values, descending order, normalised U columns
-__global__ void __launch_bounds__(ST) k_svd_finalize(const SvdSector *__restrict__ secs, const double2 *__restrict__ T,
-                                                     const double2 *__restrict__ V, double2 *__restrict__ Us,
-                                                     double2 *__restrict__ Vs, double *__restrict__ S) {
+// singular values (as double), descending order, normalised U columns
+template <class R>
+__global__ void __launch_bounds__(256) k_svd_finalize(const SvdSector *__restrict__ secs,
+                                                      const typename Cx<R>::T *__restrict__ T,
+                                                      const typename Cx<R>::T *__restrict__ V,
+                                                      typename Cx<R>::T *__restrict__ Us,
+                                                      typename Cx<R>::T *__restrict__ Vs, double *__restrict__ S) {
+    using C = typename Cx<R>::T;
     const SvdSector s = secs[blockIdx.x];
     const int p = s.p, q = s.q;
     extern __shared__ double sv[];  // q norms
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = ST / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = 256 / 32;
     for (int j = warp; j < q; j += nw) {
         double a = 0.0;
         for (int i = lane; i < p; i += 32) {
-            double2 x = T[s.t_off + (int64_t)j * p + i];
-            a += x.x * x.x + x.y * x.y;
+            C x = T[s.t_off + (int64_t)j * p + i];
+            a += (double)x.x * x.x + (double)x.y * x.y;
         }
         for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
         if (lane == 0) sv[j] = sqrt(a);
@@ -120,13 +139,126 @@ __global__ void __launch_bounds__(ST) k_svd_finalize(const SvdSector *__restrict
         const double sj = sv[j];
         int rank = 0;
         for (int i = 0; i < q; ++i) rank += (sv[i] > sj) || (sv[i] == sj && i < j);
-        const double inv = sj > 0.0 ? 1.0 / sj : 0.0;
+        const R inv = sj > 0.0 ? R(1.0 / sj) : R(0);
         for (int i = lane; i < p; i += 32) {
-            double2 x = T[s.t_off + (int64_t)j * p + i];
-            Us[s.t_off + (int64_t)rank * p + i] = make_double2(x.x * inv, x.y * inv);
+            C x = T[s.t_off + (int64_t)j * p + i];
+            x.x *= inv;
+            x.y *= inv;
+            Us[s.t_off + (int64_t)rank * p + i] = x;
         }
         for (int i = lane; i < q; i += 32) Vs[s.v_off + (int64_t)rank * q + i] = V[s.v_off + (int64_t)j * q + i];
         if (lane == 0) S[s.s_off + rank] = sj;
+    }
+}
+
+__global__ void k_to_f32(const double2 *__restrict__ in, float2 *__restrict__ out, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = make_float2((float)in[i].x, (float)in[i].y);
+}
+
+// ------------------------------------------------------- FP64 polish
+// Kept columns of one factor as a row-major FP64 matrix:
+// side 0 -> U_A[:, :k] (m x k);  side 1 -> V_A[:, :k] (n x k).
+__global__ void k_svd_extract(const SvdPolish *__restrict__ pol, const SvdSector *__restrict__ secs,
+                              const float2 *__restrict__ Us, const float2 *__restrict__ Vs, double2 *__restrict__ W,
+                              int side) {
+    const SvdPolish d = pol[blockIdx.x];
+    const SvdSector s = secs[d.sector];
+    const int rows = side == 0 ? s.m : s.n, k = d.k;
+    for (int64_t e = threadIdx.x; e < (int64_t)rows * k; e += blockDim.x) {
+        const int i = (int)(e / k), j = (int)(e % k);
+        // U_A = U (not transposed) or V (transposed); V_A = V (not transposed) or U (transposed)
+        const bool from_u = (side == 0) != (s.transposed != 0);
+        float2 v = from_u ? Us[s.t_off + (int64_t)j * s.p + i] : Vs[s.v_off + (int64_t)j * s.q + i];
+        W[d.w_off + e] = make_double2(v.x, v.y);
+    }
+}
+
+// In place: G (k x k, row-major, Hermitian positive definite) -> upper R with
+// G = R^H R (lower triangle left as is).  One CTA per sector, column-wise.
+__global__ void k_chol(const SvdPolish *__restrict__ pol, double2 *__restrict__ G, int *status, double *diagv,
+                       double shift) {
+    const SvdPolish d = pol[blockIdx.x];
+    const int k = d.k;
+    double2 *g = G + d.g_off;
+    __shared__ double diag;
+    if (shift > 0.0 && threadIdx.x == 0) {
+        // shifted Cholesky-QR: G + shift * max diag * I is safely positive definite
+        double mx = 0.0;
+        for (int j = 0; j < k; ++j) mx = fmax(mx, g[(int64_t)j * k + j].x);
+        for (int j = 0; j < k; ++j) g[(int64_t)j * k + j].x += shift * mx;
+    }
+    __syncthreads();
+    for (int j = 0; j < k; ++j) {
+        if (threadIdx.x == 0) {
+            double r = g[(int64_t)j * k + j].x;
+            if ((!(r > 0.0) || !isfinite(r)) && status[blockIdx.x] == 0) {
+                status[blockIdx.x] = j + 1;  // first failing pivot (1-based) for the error report
+                diagv[blockIdx.x] = r;
+            }
+            if (!(r > 0.0) || !isfinite(r)) r = 1e-300;
+            diag = sqrt(r);
+            g[(int64_t)j * k + j] = make_double2(diag, 0.0);
+        }
+        __syncthreads();
+        const double inv = 1.0 / diag;
+        for (int c = j + 1 + threadIdx.x; c < k; c += blockDim.x) {  // row j of R
+            double2 v = g[(int64_t)j * k + c];
+            g[(int64_t)j * k + c] = make_double2(v.x * inv, v.y * inv);
+        }
+        __syncthreads();
+        // trailing update G[a, b] -= conj(R[j, a]) R[j, b] for j < a <= b
+        for (int64_t e = threadIdx.x; e < (int64_t)(k - j - 1) * (k - j - 1); e += blockDim.x) {
+            const int a = j + 1 + (int)(e / (k - j - 1)), b = j + 1 + (int)(e % (k - j - 1));
+            if (b < a) continue;
+            const double2 ra = g[(int64_t)j * k + a], rb = g[(int64_t)j * k + b];
+            double2 v = g[(int64_t)a * k + b];
+            v.x -= ra.x * rb.x + ra.y * rb.y;
+            v.y -= ra.x * rb.y - ra.y * rb.x;
+            g[(int64_t)a * k + b] = v;
+        }
+        __syncthreads();
+    }
+}
+
+// X <- X R^{-1} row by row (R upper, from k_chol): y_c = (x_c - sum_{a<c} y_a R[a,c]) / R[c,c]
+__global__ void k_trsm_rows(const SvdPolish *__restrict__ pol, const int *__restrict__ item_pol,
+                            const int *__restrict__ item_row0, const double2 *__restrict__ G, double2 *__restrict__ X) {
+    const SvdPolish d = pol[item_pol[blockIdx.x]];
+    const int row = item_row0[blockIdx.x] + threadIdx.x;
+    if (row >= d.rows) return;
+    const int k = d.k;
+    const double2 *r = G + d.g_off;
+    double2 *x = X + d.x_off + (int64_t)row * k;
+    for (int c = 0; c < k; ++c) {
+        double2 v = x[c];
+        for (int a = 0; a < c; ++a) {
+            const double2 y = x[a], rac = r[(int64_t)a * k + c];
+            v.x -= y.x * rac.x - y.y * rac.y;
+            v.y -= y.x * rac.y + y.y * rac.x;
+        }
+        const double inv = 1.0 / r[(int64_t)c * k + c].x;
+        x[c] = make_double2(v.x * inv, v.y * inv);
+    }
+}
+
+// output blocks from dense row-major factors: side 0 block[i, j] = M[(pos+i)*ld + j]
+// (conj-transposed source: M[j*ld + pos+i] conjugated); side 1 block[j, c] = M[j*ld + pos+c]
+// (conj-transposed source: conj(M[(pos+c)*ld + j]))
+__global__ void k_scatter_dense(const SvdDense *__restrict__ d_, const double2 *__restrict__ M, double2 *__restrict__ out) {
+    const SvdDense d = d_[blockIdx.x];
+    const int64_t n = (int64_t)d.len * d.kept;
+    for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
+        double2 v;
+        if (d.side == 0) {
+            const int i = (int)(e / d.kept), j = (int)(e % d.kept);
+            v = d.ctrans ? M[d.m_off + (int64_t)j * d.ld + d.pos + i] : M[d.m_off + (int64_t)(d.pos + i) * d.ld + j];
+        } else {
+            const int j = (int)(e / d.len), c = (int)(e % d.len);
+            v = d.ctrans ? M[d.m_off + (int64_t)(d.pos + c) * d.ld + j] : M[d.m_off + (int64_t)j * d.ld + d.pos + c];
+        }
+        if (d.ctrans) v.y = -v.y;
+        out[d.out_off + e] = v;
     }
 }
 
@@ -173,15 +305,15 @@ void svd_gather(const SvdPlan &p, const double2 *A, double2 *T) {
 
 void svd_jacobi(const SvdPlan &p, double2 *T, double2 *V, int *status, int max_sweeps, double tol) {
     if (p.secs.empty()) return;
-    k_svd_jacobi<<<(unsigned)p.secs.size(), ST, 0, ctx().stream>>>(p.d_secs.as<SvdSector>(), T, V, status,
-                                                                    max_sweeps, tol);
+    k_svd_jacobi<double, ST><<<(unsigned)p.secs.size(), ST, 0, ctx().stream>>>(p.d_secs.as<SvdSector>(), T, V,
+                                                                                status, max_sweeps, tol);
     counted();
     KV_CUDA(cudaGetLastError());
 }
 
 void svd_finalize(const SvdPlan &p, const double2 *T, const double2 *V, double2 *Us, double2 *Vs, double *S) {
     if (p.secs.empty()) return;
-    k_svd_finalize<<<(unsigned)p.secs.size(), ST, sizeof(double) * p.max_q, ctx().stream>>>(
+    k_svd_finalize<double><<<(unsigned)p.secs.size(), 256, sizeof(double) * p.max_q, ctx().stream>>>(
         p.d_secs.as<SvdSector>(), T, V, Us, Vs, S);
     counted();
     KV_CUDA(cudaGetLastError());
@@ -193,6 +325,58 @@ void svd_scatter(const std::vector<SvdScatter> &sc, const SvdPlan &p, const doub
     DevBuf d = upload_vec(sc);
     k_svd_scatter<<<(unsigned)sc.size(), 256, 0, ctx().stream>>>(d.as<SvdScatter>(), p.d_secs.as<SvdSector>(), Us,
                                                                   Vs, S, out);
+    counted();
+    KV_CUDA(cudaGetLastError());
+}
+
+void svd_jacobi_f32(const SvdPlan &p, const double2 *T64, float2 *T, float2 *V, int *status, int max_sweeps,
+                    float tol) {
+    if (p.secs.empty()) return;
+    k_to_f32<<<std::max(1, ctx().num_sms * 4), 256, 0, ctx().stream>>>(T64, T, p.t_elems);
+    counted();
+    k_svd_jacobi<float, 1024><<<(unsigned)p.secs.size(), 1024, 0, ctx().stream>>>(p.d_secs.as<SvdSector>(), T, V,
+                                                                                   status, max_sweeps, tol);
+    counted();
+    KV_CUDA(cudaGetLastError());
+}
+
+void svd_finalize_f32(const SvdPlan &p, const float2 *T, const float2 *V, float2 *Us, float2 *Vs, double *S) {
+    if (p.secs.empty()) return;
+    k_svd_finalize<float><<<(unsigned)p.secs.size(), 256, sizeof(double) * p.max_q, ctx().stream>>>(
+        p.d_secs.as<SvdSector>(), T, V, Us, Vs, S);
+    counted();
+    KV_CUDA(cudaGetLastError());
+}
+
+void svd_extract(const DevBuf &pol, int npol, const SvdPlan &p, const float2 *Us, const float2 *Vs, double2 *W,
+                 int side) {
+    if (npol == 0) return;
+    k_svd_extract<<<npol, 256, 0, ctx().stream>>>(pol.as<SvdPolish>(), p.d_secs.as<SvdSector>(), Us, Vs, W, side);
+    counted();
+    KV_CUDA(cudaGetLastError());
+}
+
+void svd_chol(const DevBuf &pol, int npol, double2 *G, int *status, double *diagv, double shift) {
+    if (npol == 0) return;
+    k_chol<<<npol, 256, 0, ctx().stream>>>(pol.as<SvdPolish>(), G, status, diagv, shift);
+    counted();
+    KV_CUDA(cudaGetLastError());
+}
+
+void svd_trsm(const DevBuf &pol, const std::vector<int> &item_pol, const std::vector<int> &item_row0,
+              const double2 *G, double2 *X) {
+    if (item_pol.empty()) return;
+    DevBuf ip = upload_vec(item_pol), ir = upload_vec(item_row0);
+    k_trsm_rows<<<(unsigned)item_pol.size(), 64, 0, ctx().stream>>>(pol.as<SvdPolish>(), ip.as<int>(), ir.as<int>(),
+                                                                    G, X);
+    counted();
+    KV_CUDA(cudaGetLastError());
+}
+
+void svd_scatter_dense(const std::vector<SvdDense> &d, const double2 *M, double2 *out) {
+    if (d.empty()) return;
+    DevBuf dd = upload_vec(d);
+    k_scatter_dense<<<(unsigned)d.size(), 256, 0, ctx().stream>>>(dd.as<SvdDense>(), M, out);
     counted();
     KV_CUDA(cudaGetLastError());
 }

@@ -33,7 +33,30 @@ struct SvdPlan {
     void upload() { d_secs = upload_vec(secs); d_gathers = upload_vec(gathers); }
 };
 
+// FP64 polish of the kept factor of one sector (mixed mode): W (the FP32
+// kept singular vectors of the other side) at w_off, the factor X
+// (rows x k, row-major) at x_off, its Gram / Cholesky factor (k x k) at g_off
+struct SvdPolish {
+    int64_t x_off, g_off, w_off;
+    int sector, rows, k, pad;
+};
+// one output block copied from a dense row-major factor M (ld columns);
+// ctrans: the block is taken from M^H
+struct SvdDense {
+    int64_t out_off, m_off;
+    int side, pos, len, kept, ld, ctrans;
+};
+
 void svd_gather(const SvdPlan &p, const double2 *A, double2 *T);
+void svd_jacobi_f32(const SvdPlan &p, const double2 *T64, float2 *T, float2 *V, int *status, int max_sweeps,
+                    float tol);
+void svd_finalize_f32(const SvdPlan &p, const float2 *T, const float2 *V, float2 *Us, float2 *Vs, double *S);
+void svd_extract(const DevBuf &pol, int npol, const SvdPlan &p, const float2 *Us, const float2 *Vs, double2 *W,
+                 int side);
+void svd_chol(const DevBuf &pol, int npol, double2 *G, int *status, double *diagv, double shift);
+void svd_trsm(const DevBuf &pol, const std::vector<int> &item_pol, const std::vector<int> &item_row0,
+              const double2 *G, double2 *X);
+void svd_scatter_dense(const std::vector<SvdDense> &d, const double2 *M, double2 *out);
 void svd_jacobi(const SvdPlan &p, double2 *T, double2 *V, int *status, int max_sweeps, double tol);
 void svd_finalize(const SvdPlan &p, const double2 *T, const double2 *V, double2 *Us, double2 *Vs, double *S);
 void svd_scatter(const std::vector<SvdScatter> &sc, const SvdPlan &p, const double2 *Us, const double2 *Vs,

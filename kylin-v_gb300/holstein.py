@@ -419,7 +419,8 @@ def random_mps(chain: HolsteinChain, D: int, seed: int) -> list:
     Entries are re + i im with re, im ~ N(0, 1); each left-charge sector
     matrix of a site (rows D_l(q), columns the concatenated (sigma, D_r) blocks)
     is replaced by the orthonormal-row factor of its LQ decomposition and the
-    triangular factor is carried into the site on the left."""
+    triangular factor is carried into the site on the left (rescaled by its
+    norm, which only changes the overall scale)."""
     rng = np.random.default_rng(seed)
     bonds = random_mps_structure(chain, D)
     dims = chain.site_dims()
@@ -453,6 +454,10 @@ def random_mps(chain: HolsteinChain, D: int, seed: int) -> list:
                 t.blocks[i] = (t.blocks[i][0], Qm[:, col:col + w].reshape(m.shape[0], 1, w).copy())
                 col += w
             carry[ql] = Lf
+        # the carried factors only set the overall scale (normalised at the
+        # end); rescale them so long chains neither overflow nor underflow
+        cn = np.sqrt(sum(np.vdot(x, x).real for x in carry.values()))
+        carry = {q: x / cn for q, x in carry.items()}
         prev = sites[s - 1]
         prev.blocks = [(q, np.einsum("aib,bc->aic", a, carry[q[2]])) for q, a in prev.blocks]
     nrm = sites[0].norm()

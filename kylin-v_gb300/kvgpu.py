@@ -18,6 +18,8 @@ LIB_PATH = os.path.join(HERE, "_build", "libkvgpu.so")
 
 KV_FP64 = 0
 KV_MIXED_TF32 = 1
+KV_MIXED_GEMM = 2  # tensor-core contractions, FP64 SVD
+KV_MIXED_SVD = 3   # FP64 contractions, mixed SVD
 OP_N, OP_T, OP_C = 111, 112, 113
 MODULES = ("Evl-0", "Evl-1", "Evl-2", "SVD", "Update", "Sweep")
 
@@ -60,8 +62,8 @@ def lib():
         L.kv_env_update.argtypes = [ctypes.c_int, vp, vp, vp, ctypes.c_int, pvp]
         L.kv_lanczos_expm.argtypes = [ctypes.c_int, vp, vp, vp, vp, vp, ctypes.c_double, ctypes.c_int,
                                       ctypes.c_double, ctypes.c_int, ctypes.c_int, pvp, ip]
-        L.kv_svd_truncate.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, pvp, pvp,
-                                      ip, ip]
+        L.kv_svd_truncate.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                      pvp, pvp, ip, ip]
         L.kv_tdvp_create.argtypes = [ctypes.c_int, pvp, pvp, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                      ctypes.c_int, ctypes.c_double, ctypes.c_int, pvp]
         L.kv_tdvp_sweep.argtypes = [vp, ctypes.c_int]
@@ -104,6 +106,21 @@ class Tensor:
         check(L.kv_tensor_create(rank, dirs, nb, shapes.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
                                  qns.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
                                  data.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.byref(out)))
+        return cls(out.value)
+
+    @classmethod
+    def from_pinned(cls, t: BlockTensor, data_ptr: int) -> "Tensor":
+        """Like from_host, with the block data read from a caller-owned host
+        buffer (e.g. pinned memory) at data_ptr (complex128, block order)."""
+        L = lib()
+        rank, nb = t.rank, len(t.blocks)
+        dirs = (ctypes.c_int * rank)(*t.dirs)
+        shapes = np.array([s for _, a in t.blocks for s in a.shape] or [0], dtype=np.int32)
+        qns = np.array([q for qn, _ in t.blocks for q in qn] or [0], dtype=np.int32)
+        out = ctypes.c_void_p()
+        check(L.kv_tensor_create(rank, dirs, nb, shapes.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                 qns.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                 ctypes.cast(data_ptr, ctypes.POINTER(ctypes.c_double)), ctypes.byref(out)))
         return cls(out.value)
 
     def info(self):
@@ -178,13 +195,13 @@ def local_krylov(nsite, L, psi, W1, W2, R, dt, max_iter, tol, reverse=False, pre
     return Tensor(out.value), it.value
 
 
-def svd_impl(A, r1, left2right, tol, max_dim):
+def svd_impl(A, r1, left2right, tol, max_dim, precision=KV_FP64):
     """svd_impl<R1,R2> (holstein/svd.h:296-440); returns (U, V, n_kept, n_total)."""
     A = _t(A)
     U, V = ctypes.c_void_p(), ctypes.c_void_p()
     nk, nt = ctypes.c_int(), ctypes.c_int()
-    check(lib().kv_svd_truncate(A.ptr, r1, int(left2right), tol, max_dim, ctypes.byref(U), ctypes.byref(V),
-                                ctypes.byref(nk), ctypes.byref(nt)))
+    check(lib().kv_svd_truncate(A.ptr, r1, int(left2right), tol, max_dim, precision, ctypes.byref(U),
+                                ctypes.byref(V), ctypes.byref(nk), ctypes.byref(nt)))
     return Tensor(U.value), Tensor(V.value), nk.value, nt.value
 
 
