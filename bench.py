@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-compare", action="store_true", help="skip the mixed-vs-FP64 comparison leg")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--molecules", type=int, default=None,
+                    help="shorter chain with the same local structure (profiling runs)")
     return ap.parse_args()
 
 
@@ -197,7 +199,7 @@ def run_ours(args):
         tdist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     G.init(local)
     prec = G.KV_MIXED_TF32 if args.precision == "mixed" else G.KV_FP64
-    chain, D, d, mps, mpo = build_workload(args.config, 1234 + rank)
+    chain, D, d, mps, mpo = build_workload(args.config, 1234 + rank, n_mol=args.molecules)
     mode = d["mode"]
     t = G.TDVP(mps, mpo, d["tol_svd"], d["tol_exp"], D, d["max_iter"], d["dt"], prec)
     sweep = t.two_site if mode == 2 else t.one_site
@@ -281,7 +283,8 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None,
         "dtype": "c64 3M TF32x3 contractions + c128 Lanczos/SVD polish" if prec else "c128",
         "data": "synthetic (seeded random right-canonical U(1) MPS, Holstein FSM MPO)",
-        "config": {"workload": args.config, "n_sites": chain.n_sites, "D": D, "mode": f"{mode}-site TDVP",
+        "config": {"workload": args.config + (f" ({args.molecules} molecules)" if args.molecules else ""),
+                   "n_sites": chain.n_sites, "D": D, "mode": f"{mode}-site TDVP",
                    "dt": d["dt"], "max_iter": d["max_iter"], "precision": args.precision, "l2_flush": True,
                    "replicas_per_gpu": 1},
         "modules_ms_per_step": {k: v / args.steps for k, v in modules.items()},
