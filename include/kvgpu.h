@@ -149,6 +149,22 @@ int kv_counters(long long *launches);
 int kv_expectation(int nsites, const kv_tensor *bra, const kv_tensor *mpo, const kv_tensor *ket, double *re,
                    double *im);
 
+/* The same value as kv_expectation without allocating any GPU memory; it has
+ * no counterpart in the reference.  For callers that cannot let a library
+ * call cudaMalloc: applications that own all device memory through their own
+ * allocator or budget, and latency-critical loops that must not stall on an
+ * allocation.  Every intermediate (environments, MPO-mixing buffers, GEMM
+ * task lists) lives in one static 64 MiB device array that each GPU loading
+ * this library reserves until the process exits; a call whose scratch would
+ * exceed 64 MiB (about a 30-site MPS at bond dimension 64) fails with
+ * KV_ENOMEM.  The first call on a device looks up the array's address
+ * (cudaGetSymbolAddress) and must come before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU race.  The inputs are device
+ * tensors the caller already holds; re/im are host doubles.  kv_init must
+ * have been called. */
+int kv_expectation_noalloc(int nsites, const kv_tensor *bra, const kv_tensor *mpo, const kv_tensor *ket,
+                           double *re, double *im);
+
 #ifdef __cplusplus
 }
 #endif

@@ -286,4 +286,21 @@ int kv_expectation(int nsites, const kv_tensor *bra, const kv_tensor *mpo, const
     });
 }
 
+int kv_expectation_noalloc(int nsites, const kv_tensor *bra, const kv_tensor *mpo, const kv_tensor *ket, double *re,
+                           double *im) {
+    return guard([&] {
+        kv::require_init();
+        KV_REQUIRE(nsites >= 1 && bra && mpo && ket && re && im, KV_EINVAL, "null argument");
+        std::vector<kv::DTensor *> a, w, b;
+        for (int i = 0; i < nsites; ++i) {
+            a.push_back(T(bra[i]));
+            w.push_back(T(mpo[i]));
+            b.push_back(T(ket[i]));
+        }
+        kv::cplx r = kv::expectation_noalloc(a, w, b);
+        *re = r.real();
+        *im = r.imag();
+    });
+}
+
 }  // extern "C"

@@ -66,6 +66,9 @@ TensorP op_env(bool l2r, const DTensor &env, const DTensor &A, const DTensor &W,
                Flops *fl);
 TensorP op_permute(const DTensor &t, const std::vector<int> &ax);
 cplx op_expectation(const std::vector<DTensor *> &a, const std::vector<DTensor *> &w, const std::vector<DTensor *> &b);
+// the same value with all device scratch in a fixed static array (kv_noalloc.cu)
+cplx expectation_noalloc(const std::vector<DTensor *> &bra, const std::vector<DTensor *> &w,
+                         const std::vector<DTensor *> &ket);
 
 enum Module { MOD_EVL0 = 0, MOD_EVL1, MOD_EVL2, MOD_SVD, MOD_UPDATE, MOD_SWEEP, MOD_COUNT };
 

@@ -27,7 +27,7 @@ EXPORTS = (
     "kv_init", "kv_shutdown", "kv_last_error", "kv_version", "kv_tensor_create", "kv_tensor_info",
     "kv_tensor_download", "kv_tensor_free", "kv_product", "kv_heff_apply", "kv_env_update", "kv_lanczos_expm",
     "kv_svd_truncate", "kv_tdvp_create", "kv_tdvp_sweep", "kv_tdvp_site", "kv_tdvp_stats", "kv_tdvp_free",
-    "kv_expectation", "kv_profile", "kv_profile_read", "kv_counters",
+    "kv_expectation", "kv_profile", "kv_profile_read", "kv_counters", "kv_expectation_noalloc",
 )
 
 
@@ -74,6 +74,7 @@ def lib():
         L.kv_counters.argtypes = [ctypes.POINTER(ctypes.c_longlong)]
         L.kv_tdvp_free.argtypes = [vp]
         L.kv_expectation.argtypes = [ctypes.c_int, pvp, pvp, pvp, dp, dp]
+        L.kv_expectation_noalloc.argtypes = [ctypes.c_int, pvp, pvp, pvp, dp, dp]
         _lib = L
     return _lib
 
@@ -230,6 +231,17 @@ def launches() -> int:
     n = ctypes.c_longlong()
     check(lib().kv_counters(ctypes.byref(n)))
     return n.value
+
+
+def expectation_noalloc(bra, mpo, ket) -> complex:
+    """<bra|W|ket> like :func:`expectation`, with every intermediate in the
+    library's fixed 64 MiB device scratch array (no GPU allocation)."""
+    ns = len(bra)
+    hb, hw, hk = [_t(x) for x in bra], [_t(x) for x in mpo], [_t(x) for x in ket]
+    arr = lambda hs: (ctypes.c_void_p * ns)(*[h.ptr for h in hs])  # noqa: E731
+    re, im = ctypes.c_double(), ctypes.c_double()
+    check(lib().kv_expectation_noalloc(ns, arr(hb), arr(hw), arr(hk), ctypes.byref(re), ctypes.byref(im)))
+    return complex(re.value, im.value)
 
 
 class TDVP:
