@@ -129,36 +129,102 @@ __global__ void __launch_bounds__(KT) k_normalize(KrylovState *st, const double2
 
 // T = tridiag(Re alpha, beta upper); c = Z exp(img Lambda) Z^H e0 with
 // img = -i (forward) or +i (reverse): holstein/exponential.h:163-183.
-__global__ void k_tridiag_exp(KrylovState *st, int reverse) {
-    __shared__ double H[2 * kMaxKrylov * kMaxKrylov];
-    __shared__ double Z[2 * kMaxKrylov * kMaxKrylov];
-    if (threadIdx.x != 0) return;
+// One warp: cyclic two-sided complex Jacobi (the rotations of kv_jacobi.cuh),
+// lane 0 forms each rotation, the lanes update the two rows, the two columns
+// and the eigenvector columns in parallel.
+__global__ void __launch_bounds__(32) k_tridiag_exp(KrylovState *st, int reverse) {
+    __shared__ double2 H[kMaxKrylov][kMaxKrylov + 1];
+    __shared__ double2 Z[kMaxKrylov][kMaxKrylov + 1];
+    __shared__ double2 ph[kMaxKrylov];
+    __shared__ double rot[3];  // cs, s_re, s_im
+    __shared__ int any_rot;
+    const int lane = threadIdx.x;
     const int n = st->iters;
     if (n <= 0) return;
-    for (int i = 0; i < 2 * n * n; ++i) H[i] = 0.0;
-    for (int i = 0; i < n; ++i) {
-        H[2 * (i * n + i)] = st->alpha[i].x;
-        if (i + 1 < n) {
-            H[2 * (i * n + i + 1)] = st->beta[i].x;
-            H[2 * (i * n + i + 1) + 1] = st->beta[i].y;
-            H[2 * ((i + 1) * n + i)] = st->beta[i].x;
-            H[2 * ((i + 1) * n + i) + 1] = -st->beta[i].y;
+    for (int i = 0; i < n; ++i)
+        if (lane < n) {
+            double2 h = make_double2(0.0, 0.0);
+            if (i == lane) h.x = st->alpha[i].x;
+            else if (lane == i + 1) h = st->beta[i];                                  // upper (i, i+1)
+            else if (i == lane + 1) h = make_double2(st->beta[lane].x, -st->beta[lane].y);  // lower
+            H[i][lane] = h;
+            Z[i][lane] = make_double2(i == lane ? 1.0 : 0.0, 0.0);
         }
+    __syncwarp();
+    for (int sweep = 0; sweep < 60; ++sweep) {
+        if (lane == 0) any_rot = 0;
+        __syncwarp();
+        for (int p = 0; p < n - 1; ++p)
+            for (int q = p + 1; q < n; ++q) {
+                if (lane == 0) {
+                    const double a = H[p][p].x, b = H[q][q].x;
+                    const double cr = H[p][q].x, ci = H[p][q].y;
+                    const double ac = sqrt(cr * cr + ci * ci);
+                    kvj::Rot<double> r;
+                    r.cs = 0.0;
+                    if (ac > 1e-300 && ac > 1e-17 * (fabs(a) + fabs(b))) {
+                        const double z = (b - a) / (2.0 * ac);
+                        const double t = (z >= 0.0 ? 1.0 : -1.0) / (fabs(z) + sqrt(1.0 + z * z));
+                        r.cs = 1.0 / sqrt(1.0 + t * t);
+                        const double sn = t * r.cs;
+                        r.s_re = sn * cr / ac;
+                        r.s_im = sn * ci / ac;
+                        any_rot = 1;
+                    }
+                    rot[0] = r.cs;
+                    rot[1] = r.s_re;
+                    rot[2] = r.s_im;
+                }
+                __syncwarp();
+                kvj::Rot<double> r;
+                r.cs = rot[0];
+                r.s_re = rot[1];
+                r.s_im = rot[2];
+                __syncwarp();  // every lane has read rot before lane 0 writes the next one
+                if (r.cs == 0.0) continue;  // warp-uniform: no rotation for this pair
+                if (lane < n) {  // columns p, q  (H <- H J)
+                    double2 x = H[lane][p], y = H[lane][q];
+                    kvj::rotate_pair(r, x.x, x.y, y.x, y.y);
+                    H[lane][p] = x;
+                    H[lane][q] = y;
+                }
+                __syncwarp();
+                if (lane < n) {  // rows p, q  (H <- J^H H)
+                    double xr = H[p][lane].x, xi = -H[p][lane].y, yr = H[q][lane].x, yi = -H[q][lane].y;
+                    kvj::rotate_pair(r, xr, xi, yr, yi);
+                    H[p][lane] = make_double2(xr, -xi);
+                    H[q][lane] = make_double2(yr, -yi);
+                    double2 zx = Z[lane][p], zy = Z[lane][q];  // Z <- Z J
+                    kvj::rotate_pair(r, zx.x, zx.y, zy.x, zy.y);
+                    Z[lane][p] = zx;
+                    Z[lane][q] = zy;
+                }
+                __syncwarp();
+                if (lane == 0) {
+                    H[p][q] = H[q][p] = make_double2(0.0, 0.0);
+                    H[p][p].y = H[q][q].y = 0.0;
+                }
+                __syncwarp();
+            }
+        __syncwarp();
+        if (!any_rot) break;
     }
-    kvj::hermitian_jacobi<double>(n, H, Z, 60);
     const double sg = reverse ? 1.0 : -1.0;
-    for (int i = 0; i < n; ++i) {
+    if (lane < n) {
+        const double lam = H[lane][lane].x;
+        ph[lane] = make_double2(cos(lam), sg * sin(lam));  // exp(img lambda)
+    }
+    __syncwarp();
+    if (lane < n) {
         double cr = 0.0, ci = 0.0;
         for (int j = 0; j < n; ++j) {
-            double lam = H[2 * (j * n + j)];
-            double er = cos(lam), ei = sg * sin(lam);              // exp(img lam)
-            double zr = Z[2 * (i * n + j)], zi = Z[2 * (i * n + j) + 1];
-            double z0r = Z[2 * j], z0i = -Z[2 * j + 1];             // conj(Z[0, j])
-            double pr = zr * er - zi * ei, pi = zr * ei + zi * er;
+            const double2 z = Z[lane][j], e = ph[j];
+            const double z0r = Z[0][j].x, z0i = -Z[0][j].y;  // conj(Z[0, j])
+            const double pr = z.x * e.x - z.y * e.y, pi = z.x * e.y + z.y * e.x;
             cr += pr * z0r - pi * z0i;
             ci += pr * z0i + pi * z0r;
         }
-        st->coef[i] = make_double2(cr, ci);
+        st->coef[lane] = make_double2(cr, ci);
     }
 }
 
