@@ -221,6 +221,8 @@ void build_tiles(ProductPlan &P, const std::vector<int64_t> &target_off, int til
     GemmPlan &g = P.gemm;
     g.tiles.clear();
     g.segs.clear();
+    g.tile_m = tile_m;
+    g.tile_n = tile_n;
     for (size_t b = 0; b < P.per_out.size(); ++b) {
         const int M = P.mn[b].first, N = P.mn[b].second;
         const int sb = (int)g.segs.size();

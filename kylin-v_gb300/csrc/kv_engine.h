@@ -8,8 +8,8 @@ namespace kv {
 inline bool gemm_mixed(int precision) { return precision == KV_MIXED_TF32 || precision == KV_MIXED_GEMM; }
 inline bool svd_mixed(int precision) { return precision == KV_MIXED_TF32 || precision == KV_MIXED_SVD; }
 // Output tile shape of the grouped GEMM for a precision mode.
-inline int kTileM(int precision) { return gemm_mixed(precision) ? 128 : 32; }
-inline int kTileN(int precision) { return gemm_mixed(precision) ? 64 : 32; }
+inline int kTileM(int precision) { return gemm_mixed(precision) ? kMixedTileM : 32; }
+inline int kTileN(int precision) { return gemm_mixed(precision) ? kMixedTileN : 32; }
 
 // reference flop count split by who executes it here: the grouped GEMM
 // (product<> pairs) or the MPO mixing kernel (env_mps_mpo zgemms)

@@ -193,13 +193,45 @@ struct GemmTile {
     int ldc, M, N, m0, n0;
     int seg_begin, seg_end;
 };
+// Tile shape of the tensor-core path (kv_tc.cu).
+constexpr int kMixedTileM = 128, kMixedTileN = 32;
+
+// Tensor-core path: one operand block viewed as GEMM rows x K, sliced into
+// fixed-point digit panels (dst_off: FP16 elements into the panel buffer,
+// exp_off: first of its per-row exponents).
+struct SliceJob {
+    int64_t src_off, dst_off;
+    int rows, K, ld;
+    int trans;  // 0: (row, k) at src[row*ld + k]; 1: at src[k*ld + row]
+    int conj;   // negate the imaginary part
+    int exp_off, nkc, pad;
+};
+// Tensor-core path: a segment's sliced A and B blocks.
+struct SegX {
+    int64_t a_pan, b_pan;
+    int nkc, a_exp, b_exp, pad;
+};
+
+struct GemmPlan;
+void plan_mixed(GemmPlan &g);  // slicing jobs of a plan built with the tensor-core tile shape
+
 struct GemmPlan {
     std::vector<GemmTile> tiles;
     std::vector<GemmSeg> segs;
     DevBuf d_tiles, d_segs;
     double ref_flops = 0.0;  // sum of 8*M*N*K over the reference's zgemm pairs
     int max_k = 0;
-    void upload() { d_tiles = upload_vec(tiles); d_segs = upload_vec(segs); }
+    int tile_m = 0, tile_n = 0;
+    // tensor-core path only
+    std::vector<SliceJob> ajobs, bjobs;
+    std::vector<SegX> xsegs;
+    int64_t a_planes = 0, b_planes = 0, a_exps = 0, b_exps = 0;
+    DevBuf d_ajobs, d_bjobs, d_xsegs;
+    void upload() {
+        d_tiles = upload_vec(tiles);
+        d_segs = upload_vec(segs);
+        if (tile_m == kMixedTileM && tile_n == kMixedTileN) plan_mixed(*this);
+    }
 };
 
 // MPO mixing (env_mps_mpo family) with merging of equal output blocks.

@@ -1,23 +1,52 @@
-// Mixed-precision grouped complex GEMM on the 5th-generation tensor cores.
+// Mixed-precision grouped complex GEMM on the 5th-generation tensor cores
+// with exact accumulation.
 //
-// Same task format as the FP64 kernel (one CTA per 128 x 64 output tile,
-// summing every block pair that accumulates into it).  Complex products use
-// the 3M (Gauss) form
-//     T1 = Ar Br,  T2 = Ai Bi,  T3 = (Ar + Ai)(Br + Bi)
-//     Cr = T1 - T2,  Ci = T3 - T1 - T2
-// with every real operand split into three TF32 parts x = hi + mid + lo
-// (each the round-to-nearest TF32 of the remaining residual, ~33 bits in all)
-// and each real product formed as the six terms of order <= 2^-22:
-// hi*hi + hi*mid + mid*hi + hi*lo + mid*mid + lo*hi.
-// The 18 MMAs per K-step run as tcgen05.mma.kind::tf32 (M=128, N=64, K=8)
-// issued by one thread into three FP32 accumulators in tensor memory;
-// operands are staged by all threads from the FP64 tensors into shared memory
-// in the canonical K-major no-swizzle layout (8-row x 16-byte core matrices,
-// K-adjacent core matrices 128 B apart, 8-row groups 1024 B apart).  The
-// epilogue reads the accumulators with tcgen05.ld, forms Cr/Ci and writes
-// FP64.  All mbarrier waits are bounded; on timeout the CTA records an error,
-// drains (bounded) and frees its tensor memory.
+// GB300 runs FP64 arithmetic at a small fraction of its FP32 and tensor
+// rates, so no FP64 instruction is issued per element of a tile.  Instead:
+//
+//  1. Slicing (k_slice, once per operand per call).  Every GEMM row of an A
+//     block (and every GEMM column of a B block) gets a binary exponent e
+//     with max_k |x| < 2^e over that row; each real value becomes the
+//     fixed-point integer X = round(x 2^(29-e)), |X| <= 2^29, written as four
+//     balanced base-256 digits X = d0 2^24 + d1 2^16 + d2 2^8 + d3
+//     (|d0| <= 64, |d1..d3| <= 128) in FP16 (exact).  For the 3M complex form
+//     three values are sliced per element: re, im and re + im (the last as
+//     the exact integer sum X_re + X_im).  Integer arithmetic only.  The
+//     digits are written directly in the tensor cores' shared-memory panel
+//     layout (K-major, no swizzle: 8-row x 16-byte core matrices, K-adjacent
+//     core matrices 128 B apart, 8-row groups 256 B apart), one 16-deep K
+//     panel after another, all 12 digit planes of a panel contiguous, so a
+//     pipeline stage is one bulk copy per operand.
+//  2. Products (k_gemm_tc).  T1 = Ar Br, T2 = Ai Bi, T3 = As Bs are formed as
+//     digit-pair products of orders o = i + j <= 4 (13 per real product, 39
+//     tcgen05.mma.kind::f16 of M=128, N=32, K=16 per K panel) into 15 FP32
+//     accumulators in tensor memory.  Every digit product is an integer of
+//     at most 2^14 in magnitude, and at most 336 K-steps are accumulated
+//     between drains, so every accumulator is an integer below 2^24 and the
+//     FP32 accumulation is exact.
+//  3. Drains (epilogue warps).  At the end of each segment (one block pair)
+//     or every 336 K, the accumulators are read with tcgen05.ld, converted to
+//     int64 (sum_o P_o 2^(8(4-o))), combined into Cr = T1 - T2 and
+//     Ci = T3 - T1 - T2, aligned to the tile's largest row/column exponents
+//     and added to int64 running sums; the final sums are converted to FP64
+//     by integer operations (exponent and mantissa assembled directly).
+//
+// Result: each output element is exact up to the rounding of X (2^-30 of
+// the row/column maximum) and the dropped digit orders 5 and 6 (below
+// 2^-34 of the same scale), i.e. ~1e-10 relative to max|A_row| max|B_col| K,
+// with no FP64 arithmetic in the GEMM.
+//
+// Pipeline: warp 0 (one thread) issues the bulk copies of 3 stages
+// (cp.async.bulk completing on mbarriers), warp 1 allocates tensor memory and
+// one thread issues the MMAs (tcgen05.commit frees a stage and signals a
+// drain), warps 2-5 drain (each reads its 32-lane quarter of tensor memory).
+// Every mbarrier wait is bounded; on timeout the CTA records an error, waits
+// (bounded) for its copies and MMAs in flight, frees tensor memory and exits.
+#include <cuda_fp16.h>
+
 #include <cstdint>
+#include <map>
+#include <utility>
 
 #include "kv_internal.h"
 
@@ -25,34 +54,104 @@ namespace kv {
 
 namespace {
 
-constexpr int BM = 128, BN = 64, BK = 32;
-constexpr int A_PLANE = BM * BK * 4;  // bytes per TF32 plane of A
-constexpr int B_PLANE = BN * BK * 4;
-constexpr int NSPLIT = 3;           // TF32 parts per real operand
-constexpr int NPLANE = 3 * NSPLIT;  // (re, im, re+im) x parts
-constexpr int SMEM_BYTES = NPLANE * A_PLANE + NPLANE * B_PLANE + 1024 + 64;
-constexpr uint32_t TMEM_COLS = 256;  // 3 accumulators x 64 columns, rounded to a power of two
+constexpr int BM = kMixedTileM, BN = kMixedTileN, BKC = 16;
+constexpr int NDIG = 4, NORD = 5, NCOMP = 3;
+constexpr int NPL = NCOMP * NDIG;              // digit planes per operand
+constexpr int A_PANEL = NPL * BM * BKC;        // FP16 elements per A panel (all planes)
+constexpr int B_PANEL = NPL * BN * BKC;
+constexpr int A_BYTES = A_PANEL * 2, B_BYTES = B_PANEL * 2;
+constexpr int PLANE_A = BM * BKC * 2, PLANE_B = BN * BKC * 2;  // bytes per plane within a panel
+constexpr int STAGES = 3;
+constexpr int NACC = NCOMP * NORD;             // accumulators of BN columns
+constexpr uint32_t TMEM_COLS = 512;            // NACC * BN = 480, rounded to a power of two
+constexpr int KDRAIN = 336;                    // K-steps accumulated exactly between drains
+constexpr int GKC = KDRAIN / BKC;              // K panels per drain group
+constexpr int FRAC = 29;
+constexpr int kZeroExp = -4000;                // exponent of an all-zero (or padding) row
 constexpr long long WAIT_LIMIT = 1ll << 22;
+constexpr int SMEM_BYTES = STAGES * (A_BYTES + B_BYTES) + 1024 + 512;
 
-// plane order: (re, im, re+im) x (hi, mid, lo): plane = 3 * component + part
-__device__ __forceinline__ uint32_t kmaj_off(int r, int k) {
-    return (uint32_t)(((r >> 3) * (BK / 4) + (k >> 2)) * 128 + (r & 7) * 16 + (k & 3) * 4);
+static_assert(NACC * BN <= (int)TMEM_COLS, "accumulators exceed tensor memory");
+static_assert(A_BYTES + B_BYTES < (1 << 20), "transaction count per stage");
+
+// ----------------------------------------------------------- slicing
+// round(x 2^(29-e)) for |x| < 2^e, from the bits of x (integer operations only)
+__device__ __forceinline__ int fixq(double x, int e) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    const int E = (int)((u >> 52) & 0x7FF);
+    const int s = 1046 + e - E;  // X = m >> s with m the 53-bit significand; s >= 24 when |x| < 2^e
+    if (E == 0 || s >= 64) return 0;
+    int X;
+    if (s < 24) X = 1 << 29;  // only for non-finite input (the exponent came from an inf/NaN row)
+    else X = (int)((((u & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull) + (1ull << (s - 1))) >> s);
+    return (u >> 63) ? -X : X;
 }
 
+__device__ __forceinline__ void digits(int X, int d[NDIG]) {
+#pragma unroll
+    for (int i = NDIG - 1; i > 0; --i) {
+        d[i] = ((X + 128) & 255) - 128;
+        X = (X - d[i]) >> 8;  // exact
+    }
+    d[0] = X;
+}
+
+// element offset of (row r, k) inside one plane of a TR x 16 panel
+template <int TR>
+__device__ __forceinline__ int panel_off(int r, int k) {
+    return (r >> 3) * 128 + (k >> 3) * 64 + (r & 7) * 8 + (k & 7);
+}
+
+template <int TR>
+__global__ void __launch_bounds__(256) k_slice(const SliceJob *__restrict__ jobs, const double2 *__restrict__ src,
+                                               __half *__restrict__ dst, int *__restrict__ exps, double alpha,
+                                               const int *skip) {
+    if (skip && *skip) return;
+    const SliceJob j = jobs[blockIdx.x];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int prow = ((j.rows + TR - 1) / TR) * TR;
+    const int kpad = j.nkc * BKC;
+    const double2 *s = src + j.src_off;
+    const bool scale = alpha != 1.0;
+    for (int r = warp; r < prow; r += 8) {
+        unsigned long long mx = 0;
+        if (r < j.rows)
+            for (int k = lane; k < j.K; k += 32) {
+                double2 v = s[j.trans ? (int64_t)k * j.ld + r : (int64_t)r * j.ld + k];
+                if (scale) { v.x *= alpha; v.y *= alpha; }
+                const unsigned long long br = (unsigned long long)__double_as_longlong(v.x) & 0x7FFFFFFFFFFFFFFFull;
+                const unsigned long long bi = (unsigned long long)__double_as_longlong(v.y) & 0x7FFFFFFFFFFFFFFFull;
+                mx = max(mx, max(br, bi));
+            }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) mx = max(mx, (unsigned long long)__shfl_xor_sync(0xFFFFFFFFu, mx, o));
+        const int e = mx ? (int)(mx >> 52) - 1022 : kZeroExp;
+        if (lane == 0) exps[j.exp_off + r] = e;
+        __half *pan = dst + j.dst_off + (int64_t)(r / TR) * j.nkc * (NPL * TR * BKC);
+        const int rr = r % TR;
+        for (int k = lane; k < kpad; k += 32) {
+            int xr = 0, xi = 0;
+            if (r < j.rows && k < j.K) {
+                double2 v = s[j.trans ? (int64_t)k * j.ld + r : (int64_t)r * j.ld + k];
+                if (scale) { v.x *= alpha; v.y *= alpha; }
+                xr = fixq(v.x, e);
+                xi = fixq(j.conj ? -v.y : v.y, e);
+            }
+            const int xs[NCOMP] = {xr, xi, xr + xi};
+            __half *p = pan + (int64_t)(k / BKC) * (NPL * TR * BKC) + panel_off<TR>(rr, k & (BKC - 1));
+#pragma unroll
+            for (int c = 0; c < NCOMP; ++c) {
+                int d[NDIG];
+                digits(xs[c], d);
+#pragma unroll
+                for (int i = 0; i < NDIG; ++i) p[(c * NDIG + i) * (TR * BKC)] = __int2half_rn(d[i]);
+            }
+        }
+    }
+}
+
+// -------------------------------------------------------- tensor-core GEMM
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ float tf32_rna(float x) {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return __uint_as_float(r);
-}
-
-__device__ __forceinline__ void split3(double x, float &hi, float &mid, float &lo) {
-    hi = tf32_rna((float)x);
-    const double r = x - (double)hi;
-    mid = tf32_rna((float)r);
-    lo = tf32_rna((float)(r - (double)mid));
-}
 
 // UMMA shared-memory descriptor: start >> 4 (bits 0-13), leading byte offset
 // >> 4 (16-29), stride byte offset >> 4 (32-45), descriptor version 1 (46-47),
@@ -66,21 +165,32 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo, uint
     return d;
 }
 
-// instruction descriptor, kind::tf32: D = F32 (bits 4-5 = 1), A = B = TF32
-// (bits 7-9, 10-12 = 2), both K-major, N >> 3 at bit 17, M >> 4 at bit 24
-constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                           ((uint32_t)(BM >> 4) << 24);
+// instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = F16
+// (bits 7-9, 10-12 = 0), both K-major, N >> 3 at bit 17, M >> 4 at bit 24
+constexpr uint32_t IDESC = (1u << 4) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
 
-__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
     asm volatile(
         "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
         "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate));
 }
 
 __device__ __forceinline__ void mma_commit(uint32_t mbar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
                  : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t mbar, int count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mbar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
 }
 
 __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
@@ -97,186 +207,245 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
     return false;
 }
 
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
-    uint32_t r[32];
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t mbar) {
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+        "l"(src), "r"(bytes), "r"(mbar)
+        : "memory");
 }
 
-__global__ void __launch_bounds__(128, 1) k_gemm_tc(const GemmTile *__restrict__ tiles, const GemmSeg *__restrict__ segs,
-                                                    const double2 *__restrict__ A, const double2 *__restrict__ B,
-                                                    double2 *__restrict__ C, double alpha, const int *skip,
-                                                    int *err) {
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float *v) {
+    uint32_t r0, r1, r2, r3;
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(taddr));
+    v[0] = __uint_as_float(r0);
+    v[1] = __uint_as_float(r1);
+    v[2] = __uint_as_float(r2);
+    v[3] = __uint_as_float(r3);
+}
+
+__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+
+// v / 2^sh rounded to nearest, sh >= 0
+__device__ __forceinline__ long long sra_round(long long v, int sh) {
+    if (sh <= 0) return v;
+    if (sh >= 62) return 0;
+    return (v + (1ll << (sh - 1))) >> sh;
+}
+
+// v 2^sc as FP64, rounded to nearest even, from integer operations
+__device__ __forceinline__ double i64_ldexp(long long v, int sc) {
+    if (v == 0) return 0.0;
+    const unsigned long long neg = v < 0 ? 1ull : 0ull;
+    unsigned long long a = neg ? (unsigned long long)(-v) : (unsigned long long)v;
+    const int lz = __clzll((long long)a);
+    a <<= lz;  // leading one at bit 63
+    int ex = 63 - lz + sc;
+    unsigned long long mant = a >> 11;
+    const unsigned long long rem = a & 0x7FFull;
+    if (rem > 0x400ull || (rem == 0x400ull && (mant & 1ull))) {
+        ++mant;
+        if (mant >> 53) { mant >>= 1; ++ex; }
+    }
+    const int E = ex + 1023;
+    if (E <= 0) return 0.0;
+    if (E >= 2047) return __longlong_as_double((long long)((neg << 63) | 0x7FF0000000000000ull));
+    return __longlong_as_double((long long)((neg << 63) | ((unsigned long long)E << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+}
+
+// sum_o P_o 2^(8(4-o)) from the five order accumulators (exact integers < 2^24)
+__device__ __forceinline__ long long combine(const float *p) {
+    const int t = __float2int_rn(p[0]) * 256 + __float2int_rn(p[1]);
+    long long u = ((long long)t << 8) + __float2int_rn(p[2]);
+    u = (u << 8) + __float2int_rn(p[3]);
+    return (u << 8) + __float2int_rn(p[4]);
+}
+
+__global__ void __launch_bounds__(192, 1) k_gemm_tc(const GemmTile *__restrict__ tiles, const SegX *__restrict__ segs,
+                                                    const __half *__restrict__ Apl, const __half *__restrict__ Bpl,
+                                                    const int *__restrict__ Aexp, const int *__restrict__ Bexp,
+                                                    double2 *__restrict__ C, const int *skip, int *err) {
     if (skip && *skip) return;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    float *Ap = (float *)smem;
-    float *Bp = (float *)(smem + NPLANE * A_PLANE);
-    uint64_t *mbar = (uint64_t *)(smem + NPLANE * A_PLANE + NPLANE * B_PLANE);
-    uint32_t *tslot = (uint32_t *)(mbar + 1);
+    uint8_t *sA = smem;
+    uint8_t *sB = smem + STAGES * A_BYTES;
+    uint64_t *bars = (uint64_t *)(smem + STAGES * (A_BYTES + B_BYTES));
+    uint64_t *full = bars, *empty = bars + STAGES, *accf = bars + 2 * STAGES, *acce = accf + 1, *mdone = acce + 1;
+    uint32_t *tslot = (uint32_t *)(mdone + 1);
+    int *s_ecol = (int *)(tslot + 4);  // [BN] largest column exponent over the tile's segments
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const GemmTile t = tiles[blockIdx.x];
+    const int nseg = t.seg_end - t.seg_begin;
+    const int rt = t.m0 / BM, nt = t.n0 / BN;
 
-    if (warp == 0) {
+    if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
                      "r"(TMEM_COLS)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mbar)), "r"(1) : "memory");
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(smem_u32(full + s), 1);
+            mbar_init(smem_u32(empty + s), 1);
+        }
+        mbar_init(smem_u32(accf), 1);
+        mbar_init(smem_u32(acce), 128);
+        mbar_init(smem_u32(mdone), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tslot;
-    const uint32_t mb = smem_u32(mbar);
 
-    uint32_t parity = 0;
-    bool pending = false, first = true, ok = true;
-    for (int s = t.seg_begin; s < t.seg_end && ok; ++s) {
-        const GemmSeg g = segs[s];
-        const double2 *a = A + g.a_off;
-        const double2 *b = B + g.b_off;
-        for (int k0 = 0; k0 < g.K && ok; k0 += BK) {
-            if (pending) {  // the previous MMAs still read shared memory
-                if (!__syncthreads_and(mbar_wait(mb, parity))) { ok = false; break; }
-                parity ^= 1u;
-                pending = false;
-            }
-            for (int idx = tid; idx < BM * BK; idx += 128) {
-                int m, k;
-                if (g.opa == 0) { m = idx / BK; k = idx % BK; }
-                else { m = idx % BM; k = idx / BM; }
-                const int gm = t.m0 + m, gk = k0 + k;
-                double re = 0.0, im = 0.0;
-                if (gm < t.M && gk < g.K) {
-                    double2 v = (g.opa == 0) ? a[(int64_t)gm * g.lda + gk] : a[(int64_t)gk * g.lda + gm];
-                    re = v.x;
-                    im = (g.opa == 0) ? v.y : -v.y;
+    if (warp == 0) {
+        // ------------------------------------------------ producer
+        if (lane == 0) {
+            int it = 0;
+            int uses[STAGES] = {0, 0, 0};
+            bool ok = true;
+            for (int s = t.seg_begin; s < t.seg_end && ok; ++s) {
+                const SegX g = segs[s];
+                const __half *ap = Apl + g.a_pan + (int64_t)rt * g.nkc * A_PANEL;
+                const __half *bp = Bpl + g.b_pan + (int64_t)nt * g.nkc * B_PANEL;
+                for (int kc = 0; kc < g.nkc; ++kc, ++it) {
+                    const int st = it % STAGES;
+                    const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+                    if (!mbar_wait(smem_u32(empty + st), ph ^ 1u)) { ok = false; break; }
+                    mbar_expect_tx(smem_u32(full + st), (uint32_t)(A_BYTES + B_BYTES));
+                    bulk_g2s(smem_u32(sA + st * A_BYTES), ap + (int64_t)kc * A_PANEL, A_BYTES, smem_u32(full + st));
+                    bulk_g2s(smem_u32(sB + st * B_BYTES), bp + (int64_t)kc * B_PANEL, B_BYTES, smem_u32(full + st));
+                    ++uses[st];
                 }
-                const uint32_t o = kmaj_off(m, k) >> 2;
-                float h, md, l;
-                split3(re, h, md, l);
-                Ap[0 * (A_PLANE / 4) + o] = h;
-                Ap[1 * (A_PLANE / 4) + o] = md;
-                Ap[2 * (A_PLANE / 4) + o] = l;
-                split3(im, h, md, l);
-                Ap[3 * (A_PLANE / 4) + o] = h;
-                Ap[4 * (A_PLANE / 4) + o] = md;
-                Ap[5 * (A_PLANE / 4) + o] = l;
-                split3(re + im, h, md, l);
-                Ap[6 * (A_PLANE / 4) + o] = h;
-                Ap[7 * (A_PLANE / 4) + o] = md;
-                Ap[8 * (A_PLANE / 4) + o] = l;
             }
-            for (int idx = tid; idx < BN * BK; idx += 128) {
-                int n, k;
-                if (g.opb == 0) { n = idx % BN; k = idx / BN; }
-                else { k = idx % BK; n = idx / BK; }
-                const int gn = t.n0 + n, gk = k0 + k;
-                double re = 0.0, im = 0.0;
-                if (gn < t.N && gk < g.K) {
-                    double2 v = (g.opb == 0) ? b[(int64_t)gk * g.ldb + gn] : b[(int64_t)gn * g.ldb + gk];
-                    re = v.x;
-                    im = v.y;
+            if (!ok) atomicExch(err, 1);
+            // no copy may land after the CTA exits: wait (bounded) for the last one into each stage
+            for (int st = 0; st < STAGES; ++st)
+                if (uses[st]) mbar_wait(smem_u32(full + st), (uint32_t)(uses[st] - 1) & 1u);
+        }
+    } else if (warp == 1) {
+        // ------------------------------------------------ MMA issue
+        if (lane == 0) {
+            int it = 0, grp = 0;
+            bool ok = true;
+            for (int s = t.seg_begin; s < t.seg_end && ok; ++s) {
+                const int nkc = segs[s].nkc;
+                for (int kc0 = 0; kc0 < nkc && ok; kc0 += GKC, ++grp) {
+                    // the epilogue has read the previous group's accumulators
+                    if (!mbar_wait(smem_u32(acce), ((uint32_t)grp & 1u) ^ 1u)) { ok = false; break; }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const int kc1 = min(nkc, kc0 + GKC);
+                    for (int kc = kc0; kc < kc1; ++kc, ++it) {
+                        const int st = it % STAGES;
+                        const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+                        if (!mbar_wait(smem_u32(full + st), ph)) { ok = false; break; }
+                        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                        const uint32_t a0 = smem_u32(sA + st * A_BYTES), b0 = smem_u32(sB + st * B_BYTES);
+#pragma unroll
+                        for (int c = 0; c < NCOMP; ++c)
+#pragma unroll
+                            for (int o = 0; o < NORD; ++o) {
+                                const uint32_t d = tmem + (uint32_t)((c * NORD + o) * BN);
+#pragma unroll
+                                for (int i = (o > NDIG - 1 ? o - (NDIG - 1) : 0); i <= (o < NDIG - 1 ? o : NDIG - 1);
+                                     ++i) {
+                                    const int jj = o - i;
+                                    const bool first = (i == (o > NDIG - 1 ? o - (NDIG - 1) : 0));
+                                    const uint64_t ad = make_desc(a0 + (c * NDIG + i) * PLANE_A, 128, 256);
+                                    const uint64_t bd = make_desc(b0 + (c * NDIG + jj) * PLANE_B, 128, 256);
+                                    mma_f16(d, ad, bd, (first && kc == kc0) ? 0u : 1u);
+                                }
+                            }
+                        mma_commit(smem_u32(empty + st));  // stage free once these MMAs are done
+                    }
+                    if (!ok) break;
+                    mma_commit(smem_u32(accf));  // accumulators ready for the drain
                 }
-                const uint32_t o = kmaj_off(n, k) >> 2;
-                float h, md, l;
-                split3(re, h, md, l);
-                Bp[0 * (B_PLANE / 4) + o] = h;
-                Bp[1 * (B_PLANE / 4) + o] = md;
-                Bp[2 * (B_PLANE / 4) + o] = l;
-                split3(im, h, md, l);
-                Bp[3 * (B_PLANE / 4) + o] = h;
-                Bp[4 * (B_PLANE / 4) + o] = md;
-                Bp[5 * (B_PLANE / 4) + o] = l;
-                split3(re + im, h, md, l);
-                Bp[6 * (B_PLANE / 4) + o] = h;
-                Bp[7 * (B_PLANE / 4) + o] = md;
-                Bp[8 * (B_PLANE / 4) + o] = l;
             }
-            // make the generic-proxy smem writes visible to the tensor core
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            __syncthreads();
-            if (tid == 0) {
+            if (!ok) atomicExch(err, 1);
+            // every MMA issued by this thread has completed before tensor memory is freed
+            mma_commit(smem_u32(mdone));
+            mbar_wait(smem_u32(mdone), 0u);
+        }
+    } else {
+        // ------------------------------------------------ drains and epilogue
+        const int q = warp & 3;  // tensor-memory lane quarter of this warp
+        const int m = q * 32 + lane;
+        const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16);
+        int erow = kZeroExp;
+        for (int s = t.seg_begin; s < t.seg_end; ++s) erow = max(erow, Aexp[segs[s].a_exp + t.m0 + m]);
+        if (warp == 2) {
+            int ec = kZeroExp;
+            for (int s = t.seg_begin; s < t.seg_end; ++s) ec = max(ec, Bexp[segs[s].b_exp + t.n0 + lane]);
+            s_ecol[lane] = ec;
+        }
+        epi_bar();  // the only barrier of the epilogue warps: reached by all four unconditionally
+        long long cr[BN], ci[BN];
+#pragma unroll
+        for (int c = 0; c < BN; ++c) cr[c] = ci[c] = 0;
+        bool ok = true;
+        int grp = 0;
+        for (int sl = 0; sl < nseg && ok; ++sl) {
+            const SegX g = segs[t.seg_begin + sl];
+            const int *fcol = Bexp + g.b_exp + t.n0;
+            const int shr = erow - Aexp[g.a_exp + t.m0 + m];
+            for (int kc0 = 0; kc0 < g.nkc; kc0 += GKC, ++grp) {
+                // warp-uniform decision: tcgen05.ld below is a warp-wide instruction
+                if (!__all_sync(0xFFFFFFFFu, mbar_wait(smem_u32(accf), (uint32_t)grp & 1u))) { ok = false; break; }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const uint32_t a0 = smem_u32(Ap), b0 = smem_u32(Bp);
 #pragma unroll
-                for (int kk = 0; kk < BK / 8; ++kk) {
+                for (int c0 = 0; c0 < BN; c0 += 4) {
+                    long long I[NCOMP][4];
 #pragma unroll
-                    for (int p = 0; p < 3; ++p) {  // T1 = Ar Br, T2 = Ai Bi, T3 = As Bs
-                        const uint32_t d = tmem + (uint32_t)(p * BN);
-                        // (a part, b part) pairs with part-order sum <= 2, smallest terms first
-                        const int pa[6] = {2, 1, 0, 1, 0, 0}, pb[6] = {0, 1, 2, 0, 1, 0};
+                    for (int c = 0; c < NCOMP; ++c) {
+                        float a[NORD][4];
 #pragma unroll
-                        for (int t = 0; t < 6; ++t) {
-                            const uint32_t aa = a0 + (3 * p + pa[t]) * A_PLANE + kk * 256;
-                            const uint32_t bb = b0 + (3 * p + pb[t]) * B_PLANE + kk * 256;
-                            const uint32_t acc = (first && kk == 0 && t == 0) ? 0u : 1u;
-                            mma_tf32(d, make_desc(aa, 128, 1024), make_desc(bb, 128, 1024), acc);
+                        for (int o = 0; o < NORD; ++o) tmem_ld4(trow + (uint32_t)((c * NORD + o) * BN + c0), a[o]);
+                        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                        for (int jx = 0; jx < 4; ++jx) {
+                            float p[NORD];
+#pragma unroll
+                            for (int o = 0; o < NORD; ++o) p[o] = a[o][jx];
+                            I[c][jx] = combine(p);
                         }
                     }
-                }
-                mma_commit(mb);
-            }
-            first = false;
-            pending = true;
-        }
-    }
-    if (pending && ok) {
-        if (__syncthreads_and(mbar_wait(mb, parity))) pending = false;
-        else ok = false;
-    }
-    if (!ok) {
-        if (tid == 0) atomicExch(err, 1);
-        // drain what may still be in flight (bounded) before releasing tensor memory
-        if (pending) mbar_wait(mb, parity);
-    }
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const int m = warp * 32 + lane;
-    const int gm = t.m0 + m;
-    if (ok) {
-        for (int c0 = 0; c0 < BN; c0 += 32) {
-            float t1[32], t2[32], t3[32];
-            if (!first) {  // at least one MMA ran: read the accumulators (all warps, aligned)
-                const uint32_t row = (uint32_t)(warp * 32) << 16;
-                tmem_ld32(tmem + row + 0 * BN + c0, t1);
-                tmem_ld32(tmem + row + 1 * BN + c0, t2);
-                tmem_ld32(tmem + row + 2 * BN + c0, t3);
-            } else {
 #pragma unroll
-                for (int j = 0; j < 32; ++j) t1[j] = t2[j] = t3[j] = 0.f;
-            }
-            if (gm < t.M) {
-                double2 *crow = C + t.c_off + (int64_t)gm * t.ldc;
-#pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const int gn = t.n0 + c0 + j;
-                    if (gn < t.N) {
-                        const double cr = (double)t1[j] - (double)t2[j];
-                        const double ci = (double)t3[j] - (double)t1[j] - (double)t2[j];
-                        crow[gn] = make_double2(alpha * cr, alpha * ci);
+                    for (int jx = 0; jx < 4; ++jx) {
+                        const int col = c0 + jx;
+                        const int sh = shr + s_ecol[col] - __ldg(fcol + col);
+                        cr[col] += sra_round(I[0][jx] - I[1][jx], sh);
+                        ci[col] += sra_round(I[2][jx] - I[0][jx] - I[1][jx], sh);
                     }
+                }
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                mbar_arrive(smem_u32(acce));
+            }
+        }
+        if (!ok && lane == 0) atomicExch(err, 1);
+        const int gm = t.m0 + m;
+        if (ok && gm < t.M) {
+            double2 *crow = C + t.c_off + (int64_t)gm * t.ldc;
+#pragma unroll
+            for (int c = 0; c < BN; ++c) {
+                const int gn = t.n0 + c;
+                if (gn < t.N) {
+                    const int sc = erow + s_ecol[c] - 2 * FRAC + 16;
+                    crow[gn] = make_double2(i64_ldexp(cr[c], sc), i64_ldexp(ci[c], sc));
                 }
             }
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (warp == 0)
+    if (warp == 1) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS)
                      : "memory");
+    }
 }
 
 int *g_err = nullptr;
@@ -284,19 +453,103 @@ bool g_attr = false;
 
 }  // namespace
 
+// Slicing jobs and per-segment panel addresses of a mixed-precision plan:
+// one job per distinct (block, operation) view of A and of B.
+void plan_mixed(GemmPlan &g) {
+    g.ajobs.clear();
+    g.bjobs.clear();
+    g.xsegs.assign(g.segs.size(), SegX{});
+    g.a_planes = g.b_planes = 0;
+    g.a_exps = g.b_exps = 0;
+    std::vector<std::pair<int, int>> seg_mn(g.segs.size(), {0, 0});
+    for (auto &t : g.tiles)
+        for (int s = t.seg_begin; s < t.seg_end; ++s) seg_mn[s] = {t.M, t.N};
+    std::map<std::pair<int64_t, int>, int> amap, bmap;
+    for (size_t s = 0; s < g.segs.size(); ++s) {
+        const GemmSeg &sg = g.segs[s];
+        const int M = seg_mn[s].first, N = seg_mn[s].second;
+        if (M == 0) continue;  // segment of no tile
+        const int nkc = (sg.K + BKC - 1) / BKC;
+        auto ia = amap.find({sg.a_off, sg.opa});
+        if (ia == amap.end()) {
+            SliceJob j{};
+            j.src_off = sg.a_off;
+            j.dst_off = g.a_planes;
+            j.rows = M;
+            j.K = sg.K;
+            j.ld = sg.lda;
+            j.trans = (sg.opa == 1 || sg.opa == 2) ? 1 : 0;
+            j.conj = (sg.opa == 1 || sg.opa == 3) ? 1 : 0;
+            j.exp_off = (int)g.a_exps;
+            j.nkc = nkc;
+            const int nrt = (M + BM - 1) / BM;
+            g.a_planes += (int64_t)nrt * nkc * A_PANEL;
+            g.a_exps += (int64_t)nrt * BM;
+            ia = amap.emplace(std::make_pair(sg.a_off, sg.opa), (int)g.ajobs.size()).first;
+            g.ajobs.push_back(j);
+        }
+        auto ib = bmap.find({sg.b_off, sg.opb});
+        if (ib == bmap.end()) {
+            SliceJob j{};
+            j.src_off = sg.b_off;
+            j.dst_off = g.b_planes;
+            j.rows = N;
+            j.K = sg.K;
+            j.ld = sg.ldb;
+            j.trans = (sg.opb == 0 || sg.opb == 3) ? 1 : 0;  // B element (n, k) at b[k*ldb + n]
+            j.conj = (sg.opb == 2 || sg.opb == 3) ? 1 : 0;
+            j.exp_off = (int)g.b_exps;
+            j.nkc = nkc;
+            const int nnt = (N + BN - 1) / BN;
+            g.b_planes += (int64_t)nnt * nkc * B_PANEL;
+            g.b_exps += (int64_t)nnt * BN;
+            ib = bmap.emplace(std::make_pair(sg.b_off, sg.opb), (int)g.bjobs.size()).first;
+            g.bjobs.push_back(j);
+        }
+        const SliceJob &ja = g.ajobs[ia->second], &jb = g.bjobs[ib->second];
+        KV_REQUIRE(ja.rows == M && jb.rows == N && ja.K == sg.K && jb.K == sg.K, KV_EINVAL,
+                   "internal: inconsistent block views in a mixed-precision plan");
+        g.xsegs[s] = SegX{ja.dst_off, jb.dst_off, nkc, ja.exp_off, jb.exp_off, 0};
+    }
+    KV_REQUIRE(g.a_exps < (1ll << 31) && g.b_exps < (1ll << 31), KV_EINVAL, "mixed-precision plan too large");
+    g.d_ajobs = upload_vec(g.ajobs);
+    g.d_bjobs = upload_vec(g.bjobs);
+    g.d_xsegs = upload_vec(g.xsegs);
+}
+
 void launch_gemm_mixed(const GemmPlan &p, const double2 *A, const double2 *B, double2 *C, double alpha,
                        const int *skip) {
     if (p.tiles.empty()) return;
+    KV_REQUIRE(p.tile_m == BM && p.tile_n == BN && p.xsegs.size() == p.segs.size(), KV_EINVAL,
+               "internal: GEMM plan not prepared for the tensor-core path");
+    auto &c = ctx();
     if (!g_attr) {
         KV_CUDA(cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
         KV_CUDA(cudaMalloc(&g_err, sizeof(int)));
         KV_CUDA(cudaMemset(g_err, 0, sizeof(int)));
         g_attr = true;
     }
-    k_gemm_tc<<<(unsigned)p.tiles.size(), 128, SMEM_BYTES, ctx().stream>>>(
-        p.d_tiles.as<GemmTile>(), p.d_segs.as<GemmSeg>(), A, B, C, alpha, skip, g_err);
-    counted();
+    DevBuf ap(std::max<int64_t>(1, p.a_planes) * sizeof(__half)), bp(std::max<int64_t>(1, p.b_planes) * sizeof(__half));
+    DevBuf ae(std::max<int64_t>(1, p.a_exps) * sizeof(int)), be(std::max<int64_t>(1, p.b_exps) * sizeof(int));
+    int n = 0;
+    if (!p.ajobs.empty()) {
+        k_slice<BM><<<(unsigned)p.ajobs.size(), 256, 0, c.stream>>>(p.d_ajobs.as<SliceJob>(), A, ap.as<__half>(),
+                                                                    ae.as<int>(), 1.0, skip);
+        KV_CUDA(cudaGetLastError());
+        ++n;
+    }
+    if (!p.bjobs.empty()) {
+        k_slice<BN><<<(unsigned)p.bjobs.size(), 256, 0, c.stream>>>(p.d_bjobs.as<SliceJob>(), B, bp.as<__half>(),
+                                                                    be.as<int>(), alpha, skip);
+        KV_CUDA(cudaGetLastError());
+        ++n;
+    }
+    k_gemm_tc<<<(unsigned)p.tiles.size(), 192, SMEM_BYTES, c.stream>>>(
+        p.d_tiles.as<GemmTile>(), p.d_xsegs.as<SegX>(), ap.as<__half>(), bp.as<__half>(), ae.as<int>(), be.as<int>(),
+        C, skip, g_err);
     KV_CUDA(cudaGetLastError());
+    counted(n + 1);
+    // the slices are freed stream-ordered after the GEMM
 }
 
 // 0 if no tensor-core wait has timed out since the last call (then cleared)

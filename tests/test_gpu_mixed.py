@@ -1,9 +1,13 @@
-"""Mixed-precision (tcgen05, 3M with TF32 hi/lo split, FP32 accumulation)
-contractions against the FP64 path of the same library and against the
-reference's golden vectors.  Tolerance relative to the largest output entry:
-the split keeps ~22 mantissa bits (~2e-7); FP32 accumulation adds about
-6e-8 * sqrt(K) for a sum of K products, so 3e-6 for the short contractions
-of the fixtures and 1e-5 for the ~500-term sums of the synthetic product."""
+"""Mixed-precision contractions (tcgen05 FP16 digit products with exact
+FP32 accumulation, kv_tc.cu) against the FP64 path of the same library and
+against the reference's golden vectors.
+
+Each real operand value is a 30-bit fixed-point integer relative to its
+GEMM row's (A) or column's (B) largest entry, split into four base-256
+digits; digit products of orders 0..4 are accumulated exactly.  The error of
+an output entry is therefore below ~2^-29 of max|A_row| max|B_col| summed
+over K, which for these inputs is < 2e-8 of the largest output entry (REL);
+integer-valued inputs are reproduced bit for bit."""
 import numpy as np
 import pytest
 
@@ -14,7 +18,7 @@ from kylin_v_gb300 import kvio  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 G = U.GOLDEN
-REL = 3e-6
+REL = 2e-8
 
 
 @pytest.fixture(scope="module")
@@ -57,7 +61,68 @@ def test_mixed_product_matches_fp64(gpu):
     Bf = kvio.BlockTensor((-1, -1, 1), B.blocks)  # legs contracted against B need opposite directions
     D1 = gpu.product(B, Bf, 2, opA=gpu.OP_N, opB=gpu.OP_T, precision=gpu.KV_FP64)
     D2 = gpu.product(B, Bf, 2, opA=gpu.OP_N, opB=gpu.OP_T, precision=gpu.KV_MIXED_TF32)
-    assert _rel(D2.to_host(), D1.to_host()) < 1e-5  # ~500 products per output entry
+    assert _rel(D2.to_host(), D1.to_host()) < REL
+
+
+def _segmented_pair(rng, integer):
+    """A (x, s, k) and B (s, k, y): each output block (x, y) sums six block
+    pairs (one per s) of K = 90 .. 700 (beyond one 336-step drain), every
+    pair rescaled by 2^u on A and 2^-u on B so the pairs' row and column
+    exponents differ while the product does not change."""
+    Ks = [90, 95, 400, 100, 700, 17]
+    us = [0, 3, -4, 5, -2, 1]
+    val = (lambda sh: rng.integers(-9, 10, sh) + 1j * rng.integers(-9, 10, sh)) if integer else \
+        (lambda sh: rng.standard_normal(sh) + 1j * rng.standard_normal(sh))
+    rows = {x: 2.0 ** rng.integers(-20, 21, 60 + 40 * x) for x in range(2)}  # per-row scales of A
+    cols = {y: 2.0 ** rng.integers(-20, 21, 40 + 30 * y) for y in range(2)}  # per-column scales of B
+    if integer:
+        rows = {x: np.ones_like(v) for x, v in rows.items()}
+        cols = {y: np.ones_like(v) for y, v in cols.items()}
+    ablk, bblk = [], []
+    for x in range(2):
+        for s, (K, u) in enumerate(zip(Ks, us)):
+            a = val((60 + 40 * x, 1, K)) * rows[x][:, None, None] * 2.0 ** u
+            ablk.append(((x, s, s + x), a))
+    for s, (K, u) in enumerate(zip(Ks, us)):
+        for x in range(2):
+            for y in range(2):
+                b = val((1, K, 40 + 30 * y)) * cols[y][None, None, :] * 2.0 ** (-u)
+                bblk.append(((s, s + x, y), b))
+    A = kvio.BlockTensor((1, 1, 1), ablk)
+    B = kvio.BlockTensor((-1, -1, 1), bblk)
+    # the same product as conj-transposed A (legs s, k, x) and transposed B (legs y, s, k)
+    At = kvio.BlockTensor((1, 1, -1), [((q[1], q[2], q[0]), np.conj(np.transpose(a, (1, 2, 0)))) for q, a in ablk])
+    Bt = kvio.BlockTensor((1, 1, 1), [((q[2], q[0], q[1]), np.transpose(b, (2, 0, 1))) for q, b in bblk])
+    return A, B, At, Bt, rows, cols
+
+
+def test_mixed_product_exact_on_integers(gpu):
+    rng = np.random.default_rng(11)
+    A, B, At, Bt, _, _ = _segmented_pair(rng, integer=True)
+    ref = gpu.product(A, B, 2, precision=gpu.KV_FP64).to_host().as_dict()
+    mix = gpu.product(A, B, 2, precision=gpu.KV_MIXED_TF32).to_host().as_dict()
+    mix_t = gpu.product(At, Bt, 2, opA=gpu.OP_C, opB=gpu.OP_T, precision=gpu.KV_MIXED_TF32).to_host().as_dict()
+    assert set(ref) == set(mix) == set(mix_t) and len(ref) == 4
+    for q in ref:
+        assert np.array_equal(ref[q], mix[q])
+        assert np.array_equal(ref[q], mix_t[q])
+
+
+def test_mixed_product_row_column_dynamic_range(gpu):
+    """Rows of A and columns of B spanning 2^+-20: the error of every entry is
+    small relative to its own row and column scale, not the block's."""
+    rng = np.random.default_rng(12)
+    A, B, At, Bt, rows, cols = _segmented_pair(rng, integer=False)
+    ref = gpu.product(A, B, 2, precision=gpu.KV_FP64).to_host().as_dict()
+    for P in (gpu.product(A, B, 2, precision=gpu.KV_MIXED_TF32),
+              gpu.product(At, Bt, 2, opA=gpu.OP_C, opB=gpu.OP_T, precision=gpu.KV_MIXED_TF32)):
+        mix = P.to_host().as_dict()
+        for q, r in ref.items():
+            x, y = q[0][0], q[0][1]  # as_dict keys are (charges, shape)
+            sc = rows[x][:, None] * cols[y][None, :]
+            r2 = r.reshape(sc.shape) / sc
+            m2 = mix[q].reshape(sc.shape) / sc
+            assert np.abs(m2 - r2).max() < REL * np.abs(r2).max()
 
 
 @pytest.mark.parametrize("case,site", [("tiny1", 1), ("tiny1", 4), ("tiny2m", 2), ("tiny2m", 6)])
@@ -73,7 +138,7 @@ def test_mixed_heff_matches_reference(gpu, case, site):
     assert _rel(e, rd("envR_prev")) < REL
     k2, _ = gpu.local_krylov(2, L, rd("mm"), mpo[site], mpo[site + 1], R2, 0.05, 11, 1e-8,
                              precision=gpu.KV_MIXED_TF32)
-    assert _rel(k2.to_host(), rd("k2")) < 1e-5
+    assert _rel(k2.to_host(), rd("k2")) < 1e-7
 
 
 @pytest.mark.parametrize("case,site", [("tiny1", 1), ("tiny1", 4), ("tiny2m", 2), ("tiny2m", 6)])
