@@ -133,6 +133,12 @@ int kv_tdvp_site(kv_tdvp s, int i, kv_tensor *out);
  * reference issues for the same sweep, Lanczos iterations as actually run)
  * and the part of it in product<> block pairs (the grouped GEMM kernel). */
 int kv_tdvp_stats(kv_tdvp s, double *module_ms, double *sweep_ms, double *ref_flops, double *gemm_ref_flops);
+/* Host side of the last sweep: wall-clock ms per module (same order; the
+ * reference's Timer table measures wall-clock, util/timer.h:19-66), the
+ * sweep's wall-clock ms, and the H_eff plans built (plan-cache misses) with
+ * the host ms spent building them.  No other reference counterpart. */
+int kv_tdvp_host_stats(kv_tdvp s, double *module_host_ms, double *sweep_host_ms, long long *plans_built,
+                       double *plan_ms);
 int kv_tdvp_free(kv_tdvp s);
 
 /* ------------------------------------------------------ instrumentation */

@@ -240,6 +240,18 @@ int kv_tdvp_stats(kv_tdvp s, double *module_ms, double *sweep_ms, double *ref_fl
     });
 }
 
+int kv_tdvp_host_stats(kv_tdvp s, double *module_host_ms, double *sweep_host_ms, long long *plans_built,
+                       double *plan_ms) {
+    return guard([&] {
+        KV_REQUIRE(s && s->s, KV_EINVAL, "null TDVP handle");
+        if (module_host_ms)
+            for (int i = 0; i < kv::MOD_COUNT; ++i) module_host_ms[i] = s->s->module_host_ms[i];
+        if (sweep_host_ms) *sweep_host_ms = s->s->sweep_host_ms;
+        if (plans_built) *plans_built = s->s->plans_built;
+        if (plan_ms) *plan_ms = s->s->plan_ms;
+    });
+}
+
 int kv_profile(int enable) {
     return guard([&] {
         kv::require_init();

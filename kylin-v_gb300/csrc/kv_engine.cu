@@ -396,34 +396,15 @@ TensorP op_product(const DTensor &A, const DTensor &B, int nc, int opA, int opB,
 }
 
 // --------------------------------------------------------- H_eff plans
-// Reference flops of one H_eff application on input structure S, split into
-// product<> pairs and MPO-mixing zgemms, and the output block set.
-static Flops heff_ref_flops(int nsite, const Meta &L, const Meta &S, const Meta *W1, const Meta *W2, const Meta &R,
-                            Meta *out_blocks) {
-    Flops f;
-    ProductPlan P1 = plan_product(L, S, 1, KV_OP_N, KV_OP_N);
-    f.gemm += P1.gemm.ref_flops;
-    Meta merged = P1.out;
-    std::vector<double> mult(P1.out.blocks.size(), 1.0);
-    const Meta *Ws[2] = {W1, W2};
-    for (int st = 0; st < nsite; ++st) {
-        MixPlanFull m = plan_mix(merged, *Ws[st], st + 1, &mult);
-        f.mix += m.ref_flops;
-        merged = std::move(m.out);
-        mult = std::move(m.mult);
-    }
-    f.gemm += ref_product_flops(merged, R, 2, KV_OP_N, KV_OP_T, &mult, nullptr);
-    if (out_blocks) *out_blocks = plan_product(merged, R, 2, KV_OP_N, KV_OP_T).out;
-    return f;
-}
-
 // Krylov layout: the closure of psi's blocks under H_eff (union of input and
 // output block sets until stable), so every Lanczos vector and H_eff . v share
 // one layout; blocks absent from the reference's tensors are zero.  The
 // reference's vectors grow towards that closure one application at a time
 // (hv += V_{k-1} beta, V_k alpha merge block sets, holstein/exponential.h:126-137);
 // iter_flops[k] replays that growth so only the block pairs the reference
-// multiplies at iteration k are credited.
+// multiplies at iteration k are credited.  Each closure step builds the
+// product / mixing plans of one application once; those of the step that
+// adds no block are the final plans.
 HeffPlan plan_heff(int nsite, const Meta &L, const Meta &psi, const Meta *W1, const Meta *W2, const Meta &R,
                    int precision, int max_iter) {
     HeffPlan H;
@@ -432,35 +413,46 @@ HeffPlan plan_heff(int nsite, const Meta &L, const Meta &psi, const Meta *W1, co
     K.layout();
     for (int iter = 0;; ++iter) {
         KV_REQUIRE(iter < 4096, KV_EINVAL, "H_eff block closure did not converge");
-        Meta out;
-        Flops f = heff_ref_flops(nsite, L, K, W1, W2, R, &out);
+        Flops f;
+        ProductPlan P1 = plan_product(L, K, 1, KV_OP_N, KV_OP_N);
+        f.gemm += P1.gemm.ref_flops;
+        // reference blocks merged into each computed block (the reference keeps
+        // every matched MPO-mixing pair as its own block)
+        std::vector<double> mult(P1.out.blocks.size(), 1.0);
+        MixPlanFull m1, m2;
+        const Meta *last = &P1.out;
+        if (nsite >= 1) {
+            m1 = plan_mix(*last, *W1, 1, &mult);
+            f.mix += m1.ref_flops;
+            mult = m1.mult;
+            last = &m1.out;
+        }
+        if (nsite == 2) {
+            m2 = plan_mix(*last, *W2, 2, &mult);
+            f.mix += m2.ref_flops;
+            mult = m2.mult;
+            last = &m2.out;
+        }
+        f.gemm += ref_product_flops(*last, R, 2, KV_OP_N, KV_OP_T, &mult, nullptr);
+        ProductPlan P2 = plan_product(*last, R, 2, KV_OP_N, KV_OP_T);
         if (iter < max_iter) H.iter_flops.push_back(f);
         bool grew = false;
-        for (auto &b : out.blocks) {
+        for (auto &b : P2.out.blocks) {
             const size_t before = K.blocks.size();
             if ((size_t)K.add(b) == before) grew = true;
         }
-        K.layout();
         if (!grew) {
             while ((int)H.iter_flops.size() < max_iter) H.iter_flops.push_back(f);
+            H.p1 = std::move(P1);
+            H.m1 = std::move(m1);
+            H.m2 = std::move(m2);
+            H.p2 = std::move(P2);
             break;
         }
+        K.layout();
     }
-    K.layout();
     H.klayout = K;
-    // final plans on the closed layout
-    H.p1 = plan_product(L, K, 1, KV_OP_N, KV_OP_N);
     build_tiles(H.p1, own_offsets(H.p1.out), kTileM(precision), kTileN(precision));
-    Meta last = H.p1.out;
-    if (nsite >= 1) {
-        H.m1 = plan_mix(last, *W1, 1);
-        last = H.m1.out;
-    }
-    if (nsite == 2) {
-        H.m2 = plan_mix(last, *W2, 2);
-        last = H.m2.out;
-    }
-    H.p2 = plan_product(last, R, 2, KV_OP_N, KV_OP_T);
     std::vector<int64_t> tgt;
     std::vector<char> produced(K.blocks.size(), 0);
     for (auto &b : H.p2.out.blocks) {
@@ -507,9 +499,16 @@ struct VecHash {
 };
 std::unordered_map<std::vector<int>, std::shared_ptr<HeffPlan>, VecHash> g_plan_cache;
 constexpr size_t kPlanCacheMax = 16384;
+long long g_plans_built = 0;
+double g_plan_ms = 0.0;
 }  // namespace
 
 void clear_plan_cache() { g_plan_cache.clear(); }
+
+void plan_stats(long long *built, double *ms) {
+    *built = g_plans_built;
+    *ms = g_plan_ms;
+}
 
 std::shared_ptr<HeffPlan> get_heff_plan(int nsite, const Meta &L, const Meta &psi, const Meta *W1, const Meta *W2,
                                         const Meta &R, int precision, int max_iter) {
@@ -522,7 +521,10 @@ std::shared_ptr<HeffPlan> get_heff_plan(int nsite, const Meta &L, const Meta &ps
     auto it = g_plan_cache.find(key);
     if (it != g_plan_cache.end()) return it->second;
     if (g_plan_cache.size() >= kPlanCacheMax) g_plan_cache.clear();
+    const auto t0 = std::chrono::steady_clock::now();
     auto p = std::make_shared<HeffPlan>(plan_heff(nsite, L, psi, W1, W2, R, precision, max_iter));
+    ++g_plans_built;
+    g_plan_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     g_plan_cache.emplace(std::move(key), p);
     return p;
 }
@@ -688,24 +690,28 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
     }
     SvdPlan P;
     std::vector<std::pair<int, int>> sec_rc;
+    const bool mixed = svd_mixed(precision);
     for (int ri = 0; ri < (int)rows.size(); ++ri)
         for (int ci = 0; ci < (int)cols.size(); ++ci) {
             if (rows[ri].q + cols[ci].q != 0) continue;
             SvdSector s{};
             s.m = rows[ri].len;
             s.n = cols[ci].len;
-            s.transposed = s.m < s.n ? 1 : 0;
-            s.p = std::max(s.m, s.n);
-            s.q = std::min(s.m, s.n);
+            // FP64: tall T with accumulated V.  Mixed: T's columns are the
+            // singular vectors the polish needs (right ones for L->R, left
+            // ones for R->L), so no rotations are accumulated; T may be wide.
+            s.transposed = mixed ? (l2r ? 1 : 0) : (s.m < s.n ? 1 : 0);
+            s.p = s.transposed ? s.n : s.m;
+            s.q = s.transposed ? s.m : s.n;
             s.t_off = P.t_elems;
             s.v_off = P.v_elems;
             s.s_off = P.s_elems;
             P.t_elems += (int64_t)s.p * s.q;
-            P.v_elems += (int64_t)s.q * s.q;
+            if (!mixed) P.v_elems += (int64_t)s.q * s.q;
             P.s_elems += s.q;
             P.max_q = std::max(P.max_q, s.q);
-            rows[ri].kept = s.q;
-            cols[ci].kept = s.q;
+            rows[ri].kept = std::min(s.m, s.n);
+            cols[ci].kept = std::min(s.m, s.n);
             const int sid = (int)P.secs.size();
             for (auto &ra : rows[ri].subs)
                 for (auto &ca : cols[ci].subs)
@@ -716,7 +722,6 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
             sec_rc.push_back({ri, ci});
         }
     P.upload();
-    const bool mixed = svd_mixed(precision);
     const size_t cb = mixed ? sizeof(float2) : sizeof(double2);
     DevBuf T(std::max<int64_t>(1, P.t_elems) * sizeof(double2));
     DevBuf Us(std::max<int64_t>(1, P.t_elems) * cb), V(std::max<int64_t>(1, P.v_elems) * cb);
@@ -725,8 +730,8 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
     DevBuf status(std::max<size_t>(1, P.secs.size()) * sizeof(int));
     svd_gather(P, A.data(), T.as<double2>());
     if (mixed) {
-        svd_jacobi_f32(P, T.as<double2>(), T32.as<float2>(), V.as<float2>(), status.as<int>(), 60, 3e-7f);
-        svd_finalize_f32(P, T32.as<float2>(), V.as<float2>(), Us.as<float2>(), Vs.as<float2>(), S.as<double>());
+        svd_jacobi_f32(P, T.as<double2>(), T32.as<float2>(), status.as<int>(), 60, 3e-7f);
+        svd_finalize_f32(P, T32.as<float2>(), Us.as<float2>(), S.as<double>());
     } else {
         svd_jacobi(P, T.as<double2>(), V.as<double2>(), status.as<int>(), 60, 1e-15);
         svd_finalize(P, T.as<double2>(), V.as<double2>(), Us.as<double2>(), Vs.as<double2>(), S.as<double>());
@@ -753,7 +758,9 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
     std::vector<std::pair<int, double>> collect;
     for (size_t s = 0; s < P.secs.size(); ++s) {
         const int q = l2r ? rows[sec_rc[s].first].q : cols[sec_rc[s].second].q;
-        for (int i = 0; i < P.secs[s].q; ++i) collect.push_back({q, sv[P.secs[s].s_off + i]});
+        // min(m, n) singular values (a wide mixed-mode T has q - p surplus zero columns, sorted last)
+        const int ns = std::min(P.secs[s].m, P.secs[s].n);
+        for (int i = 0; i < ns; ++i) collect.push_back({q, sv[P.secs[s].s_off + i]});
     }
     std::sort(collect.begin(), collect.end(), [](const std::pair<int, double> &a, const std::pair<int, double> &b) {
         return a.second > b.second;
@@ -843,7 +850,7 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
     DevBuf Y(std::max<int64_t>(1, y_elems) * sizeof(double2)), Wb(std::max<int64_t>(1, w_elems) * sizeof(double2));
     DevBuf cst(std::max<size_t>(1, pol.size()) * sizeof(int)), cdiag(std::max<size_t>(1, pol.size()) * sizeof(double));
     KV_CUDA(cudaMemsetAsync(cst.p, 0, std::max<size_t>(1, pol.size()) * sizeof(int), ctx().stream));
-    svd_extract(dpol, (int)pol.size(), P, Us.as<float2>(), Vs.as<float2>(), Wb.as<double2>(), 1 - side);
+    svd_extract(dpol, (int)pol.size(), P, Us.as<float2>(), Wb.as<double2>());
     const int tm = kTileM(KV_FP64), tn = kTileN(KV_FP64);
     auto add_gemm = [&](GemmPlan &g, int64_t c_off, int M, int N, GemmSeg seg) {
         const int sb = (int)g.segs.size();
@@ -1035,6 +1042,9 @@ Tdvp::~Tdvp() {
 }
 
 void Tdvp::mark(int module, bool start) {
+    const auto now = std::chrono::steady_clock::now();
+    if (start) host_t0 = now;
+    else module_host_ms[module] += std::chrono::duration<double, std::milli>(now - host_t0).count();
     if (n_marks >= kMaxEvents) return;
     KV_CUDA(cudaEventRecord(events[2 * n_marks + (start ? 0 : 1)], ctx().stream));
     if (!start) { mark_module[n_marks] = module; ++n_marks; }
@@ -1062,6 +1072,9 @@ void Tdvp::begin_sweep() {
     n_krylov = 0;
     krylov_flops.clear();
     other = Flops{};
+    for (auto &m : module_host_ms) m = 0.0;
+    plan_stats(&plans0, &plan_ms0);
+    sweep_t0 = std::chrono::steady_clock::now();
     KV_CUDA(cudaEventRecord(sweep_ev[0], ctx().stream));
 }
 
@@ -1074,6 +1087,14 @@ static int tdvp_iters_of(const KrylovState *st, void *arg) {
 void Tdvp::end_sweep() {
     KV_CUDA(cudaEventRecord(sweep_ev[1], ctx().stream));
     KV_CUDA(cudaStreamSynchronize(ctx().stream));
+    sweep_host_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - sweep_t0).count();
+    {
+        long long b = 0;
+        double ms = 0.0;
+        plan_stats(&b, &ms);
+        plans_built = b - plans0;
+        plan_ms = ms - plan_ms0;
+    }
     float sms = 0.f;
     KV_CUDA(cudaEventElapsedTime(&sms, sweep_ev[0], sweep_ev[1]));
     sweep_ms = sms;

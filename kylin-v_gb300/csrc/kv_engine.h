@@ -1,5 +1,7 @@
 // Host-side engine declarations: plans, operations, TDVP driver.
 #pragma once
+#include <chrono>
+
 #include "kv_internal.h"
 
 namespace kv {
@@ -54,6 +56,8 @@ HeffPlan plan_heff(int nsite, const Meta &L, const Meta &psi, const Meta *W1, co
                    int precision, int max_iter);
 
 void clear_plan_cache();
+// H_eff plans built (cache misses) and host ms spent building them since kv_init
+void plan_stats(long long *built, double *ms);
 TensorP op_product(const DTensor &A, const DTensor &B, int nc, int opA, int opB, int precision,
                    Flops *fl = nullptr);
 TensorP op_heff(int nsite, const DTensor &L, const DTensor &psi, const DTensor *W1, const DTensor *W2,
@@ -87,6 +91,10 @@ class Tdvp {
     int precision;
     double module_ms[MOD_COUNT] = {};
     double sweep_ms = 0.0;
+    double module_host_ms[MOD_COUNT] = {};  // host wall-clock of the last sweep
+    double sweep_host_ms = 0.0;
+    long long plans_built = 0;               // H_eff plan-cache misses in the last sweep
+    double plan_ms = 0.0;                    // host ms spent building them
     double last_ref_flops = 0.0;   // all reference zgemm flops of the last sweep
     double last_gemm_flops = 0.0;  // of which in product<> pairs (grouped GEMM)
 
@@ -102,6 +110,9 @@ class Tdvp {
     DevBuf kstate;
     std::vector<cudaEvent_t> events;
     int mark_module[kMaxEvents] = {};
+    std::chrono::steady_clock::time_point host_t0, sweep_t0;
+    long long plans0 = 0;
+    double plan_ms0 = 0.0;
     int n_marks = 0, n_krylov = 0;
     std::vector<std::pair<KrylovState *, std::vector<Flops>>> krylov_flops;
     Flops other;

@@ -225,8 +225,9 @@ struct GemmPlan {
     // tensor-core path only
     std::vector<SliceJob> ajobs, bjobs;
     std::vector<SegX> xsegs;
+    std::vector<int2> aitems, bitems;  // (job, first of 8 rows) per slicing CTA
     int64_t a_planes = 0, b_planes = 0, a_exps = 0, b_exps = 0;
-    DevBuf d_ajobs, d_bjobs, d_xsegs;
+    DevBuf d_ajobs, d_bjobs, d_xsegs, d_aitems, d_bitems;
     void upload() {
         d_tiles = upload_vec(tiles);
         d_segs = upload_vec(segs);

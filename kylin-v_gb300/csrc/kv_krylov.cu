@@ -151,6 +151,16 @@ __global__ void __launch_bounds__(32) k_tridiag_exp(KrylovState *st, int reverse
             Z[i][lane] = make_double2(i == lane ? 1.0 : 0.0, 0.0);
         }
     __syncwarp();
+    // off-diagonal entries below 1e-15 ||T||_F are below FP64 resolution of
+    // the eigen-decomposition and are not rotated (quadratic convergence: a
+    // handful of sweeps)
+    double fro = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double2 h = lane < n ? H[i][lane] : make_double2(0.0, 0.0);
+        fro += h.x * h.x + h.y * h.y;
+    }
+    for (int o = 16; o; o >>= 1) fro += __shfl_xor_sync(0xFFFFFFFFu, fro, o);
+    const double thr = 1e-15 * sqrt(fro);
     for (int sweep = 0; sweep < 60; ++sweep) {
         if (lane == 0) any_rot = 0;
         __syncwarp();
@@ -162,7 +172,7 @@ __global__ void __launch_bounds__(32) k_tridiag_exp(KrylovState *st, int reverse
                     const double ac = sqrt(cr * cr + ci * ci);
                     kvj::Rot<double> r;
                     r.cs = 0.0;
-                    if (ac > 1e-300 && ac > 1e-17 * (fabs(a) + fabs(b))) {
+                    if (ac > 1e-300 && ac > thr) {
                         const double z = (b - a) / (2.0 * ac);
                         const double t = (z >= 0.0 ? 1.0 : -1.0) / (fabs(z) + sqrt(1.0 + z * z));
                         r.cs = 1.0 / sqrt(1.0 + t * t);

@@ -113,6 +113,79 @@ __global__ void __launch_bounds__(NT) k_svd_jacobi(const SvdSector *__restrict__
     if (threadIdx.x == 0) status[blockIdx.x] = converged ? sweep : -sweep;
 }
 
+// Mixed mode: one-sided Jacobi in FP32 without accumulated rotations.  T is
+// oriented so that the singular vectors wanted afterwards are its own columns
+// (they converge to sigma_j w_j); T stays in shared memory when p*q <=
+// smem_elems.  Columns below 1e-7 of ||T||_F are numerically zero in FP32 and
+// are not rotated (this also lets wide T, q > p, converge: its q - p surplus
+// columns go to zero).
+template <int NT>
+__global__ void __launch_bounds__(NT) k_svd_jacobi_w(const SvdSector *__restrict__ secs, float2 *__restrict__ T,
+                                                     int *status, int max_sweeps, float tol, int smem_elems) {
+    extern __shared__ float2 sT[];
+    __shared__ int rotated;
+    __shared__ float red[NT / 32];
+    const SvdSector s = secs[blockIdx.x];
+    const int p = s.p, q = s.q;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = NT / 32;
+    float2 *g = T + s.t_off;
+    const int64_t n = (int64_t)p * q;
+    const bool in_smem = n <= smem_elems;
+    float2 *t = in_smem ? sT : g;
+    float fro = 0.f;
+    for (int64_t e = threadIdx.x; e < n; e += NT) {
+        const float2 v = g[e];
+        if (in_smem) sT[e] = v;
+        fro += v.x * v.x + v.y * v.y;
+    }
+    for (int o = 16; o > 0; o >>= 1) fro += __shfl_xor_sync(0xffffffffu, fro, o);
+    if (lane == 0) red[warp] = fro;
+    __syncthreads();
+    float tot = 0.f;
+    for (int w = 0; w < nw; ++w) tot += red[w];
+    const float zt = 1e-14f * tot;  // (1e-7 ||T||_F)^2
+    const int qe = q + (q & 1);
+    int sweep = 0;
+    bool converged = (q < 2);
+    for (; sweep < max_sweeps && !converged; ++sweep) {
+        if (threadIdx.x == 0) rotated = 0;
+        __syncthreads();
+        for (int r = 0; r < qe - 1; ++r) {
+            for (int pi = warp; pi < qe / 2; pi += nw) {
+                int c0, c1;
+                kvj::tournament_pair(qe, r, pi, c0, c1);
+                if (c1 >= q) continue;
+                float2 *x = t + (int64_t)c0 * p, *y = t + (int64_t)c1 * p;
+                float a = 0, b = 0, cr = 0, ci = 0;
+                for (int i = lane; i < p; i += 32) {
+                    const float2 xi = x[i], yi = y[i];
+                    a += xi.x * xi.x + xi.y * xi.y;
+                    b += yi.x * yi.x + yi.y * yi.y;
+                    cr += xi.x * yi.x + xi.y * yi.y;
+                    ci += xi.x * yi.y - xi.y * yi.x;
+                }
+                warp_sum3<float>(a, b, cr, ci);
+                if (!(a > zt) || !(b > zt)) continue;
+                kvj::Rot<float> rot;
+                if (!kvj::make_rotation<float>(a, b, cr, ci, tol, rot)) continue;
+                if (lane == 0) rotated = 1;
+                for (int i = lane; i < p; i += 32) {
+                    float2 xi = x[i], yi = y[i];
+                    kvj::rotate_pair(rot, xi.x, xi.y, yi.x, yi.y);
+                    x[i] = xi;
+                    y[i] = yi;
+                }
+            }
+            __syncthreads();
+        }
+        converged = (rotated == 0);
+        __syncthreads();
+    }
+    if (in_smem)
+        for (int64_t e = threadIdx.x; e < n; e += NT) g[e] = sT[e];
+    if (threadIdx.x == 0) status[blockIdx.x] = converged ? sweep : -sweep;
+}
+
 // singular values (as double), descending order, normalised U columns
 template <class R>
 __global__ void __launch_bounds__(256) k_svd_finalize(const SvdSector *__restrict__ secs,
@@ -146,7 +219,8 @@ __global__ void __launch_bounds__(256) k_svd_finalize(const SvdSector *__restric
             x.y *= inv;
             Us[s.t_off + (int64_t)rank * p + i] = x;
         }
-        for (int i = lane; i < q; i += 32) Vs[s.v_off + (int64_t)rank * q + i] = V[s.v_off + (int64_t)j * q + i];
+        if (V)
+            for (int i = lane; i < q; i += 32) Vs[s.v_off + (int64_t)rank * q + i] = V[s.v_off + (int64_t)j * q + i];
         if (lane == 0) S[s.s_off + rank] = sj;
     }
 }
@@ -157,19 +231,16 @@ __global__ void k_to_f32(const double2 *__restrict__ in, float2 *__restrict__ ou
 }
 
 // ------------------------------------------------------- FP64 polish
-// Kept columns of one factor as a row-major FP64 matrix:
-// side 0 -> U_A[:, :k] (m x k);  side 1 -> V_A[:, :k] (n x k).
+// The first k sorted Jacobi columns (the kept singular vectors of the side
+// T's columns live in) as a row-major FP64 matrix W (p x k).
 __global__ void k_svd_extract(const SvdPolish *__restrict__ pol, const SvdSector *__restrict__ secs,
-                              const float2 *__restrict__ Us, const float2 *__restrict__ Vs, double2 *__restrict__ W,
-                              int side) {
+                              const float2 *__restrict__ Us, double2 *__restrict__ W) {
     const SvdPolish d = pol[blockIdx.x];
     const SvdSector s = secs[d.sector];
-    const int rows = side == 0 ? s.m : s.n, k = d.k;
-    for (int64_t e = threadIdx.x; e < (int64_t)rows * k; e += blockDim.x) {
+    const int k = d.k;
+    for (int64_t e = threadIdx.x; e < (int64_t)s.p * k; e += blockDim.x) {
         const int i = (int)(e / k), j = (int)(e % k);
-        // U_A = U (not transposed) or V (transposed); V_A = V (not transposed) or U (transposed)
-        const bool from_u = (side == 0) != (s.transposed != 0);
-        float2 v = from_u ? Us[s.t_off + (int64_t)j * s.p + i] : Vs[s.v_off + (int64_t)j * s.q + i];
+        const float2 v = Us[s.t_off + (int64_t)j * s.p + i];
         W[d.w_off + e] = make_double2(v.x, v.y);
     }
 }
@@ -329,29 +400,38 @@ void svd_scatter(const std::vector<SvdScatter> &sc, const SvdPlan &p, const doub
     KV_CUDA(cudaGetLastError());
 }
 
-void svd_jacobi_f32(const SvdPlan &p, const double2 *T64, float2 *T, float2 *V, int *status, int max_sweeps,
-                    float tol) {
+void svd_jacobi_f32(const SvdPlan &p, const double2 *T64, float2 *T, int *status, int max_sweeps, float tol) {
     if (p.secs.empty()) return;
+    static int smem_bytes = 0;  // dynamic shared memory the kernel may use (opt-in maximum less 4 KB)
+    if (!smem_bytes) {
+        int optin = 0;
+        KV_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx().device));
+        smem_bytes = std::max(0, optin - 4096);
+        KV_CUDA(cudaFuncSetAttribute(k_svd_jacobi_w<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
+    }
+    int64_t max_pq = 0;
+    for (auto &s : p.secs) max_pq = std::max<int64_t>(max_pq, (int64_t)s.p * s.q);
+    const int cap = smem_bytes / (int)sizeof(float2);
+    const int elems = (int)std::min<int64_t>(max_pq, cap);
     k_to_f32<<<std::max(1, ctx().num_sms * 4), 256, 0, ctx().stream>>>(T64, T, p.t_elems);
     counted();
-    k_svd_jacobi<float, 1024><<<(unsigned)p.secs.size(), 1024, 0, ctx().stream>>>(p.d_secs.as<SvdSector>(), T, V,
-                                                                                   status, max_sweeps, tol);
+    k_svd_jacobi_w<1024><<<(unsigned)p.secs.size(), 1024, (size_t)elems * sizeof(float2), ctx().stream>>>(
+        p.d_secs.as<SvdSector>(), T, status, max_sweeps, tol, elems);
     counted();
     KV_CUDA(cudaGetLastError());
 }
 
-void svd_finalize_f32(const SvdPlan &p, const float2 *T, const float2 *V, float2 *Us, float2 *Vs, double *S) {
+void svd_finalize_f32(const SvdPlan &p, const float2 *T, float2 *Us, double *S) {
     if (p.secs.empty()) return;
     k_svd_finalize<float><<<(unsigned)p.secs.size(), 256, sizeof(double) * p.max_q, ctx().stream>>>(
-        p.d_secs.as<SvdSector>(), T, V, Us, Vs, S);
+        p.d_secs.as<SvdSector>(), T, nullptr, Us, nullptr, S);
     counted();
     KV_CUDA(cudaGetLastError());
 }
 
-void svd_extract(const DevBuf &pol, int npol, const SvdPlan &p, const float2 *Us, const float2 *Vs, double2 *W,
-                 int side) {
+void svd_extract(const DevBuf &pol, int npol, const SvdPlan &p, const float2 *Us, double2 *W) {
     if (npol == 0) return;
-    k_svd_extract<<<npol, 256, 0, ctx().stream>>>(pol.as<SvdPolish>(), p.d_secs.as<SvdSector>(), Us, Vs, W, side);
+    k_svd_extract<<<npol, 256, 0, ctx().stream>>>(pol.as<SvdPolish>(), p.d_secs.as<SvdSector>(), Us, W);
     counted();
     KV_CUDA(cudaGetLastError());
 }

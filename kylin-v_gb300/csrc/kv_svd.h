@@ -9,7 +9,7 @@ struct SvdSector {
     int64_t t_off;  // T (p x q, column-major) and its sorted U copy
     int64_t v_off;  // V (q x q, column-major) and its sorted copy
     int64_t s_off;  // q singular values
-    int p, q;       // tall orientation, p >= q
+    int p, q;       // FP64 path: tall orientation, p >= q; mixed path: see op_svd
     int transposed; // 0: T = A (m = p, n = q); 1: T = A^H (m = q, n = p)
     int m, n;       // sector matrix of A (rows x cols)
 };
@@ -48,11 +48,12 @@ struct SvdDense {
 };
 
 void svd_gather(const SvdPlan &p, const double2 *A, double2 *T);
-void svd_jacobi_f32(const SvdPlan &p, const double2 *T64, float2 *T, float2 *V, int *status, int max_sweeps,
-                    float tol);
-void svd_finalize_f32(const SvdPlan &p, const float2 *T, const float2 *V, float2 *Us, float2 *Vs, double *S);
-void svd_extract(const DevBuf &pol, int npol, const SvdPlan &p, const float2 *Us, const float2 *Vs, double2 *W,
-                 int side);
+// mixed mode: FP32 one-sided Jacobi of T without accumulated rotations
+// (T oriented so the wanted singular vectors are its columns), sorted
+// normalised columns and singular values, and the first k columns in FP64
+void svd_jacobi_f32(const SvdPlan &p, const double2 *T64, float2 *T, int *status, int max_sweeps, float tol);
+void svd_finalize_f32(const SvdPlan &p, const float2 *T, float2 *Us, double *S);
+void svd_extract(const DevBuf &pol, int npol, const SvdPlan &p, const float2 *Us, double2 *W);
 void svd_chol(const DevBuf &pol, int npol, double2 *G, int *status, double *diagv, double shift);
 void svd_trsm(const DevBuf &pol, const std::vector<int> &item_pol, const std::vector<int> &item_row0,
               const double2 *G, double2 *X);

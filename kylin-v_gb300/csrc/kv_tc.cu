@@ -45,6 +45,7 @@
 #include <cuda_fp16.h>
 
 #include <cstdint>
+#include <cstring>
 #include <map>
 #include <utility>
 
@@ -102,50 +103,74 @@ __device__ __forceinline__ int panel_off(int r, int k) {
     return (r >> 3) * 128 + (k >> 3) * 64 + (r & 7) * 8 + (k & 7);
 }
 
+// two digits (|d| <= 512) as FP16: 1536 + d in the binade [1024, 2048) has
+// unit spacing, so its bits are 0x6600 + d; subtracting 1536 is exact
+__device__ __forceinline__ __half2 digits2(int d0, int d1) {
+    const uint32_t u = (uint32_t)(0x6600 + d0) | ((uint32_t)(0x6600 + d1) << 16);
+    __half2 h;
+    memcpy(&h, &u, sizeof(h));
+    return __hsub2(h, __float2half2_rn(1536.f));
+}
+
+// One CTA per (job, 8 consecutive rows); one warp per row: pass 1 finds the
+// row exponent, pass 2 writes the digits of two adjacent K positions per lane.
 template <int TR>
-__global__ void __launch_bounds__(256) k_slice(const SliceJob *__restrict__ jobs, const double2 *__restrict__ src,
-                                               __half *__restrict__ dst, int *__restrict__ exps, double alpha,
-                                               const int *skip) {
+__global__ void __launch_bounds__(256) k_slice(const SliceJob *__restrict__ jobs, const int2 *__restrict__ items,
+                                               const double2 *__restrict__ src, __half *__restrict__ dst,
+                                               int *__restrict__ exps, double alpha, const int *skip) {
     if (skip && *skip) return;
-    const SliceJob j = jobs[blockIdx.x];
+    const int2 it = items[blockIdx.x];
+    const SliceJob j = jobs[it.x];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r = it.y + warp;
     const int prow = ((j.rows + TR - 1) / TR) * TR;
+    if (r >= prow) return;
     const int kpad = j.nkc * BKC;
     const double2 *s = src + j.src_off;
     const bool scale = alpha != 1.0;
-    for (int r = warp; r < prow; r += 8) {
-        unsigned long long mx = 0;
-        if (r < j.rows)
-            for (int k = lane; k < j.K; k += 32) {
-                double2 v = s[j.trans ? (int64_t)k * j.ld + r : (int64_t)r * j.ld + k];
-                if (scale) { v.x *= alpha; v.y *= alpha; }
-                const unsigned long long br = (unsigned long long)__double_as_longlong(v.x) & 0x7FFFFFFFFFFFFFFFull;
-                const unsigned long long bi = (unsigned long long)__double_as_longlong(v.y) & 0x7FFFFFFFFFFFFFFFull;
-                mx = max(mx, max(br, bi));
-            }
+    auto load = [&](int k) {
+        double2 v = s[j.trans ? (int64_t)k * j.ld + r : (int64_t)r * j.ld + k];
+        if (scale) { v.x *= alpha; v.y *= alpha; }
+        if (j.conj) v.y = -v.y;
+        return v;
+    };
+    unsigned long long mx = 0;
+    if (r < j.rows)
+        for (int k = lane; k < j.K; k += 32) {
+            const double2 v = load(k);
+            const unsigned long long br = (unsigned long long)__double_as_longlong(v.x) & 0x7FFFFFFFFFFFFFFFull;
+            const unsigned long long bi = (unsigned long long)__double_as_longlong(v.y) & 0x7FFFFFFFFFFFFFFFull;
+            mx = max(mx, max(br, bi));
+        }
 #pragma unroll
-        for (int o = 16; o; o >>= 1) mx = max(mx, (unsigned long long)__shfl_xor_sync(0xFFFFFFFFu, mx, o));
-        const int e = mx ? (int)(mx >> 52) - 1022 : kZeroExp;
-        if (lane == 0) exps[j.exp_off + r] = e;
-        __half *pan = dst + j.dst_off + (int64_t)(r / TR) * j.nkc * (NPL * TR * BKC);
-        const int rr = r % TR;
-        for (int k = lane; k < kpad; k += 32) {
+    for (int o = 16; o; o >>= 1) mx = max(mx, (unsigned long long)__shfl_xor_sync(0xFFFFFFFFu, mx, o));
+    const int e = mx ? (int)(mx >> 52) - 1022 : kZeroExp;
+    if (lane == 0) exps[j.exp_off + r] = e;
+    __half *pan = dst + j.dst_off + (int64_t)(r / TR) * j.nkc * (NPL * TR * BKC);
+    const int rr = r % TR;
+    for (int k = 2 * lane; k < kpad; k += 64) {  // k even: k and k + 1 are adjacent in the panel
+        int x[2][NCOMP];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
             int xr = 0, xi = 0;
-            if (r < j.rows && k < j.K) {
-                double2 v = s[j.trans ? (int64_t)k * j.ld + r : (int64_t)r * j.ld + k];
-                if (scale) { v.x *= alpha; v.y *= alpha; }
+            if (r < j.rows && k + h < j.K) {
+                const double2 v = load(k + h);
                 xr = fixq(v.x, e);
-                xi = fixq(j.conj ? -v.y : v.y, e);
+                xi = fixq(v.y, e);
             }
-            const int xs[NCOMP] = {xr, xi, xr + xi};
-            __half *p = pan + (int64_t)(k / BKC) * (NPL * TR * BKC) + panel_off<TR>(rr, k & (BKC - 1));
+            x[h][0] = xr;
+            x[h][1] = xi;
+            x[h][2] = xr + xi;
+        }
+        __half *p = pan + (int64_t)(k / BKC) * (NPL * TR * BKC) + panel_off<TR>(rr, k & (BKC - 1));
 #pragma unroll
-            for (int c = 0; c < NCOMP; ++c) {
-                int d[NDIG];
-                digits(xs[c], d);
+        for (int c = 0; c < NCOMP; ++c) {
+            int d0[NDIG], d1[NDIG];
+            digits(x[0][c], d0);
+            digits(x[1][c], d1);
 #pragma unroll
-                for (int i = 0; i < NDIG; ++i) p[(c * NDIG + i) * (TR * BKC)] = __int2half_rn(d[i]);
-            }
+            for (int i = 0; i < NDIG; ++i)
+                *reinterpret_cast<__half2 *>(p + (c * NDIG + i) * (TR * BKC)) = digits2(d0[i], d1[i]);
         }
     }
 }
@@ -511,10 +536,18 @@ void plan_mixed(GemmPlan &g) {
                    "internal: inconsistent block views in a mixed-precision plan");
         g.xsegs[s] = SegX{ja.dst_off, jb.dst_off, nkc, ja.exp_off, jb.exp_off, 0};
     }
+    g.aitems.clear();
+    g.bitems.clear();
+    for (size_t i = 0; i < g.ajobs.size(); ++i)
+        for (int r0 = 0; r0 < (g.ajobs[i].rows + BM - 1) / BM * BM; r0 += 8) g.aitems.push_back({(int)i, r0});
+    for (size_t i = 0; i < g.bjobs.size(); ++i)
+        for (int r0 = 0; r0 < (g.bjobs[i].rows + BN - 1) / BN * BN; r0 += 8) g.bitems.push_back({(int)i, r0});
     KV_REQUIRE(g.a_exps < (1ll << 31) && g.b_exps < (1ll << 31), KV_EINVAL, "mixed-precision plan too large");
     g.d_ajobs = upload_vec(g.ajobs);
     g.d_bjobs = upload_vec(g.bjobs);
     g.d_xsegs = upload_vec(g.xsegs);
+    g.d_aitems = upload_vec(g.aitems);
+    g.d_bitems = upload_vec(g.bitems);
 }
 
 void launch_gemm_mixed(const GemmPlan &p, const double2 *A, const double2 *B, double2 *C, double alpha,
@@ -532,15 +565,15 @@ void launch_gemm_mixed(const GemmPlan &p, const double2 *A, const double2 *B, do
     DevBuf ap(std::max<int64_t>(1, p.a_planes) * sizeof(__half)), bp(std::max<int64_t>(1, p.b_planes) * sizeof(__half));
     DevBuf ae(std::max<int64_t>(1, p.a_exps) * sizeof(int)), be(std::max<int64_t>(1, p.b_exps) * sizeof(int));
     int n = 0;
-    if (!p.ajobs.empty()) {
-        k_slice<BM><<<(unsigned)p.ajobs.size(), 256, 0, c.stream>>>(p.d_ajobs.as<SliceJob>(), A, ap.as<__half>(),
-                                                                    ae.as<int>(), 1.0, skip);
+    if (!p.aitems.empty()) {
+        k_slice<BM><<<(unsigned)p.aitems.size(), 256, 0, c.stream>>>(p.d_ajobs.as<SliceJob>(), p.d_aitems.as<int2>(),
+                                                                     A, ap.as<__half>(), ae.as<int>(), 1.0, skip);
         KV_CUDA(cudaGetLastError());
         ++n;
     }
-    if (!p.bjobs.empty()) {
-        k_slice<BN><<<(unsigned)p.bjobs.size(), 256, 0, c.stream>>>(p.d_bjobs.as<SliceJob>(), B, bp.as<__half>(),
-                                                                    be.as<int>(), alpha, skip);
+    if (!p.bitems.empty()) {
+        k_slice<BN><<<(unsigned)p.bitems.size(), 256, 0, c.stream>>>(p.d_bjobs.as<SliceJob>(), p.d_bitems.as<int2>(),
+                                                                     B, bp.as<__half>(), be.as<int>(), alpha, skip);
         KV_CUDA(cudaGetLastError());
         ++n;
     }

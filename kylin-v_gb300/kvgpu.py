@@ -28,6 +28,7 @@ EXPORTS = (
     "kv_tensor_download", "kv_tensor_free", "kv_product", "kv_heff_apply", "kv_env_update", "kv_lanczos_expm",
     "kv_svd_truncate", "kv_tdvp_create", "kv_tdvp_sweep", "kv_tdvp_site", "kv_tdvp_stats", "kv_tdvp_free",
     "kv_expectation", "kv_profile", "kv_profile_read", "kv_counters", "kv_expectation_noalloc",
+    "kv_tdvp_host_stats",
 )
 
 
@@ -69,6 +70,7 @@ def lib():
         L.kv_tdvp_sweep.argtypes = [vp, ctypes.c_int]
         L.kv_tdvp_site.argtypes = [vp, ctypes.c_int, pvp]
         L.kv_tdvp_stats.argtypes = [vp, dp, dp, dp, dp]
+        L.kv_tdvp_host_stats.argtypes = [vp, dp, dp, ctypes.POINTER(ctypes.c_longlong), dp]
         L.kv_profile.argtypes = [ctypes.c_int]
         L.kv_profile_read.argtypes = [dp, dp, ctypes.POINTER(ctypes.c_longlong)]
         L.kv_counters.argtypes = [ctypes.POINTER(ctypes.c_longlong)]
@@ -282,6 +284,16 @@ class TDVP:
         check(lib().kv_tdvp_stats(self.ptr, ms, ctypes.byref(sw), ctypes.byref(fl), ctypes.byref(fg)))
         return {"modules_ms": dict(zip(MODULES, list(ms))), "sweep_ms": sw.value, "ref_flops": fl.value,
                 "gemm_ref_flops": fg.value}
+
+    def host_stats(self) -> dict:
+        """Last sweep, host side: per-module and sweep wall-clock ms, H_eff
+        plans built (plan-cache misses) and the host ms spent building them."""
+        ms = (ctypes.c_double * len(MODULES))()
+        sw, pm = ctypes.c_double(), ctypes.c_double()
+        nb = ctypes.c_longlong()
+        check(lib().kv_tdvp_host_stats(self.ptr, ms, ctypes.byref(sw), ctypes.byref(nb), ctypes.byref(pm)))
+        return {"modules_ms": dict(zip(MODULES, list(ms))), "sweep_ms": sw.value, "plans_built": nb.value,
+                "plan_ms": pm.value}
 
     def __del__(self):
         if getattr(self, "ptr", None) and _lib is not None:
