@@ -194,6 +194,7 @@ ProductPlan plan_product(const Meta &A, const Meta &B, int nc, int opA, int opB)
             const int pos = P.out.add(o);
             if (pos == before) {
                 per_out.emplace_back();
+                P.pairs.emplace_back();
                 mn.push_back({nrow, ncol});
             }
             GemmSeg sg;
@@ -205,6 +206,7 @@ ProductPlan plan_product(const Meta &A, const Meta &B, int nc, int opA, int opB)
             sg.lda = (opA == KV_OP_N) ? nk : nrow;
             sg.ldb = (opB == KV_OP_N) ? ncol : nk;
             per_out[pos].push_back(sg);
+            P.pairs[pos].push_back({(int)i, j});
             P.gemm.ref_flops += 8.0 * nrow * (double)ncol * nk;
             P.gemm.max_k = std::max(P.gemm.max_k, nk);
         }
@@ -282,6 +284,8 @@ MixPlanFull plan_mix(const Meta &lm, const Meta &W, int lead, const std::vector<
     R.out.dirs[lead] = W.dirs[0];
     R.out.dirs[lead + 1] = W.dirs[3];
     std::vector<std::vector<MixTerm>> terms;
+    std::vector<std::vector<int>> tin;
+    std::vector<std::vector<double>> tco;
     std::vector<std::array<int, 3>> geo;  // so, wr, rest
     std::unordered_map<LegKey, std::vector<int>, LegKeyHash> widx;
     for (size_t j = 0; j < W.blocks.size(); ++j) widx[leg_key(W.blocks[j], 1, 3)].push_back((int)j);
@@ -302,6 +306,8 @@ MixPlanFull plan_mix(const Meta &lm, const Meta &W, int lead, const std::vector<
             const int pos = R.out.add(o);
             if (pos == before) {
                 terms.emplace_back();
+                tin.emplace_back();
+                tco.emplace_back();
                 geo.push_back({w.shape[0], w.shape[3], rest});
                 R.mult.push_back(0.0);
             }
@@ -309,7 +315,10 @@ MixPlanFull plan_mix(const Meta &lm, const Meta &W, int lead, const std::vector<
             const int K = a.shape[lead] * a.shape[lead + 1];
             terms[pos].push_back({a.off, w.off, K});
             const double nk = (double)prod_range(a, 0, lead);
-            R.ref_flops += mi * 8.0 * nk * w.shape[0] * (double)w.shape[3] * rest * K;
+            const double coef = 8.0 * nk * w.shape[0] * (double)w.shape[3] * rest * K;
+            tin[pos].push_back((int)ai);
+            tco[pos].push_back(coef);
+            R.ref_flops += mi * coef;
         }
     }
     R.out.layout();
@@ -322,7 +331,11 @@ MixPlanFull plan_mix(const Meta &lm, const Meta &W, int lead, const std::vector<
         j.wr = geo[b][1];
         j.rest = geo[b][2];
         j.term_begin = (int)R.mix.terms.size();
-        for (auto &t : terms[b]) R.mix.terms.push_back(t);
+        for (size_t x = 0; x < terms[b].size(); ++x) {
+            R.mix.terms.push_back(terms[b][x]);
+            R.term_in.push_back(tin[b][x]);
+            R.term_coef.push_back(tco[b][x]);
+        }
         j.term_end = (int)R.mix.terms.size();
         const int job = (int)R.mix.jobs.size();
         R.mix.jobs.push_back(j);
@@ -364,14 +377,15 @@ void run_gemm(const GemmPlan &g, const double2 *A, const double2 *B, double2 *C,
               const int *skip, const KrylovState *st, int k, double credit_flops) {
     precision = gemm_mixed(precision) ? KV_MIXED_TF32 : KV_FP64;
     if (g.tiles.empty()) return;
+    const int step = k >= 0 ? k : kAllSteps;
     auto &c = ctx();
     ProfRec rec{};
     if (c.prof) {
         rec = {prof_event(), prof_event(), credit_flops >= 0.0 ? credit_flops : g.ref_flops, st, k};
         KV_CUDA(cudaEventRecord(rec.a, c.stream));
     }
-    if (precision == KV_FP64) launch_gemm_fp64(g, A, B, C, alpha, skip);
-    else if (precision == KV_MIXED_TF32) launch_gemm_mixed(g, A, B, C, alpha, skip);
+    if (precision == KV_FP64) launch_gemm_fp64(g, A, B, C, alpha, skip, step);
+    else if (precision == KV_MIXED_TF32) launch_gemm_mixed(g, A, B, C, alpha, skip, step);
     else throw Error(KV_EINVAL, "unknown precision mode");
     if (c.prof) {
         KV_CUDA(cudaEventRecord(rec.b, c.stream));
@@ -396,63 +410,126 @@ TensorP op_product(const DTensor &A, const DTensor &B, int nc, int opA, int opB,
 }
 
 // --------------------------------------------------------- H_eff plans
-// Krylov layout: the closure of psi's blocks under H_eff (union of input and
-// output block sets until stable), so every Lanczos vector and H_eff . v share
-// one layout; blocks absent from the reference's tensors are zero.  The
-// reference's vectors grow towards that closure one application at a time
-// (hv += V_{k-1} beta, V_k alpha merge block sets, holstein/exponential.h:126-137);
-// iter_flops[k] replays that growth so only the block pairs the reference
-// multiplies at iteration k are credited.  Each closure step builds the
-// product / mixing plans of one application once; those of the step that
-// adds no block are the final plans.
+// Krylov layout.  The reference's Lanczos vector v_k carries the blocks
+// reached from psi within k applications of H_eff (hv += V_{k-1} beta,
+// V_k alpha merge block sets, holstein/exponential.h:126-137), and iteration
+// k multiplies exactly the block pairs of v_k.  Here the layout is psi's
+// blocks followed by the blocks first reached at application 1, 2, ..., napply
+// = max(1, max_iter - 1) (v_k occupies a prefix of the layout), found by
+// applying the planner to the newly reached blocks only.  Every block pair
+// and mixing term carries the application from which its input is nonzero
+// (its entry): launches at iteration k skip entries > k, the vector kernels
+// work on the prefix, and iter_flops[k] credits exactly the pairs with entry
+// <= k.
 HeffPlan plan_heff(int nsite, const Meta &L, const Meta &psi, const Meta *W1, const Meta *W2, const Meta &R,
                    int precision, int max_iter) {
     HeffPlan H;
     H.nsite = nsite;
+    H.napply = std::max(1, max_iter - 1);
     Meta K = psi;
     K.layout();
-    for (int iter = 0;; ++iter) {
-        KV_REQUIRE(iter < 4096, KV_EINVAL, "H_eff block closure did not converge");
-        Flops f;
-        ProductPlan P1 = plan_product(L, K, 1, KV_OP_N, KV_OP_N);
-        f.gemm += P1.gemm.ref_flops;
-        // reference blocks merged into each computed block (the reference keeps
-        // every matched MPO-mixing pair as its own block)
-        std::vector<double> mult(P1.out.blocks.size(), 1.0);
-        MixPlanFull m1, m2;
-        const Meta *last = &P1.out;
-        if (nsite >= 1) {
-            m1 = plan_mix(*last, *W1, 1, &mult);
-            f.mix += m1.ref_flops;
-            mult = m1.mult;
-            last = &m1.out;
-        }
-        if (nsite == 2) {
-            m2 = plan_mix(*last, *W2, 2, &mult);
-            f.mix += m2.ref_flops;
-            mult = m2.mult;
-            last = &m2.out;
-        }
-        f.gemm += ref_product_flops(*last, R, 2, KV_OP_N, KV_OP_T, &mult, nullptr);
-        ProductPlan P2 = plan_product(*last, R, 2, KV_OP_N, KV_OP_T);
-        if (iter < max_iter) H.iter_flops.push_back(f);
-        bool grew = false;
-        for (auto &b : P2.out.blocks) {
+    std::vector<int> entry(K.blocks.size(), 0);
+    H.prefix.push_back(K.nelem);
+    Meta fresh = psi;  // blocks whose images under H_eff are not yet in K
+    fresh.layout();
+    for (int reached = 1; reached <= H.napply && !fresh.blocks.empty(); ++reached) {
+        Meta last = plan_product(L, fresh, 1, KV_OP_N, KV_OP_N).out;
+        if (nsite >= 1) last = plan_mix(last, *W1, 1).out;
+        if (nsite == 2) last = plan_mix(last, *W2, 2).out;
+        const Meta out = plan_product(last, R, 2, KV_OP_N, KV_OP_T).out;
+        Meta next;
+        next.rank = K.rank;
+        next.dirs = K.dirs;
+        for (auto &b : out.blocks) {
             const size_t before = K.blocks.size();
-            if ((size_t)K.add(b) == before) grew = true;
-        }
-        if (!grew) {
-            while ((int)H.iter_flops.size() < max_iter) H.iter_flops.push_back(f);
-            H.p1 = std::move(P1);
-            H.m1 = std::move(m1);
-            H.m2 = std::move(m2);
-            H.p2 = std::move(P2);
-            break;
+            if ((size_t)K.add(b) == before) {
+                entry.push_back(reached);
+                next.blocks.push_back(b);
+            }
         }
         K.layout();
+        H.prefix.push_back(K.nelem);
+        next.layout();
+        fresh = std::move(next);
+    }
+    while ((int)H.prefix.size() <= H.napply) H.prefix.push_back(K.nelem);
+    // the inputs: blocks of v_0 .. v_{napply-1} (a prefix of K, same offsets)
+    Meta Kin;
+    Kin.rank = K.rank;
+    Kin.dirs = K.dirs;
+    for (size_t b = 0; b < K.blocks.size() && entry[b] < H.napply; ++b) Kin.blocks.push_back(K.blocks[b]);
+    Kin.layout();
+    H.p1 = plan_product(L, Kin, 1, KV_OP_N, KV_OP_N);
+    std::vector<int> e_last(H.p1.out.blocks.size(), kAllSteps);
+    for (size_t b = 0; b < H.p1.per_out.size(); ++b)
+        for (size_t x = 0; x < H.p1.per_out[b].size(); ++x) {
+            const int e = entry[H.p1.pairs[b][x].second];
+            H.p1.per_out[b][x].entry = e;
+            e_last[b] = std::min(e_last[b], e);
+        }
+    // a mixing term is live from its input block's entry; an output block from its first live term
+    auto mix_entries = [](MixPlanFull &m, const std::vector<int> &ein) {
+        std::vector<int> eout(m.out.blocks.size(), kAllSteps);
+        for (size_t j = 0; j < m.mix.jobs.size(); ++j)
+            for (int t = m.mix.jobs[j].term_begin; t < m.mix.jobs[j].term_end; ++t) {
+                const int e = ein[m.term_in[t]];
+                m.mix.terms[t].entry = e;
+                eout[j] = std::min(eout[j], e);
+            }
+        return eout;
+    };
+    const Meta *last = &H.p1.out;
+    if (nsite >= 1) {
+        H.m1 = plan_mix(*last, *W1, 1);
+        e_last = mix_entries(H.m1, e_last);
+        last = &H.m1.out;
+    }
+    if (nsite == 2) {
+        H.m2 = plan_mix(*last, *W2, 2);
+        e_last = mix_entries(H.m2, e_last);
+        last = &H.m2.out;
+    }
+    H.p2 = plan_product(*last, R, 2, KV_OP_N, KV_OP_T);
+    for (size_t b = 0; b < H.p2.per_out.size(); ++b)
+        for (size_t x = 0; x < H.p2.per_out[b].size(); ++x) H.p2.per_out[b][x].entry = e_last[H.p2.pairs[b][x].first];
+    // reference flops of iteration k: the pairs and terms live at k, MPO-mixing
+    // outputs counted once per matched reference block (the reference does not
+    // merge them, holstein/product.h:203-477)
+    for (int k = 0; k < max_iter; ++k) {
+        Flops f;
+        std::vector<double> mult(H.p1.out.blocks.size(), 0.0);
+        for (size_t b = 0; b < H.p1.per_out.size(); ++b)
+            for (auto &sg : H.p1.per_out[b])
+                if (sg.entry <= k) {
+                    f.gemm += 8.0 * H.p1.mn[b].first * (double)H.p1.mn[b].second * sg.K;
+                    mult[b] = 1.0;
+                }
+        for (MixPlanFull *m : {nsite >= 1 ? &H.m1 : nullptr, nsite == 2 ? &H.m2 : nullptr}) {
+            if (!m) continue;
+            std::vector<double> mo(m->out.blocks.size(), 0.0);
+            for (size_t j = 0; j < m->mix.jobs.size(); ++j)
+                for (int t = m->mix.jobs[j].term_begin; t < m->mix.jobs[j].term_end; ++t)
+                    if (m->mix.terms[t].entry <= k) {
+                        const double mi = mult[m->term_in[t]];
+                        mo[j] += mi;
+                        f.mix += mi * m->term_coef[t];
+                    }
+            mult = std::move(mo);
+        }
+        for (size_t b = 0; b < H.p2.per_out.size(); ++b)
+            for (size_t x = 0; x < H.p2.per_out[b].size(); ++x) {
+                const GemmSeg &sg = H.p2.per_out[b][x];
+                if (sg.entry <= k)
+                    f.gemm += mult[H.p2.pairs[b][x].first] * 8.0 * H.p2.mn[b].first * (double)H.p2.mn[b].second * sg.K;
+            }
+        H.iter_flops.push_back(f);
     }
     H.klayout = K;
     build_tiles(H.p1, own_offsets(H.p1.out), kTileM(precision), kTileN(precision));
+    // intermediates: blocks with no live input are neither computed nor read
+    H.p1.gemm.write_inactive = false;
+    H.m1.mix.write_inactive = false;
+    H.m2.mix.write_inactive = false;
     std::vector<int64_t> tgt;
     std::vector<char> produced(K.blocks.size(), 0);
     for (auto &b : H.p2.out.blocks) {
@@ -548,12 +625,13 @@ void run_heff(const HeffPlan &H, HeffWork &w, const DTensor &L, const double2 *v
     const double credit = (k >= 0 && k < (int)H.iter_flops.size()) ? H.iter_flops[k].gemm : -1.0;
     run_gemm(H.p1.gemm, L.data(), v, w.t1.as<double2>(), 1.0, precision, skip, st, k, credit);
     const double2 *last = w.t1.as<double2>();
+    const int step = k >= 0 ? k : kAllSteps;
     if (H.nsite >= 1) {
-        launch_mix(H.m1.mix, last, W1->data(), w.t2.as<double2>(), skip);
+        launch_mix(H.m1.mix, last, W1->data(), w.t2.as<double2>(), skip, step);
         last = w.t2.as<double2>();
     }
     if (H.nsite == 2) {
-        launch_mix(H.m2.mix, last, W2->data(), w.t3.as<double2>(), skip);
+        launch_mix(H.m2.mix, last, W2->data(), w.t3.as<double2>(), skip, step);
         last = w.t3.as<double2>();
     }
     run_gemm(H.p2.gemm, last, R.data(), out, scale, precision, skip, st, k, credit >= 0.0 ? 0.0 : -1.0);
@@ -596,7 +674,7 @@ TensorP op_heff(int nsite, const DTensor &L, const DTensor &psi, const DTensor *
 // ------------------------------------------------------- local_krylov
 TensorP op_lanczos(int nsite, const DTensor &L, const DTensor &psi, const DTensor *W1, const DTensor *W2,
                    const DTensor &R, double dt, int max_iter, double tol, bool reverse, int precision,
-                   KrylovState *st_dev, std::vector<Flops> *per_iter) {
+                   KrylovState *st_dev, std::vector<Flops> *per_iter, int *iters_out) {
     check_precision(precision);
     KV_REQUIRE(max_iter >= 2 && max_iter <= kMaxKrylov, KV_EINVAL, "max_iter must be in [2, 32]");
     KV_REQUIRE(tol < 1.0, KV_EINVAL, "Krylov tolerance must be < 1");
@@ -605,26 +683,45 @@ TensorP op_lanczos(int nsite, const DTensor &L, const DTensor &psi, const DTenso
     const HeffPlan &H = *Hp;
     HeffWork w(H);
     if (per_iter) *per_iter = H.iter_flops;
+    // v_j lives on the first nl[j] elements of the layout; the vectors are packed
+    KrylovLens nl{};
+    for (int j = 0; j <= kMaxKrylov; ++j) nl.n[j] = H.prefix[std::min(j, H.napply)];
     const int64_t n = H.klayout.nelem;
     const int nvec = max_iter;  // V_0 .. V_{max_iter-1}
-    DevBuf Vbuf(std::max<int64_t>(1, n) * nvec * sizeof(double2));
+    std::vector<int64_t> voff(nvec + 1, 0);
+    for (int j = 0; j < nvec; ++j) voff[j + 1] = voff[j] + nl.n[j];
+    DevBuf Vbuf(std::max<int64_t>(1, voff[nvec]) * sizeof(double2));
     DevBuf hv(std::max<int64_t>(1, n) * sizeof(double2));
     DevBuf parts(2 * reduce_parts() * sizeof(double2));
-    DevBuf tmp(std::max<int64_t>(1, n) * sizeof(double2));
     double2 *V = Vbuf.as<double2>();
-    scatter_into(psi, H.klayout, tmp.as<double2>());
-    krylov_start(st_dev, tmp.as<double2>(), V, n, parts.as<double2>());
+    // psi's blocks are the layout's first blocks at the same offsets (both laid out in block order)
+    KV_REQUIRE(psi.meta.nelem == nl.n[0], KV_EINVAL, "internal: Krylov layout does not start with psi");
+    krylov_start(st_dev, psi.data(), V, nl.n[0], parts.as<double2>());
     const int *skip = &st_dev->done;
     for (int k = 0; k < max_iter - 1; ++k) {
-        run_heff(H, w, L, V + (int64_t)k * n, W1, W2, R, hv.as<double2>(), dt * 0.5, precision, skip, st_dev, k);
-        krylov_step(st_dev, k, hv.as<double2>(), k > 0 ? V + (int64_t)(k - 1) * n : nullptr, V + (int64_t)k * n,
-                    V + (int64_t)(k + 1) * n, n, parts.as<double2>(), tol, max_iter);
+        run_heff(H, w, L, V + voff[k], W1, W2, R, hv.as<double2>(), dt * 0.5, precision, skip, st_dev, k);
+        krylov_step(st_dev, k, hv.as<double2>(), k > 0 ? V + voff[k - 1] : nullptr, V + voff[k], V + voff[k + 1], nl,
+                    parts.as<double2>(), tol, max_iter);
     }
     std::vector<double2 *> ptrs(nvec);
-    for (int i = 0; i < nvec; ++i) ptrs[i] = V + (int64_t)i * n;
+    for (int i = 0; i < nvec; ++i) ptrs[i] = V + voff[i];
     DevBuf dptrs = upload_vec(ptrs);
     auto out = DTensor::make(H.klayout, false);
-    krylov_finish(st_dev, dptrs.as<double2 *>(), out->data(), n, reverse ? 1 : 0);
+    krylov_finish(st_dev, dptrs.as<double2 *>(), out->data(), nl, reverse ? 1 : 0);
+    // the result carries the blocks of v_0 .. v_{iters-1}, as the reference's
+    // sum of Krylov vectors does: a prefix of the layout
+    KrylovState h;
+    KV_CUDA(cudaMemcpyAsync(&h, st_dev, sizeof(h), cudaMemcpyDeviceToHost, ctx().stream));
+    KV_CUDA(cudaStreamSynchronize(ctx().stream));
+    KV_REQUIRE(h.status == KV_OK, h.status, "non-finite norm in the Lanczos recurrence");
+    KV_REQUIRE(h.iters >= 1 && h.iters <= max_iter, KV_EINVAL, "internal: Krylov dimension out of range");
+    const int64_t keep = nl.n[h.iters - 1];
+    size_t nb = 0;
+    while (nb < out->meta.blocks.size() && out->meta.blocks[nb].off < keep) ++nb;
+    out->meta.blocks.resize(nb);
+    out->meta.layout();
+    KV_REQUIRE(out->meta.nelem == keep, KV_EINVAL, "internal: Krylov prefix is not block aligned");
+    if (iters_out) *iters_out = h.iters;
     return out;
 }
 

@@ -23,6 +23,7 @@ struct ProductPlan {
     Meta out;
     GemmPlan gemm;
     std::vector<std::vector<GemmSeg>> per_out;  // segments per output block
+    std::vector<std::vector<std::pair<int, int>>> pairs;  // (A block, B block) of each segment
     std::vector<std::pair<int, int>> mn;        // (M, N) per output block
 };
 
@@ -31,6 +32,8 @@ struct MixPlanFull {
     std::vector<double> mult;  // reference blocks (matched pairs) merged into each output block
     MixPlan mix;
     double ref_flops = 0.0;
+    std::vector<int> term_in;        // input block of each term (aligned with mix.terms)
+    std::vector<double> term_coef;   // its reference flops per matched input block
 };
 
 struct HeffPlan {
@@ -39,6 +42,10 @@ struct HeffPlan {
     ProductPlan p1, p2;
     MixPlanFull m1, m2;
     std::vector<Flops> iter_flops;  // reference flops of the apply at Lanczos iteration k
+    // elements of the layout prefix holding the blocks reached within j
+    // applications (j = 0 .. napply; later iterations keep the last)
+    std::vector<int64_t> prefix;
+    int napply = 1;
 };
 
 struct SvdOut {
@@ -64,7 +71,7 @@ TensorP op_heff(int nsite, const DTensor &L, const DTensor &psi, const DTensor *
                 const DTensor &R, double scale, int precision);
 TensorP op_lanczos(int nsite, const DTensor &L, const DTensor &psi, const DTensor *W1, const DTensor *W2,
                    const DTensor &R, double dt, int max_iter, double tol, bool reverse, int precision,
-                   KrylovState *st_dev, std::vector<Flops> *per_iter);
+                   KrylovState *st_dev, std::vector<Flops> *per_iter, int *iters_out = nullptr);
 SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int precision);
 TensorP op_env(bool l2r, const DTensor &env, const DTensor &A, const DTensor &W, const DTensor *Wt, int precision,
                Flops *fl);

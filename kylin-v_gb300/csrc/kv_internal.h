@@ -186,7 +186,7 @@ struct GemmSeg {
     int K, lda, ldb;
     int opa;  // 0: A[m*lda + k]; 1: conj(A[k*lda + m]); 2: A[k*lda + m]; 3: conj(A[m*lda + k])
     int opb;  // 0: B[k*ldb + n]; 1: B[n*ldb + k]; 2: conj(B[n*ldb + k]); 3: conj(B[k*ldb + n])
-              // (the tensor-core kernel implements opa, opb in {0, 1})
+    int entry = 0;  // Lanczos step from which this block pair is nonzero (launches skip it before)
 };
 struct GemmTile {
     int64_t c_off;
@@ -204,12 +204,13 @@ struct SliceJob {
     int rows, K, ld;
     int trans;  // 0: (row, k) at src[row*ld + k]; 1: at src[k*ld + row]
     int conj;   // negate the imaginary part
-    int exp_off, nkc, pad;
+    int exp_off, nkc;
+    int entry;  // first step at which a segment reading this block is active
 };
 // Tensor-core path: a segment's sliced A and B blocks.
 struct SegX {
     int64_t a_pan, b_pan;
-    int nkc, a_exp, b_exp, pad;
+    int nkc, a_exp, b_exp, entry;
 };
 
 struct GemmPlan;
@@ -222,6 +223,9 @@ struct GemmPlan {
     double ref_flops = 0.0;  // sum of 8*M*N*K over the reference's zgemm pairs
     int max_k = 0;
     int tile_m = 0, tile_n = 0;
+    // tiles whose segments are all inactive at the launch's step write zeros
+    // (false: they write nothing; for intermediates only read by active consumers)
+    bool write_inactive = true;
     // tensor-core path only
     std::vector<SliceJob> ajobs, bjobs;
     std::vector<SegX> xsegs;
@@ -238,7 +242,8 @@ struct GemmPlan {
 // MPO mixing (env_mps_mpo family) with merging of equal output blocks.
 struct MixTerm {
     int64_t in_off, w_off;
-    int K;  // contracted extent (w_l sector dim * sigma dim)
+    int K;          // contracted extent (w_l sector dim * sigma dim)
+    int entry = 0;  // Lanczos step from which the input block is nonzero
 };
 struct MixJob {
     int64_t out_off, count;    // output block and its element count
@@ -254,20 +259,27 @@ struct MixPlan {
     std::vector<MixJob> jobs;
     std::vector<MixItem> items;
     DevBuf d_terms, d_jobs, d_items;
+    bool write_inactive = true;  // as GemmPlan::write_inactive, per output block
     void upload() { d_terms = upload_vec(terms); d_jobs = upload_vec(jobs); d_items = upload_vec(items); }
 };
 
+// Launch step meaning "every segment / term is active".
+constexpr int kAllSteps = 1 << 30;
+
 // ------------------------------------------------------- kernel wrappers
+// step: block pairs (and mixing terms) with entry > step are skipped
 void launch_gemm_fp64(const GemmPlan &p, const double2 *A, const double2 *B, double2 *C, double alpha,
-                      const int *skip);
-// dispatch by precision; st/k identify a Lanczos apply for profiling
+                      const int *skip, int step = kAllSteps);
+// dispatch by precision; st/k identify a Lanczos apply for profiling and
+// its step (k >= 0: only block pairs with entry <= k are multiplied)
 void run_gemm(const GemmPlan &g, const double2 *A, const double2 *B, double2 *C, double alpha, int precision,
               const int *skip, const KrylovState *st = nullptr, int k = -1, double credit_flops = -1.0);
 void launch_gemm_mixed(const GemmPlan &p, const double2 *A, const double2 *B, double2 *C, double alpha,
-                       const int *skip);
+                       const int *skip, int step = kAllSteps);
 // KV_ETIMEOUT if a tensor-core kernel's bounded wait gave up since the last call
 int mixed_gemm_status();
-void launch_mix(const MixPlan &p, const double2 *in, const double2 *W, double2 *out, const int *skip);
+void launch_mix(const MixPlan &p, const double2 *in, const double2 *W, double2 *out, const int *skip,
+                int step = kAllSteps);
 void launch_permute(const double2 *in, double2 *out, const std::vector<int64_t> &desc, int nblocks);
 void launch_zero(double2 *p, int64_t n);
 void launch_copy(double2 *dst, const double2 *src, int64_t n);
@@ -290,12 +302,19 @@ struct KrylovState {
 int reduce_parts();  // number of partial sums used by the vector kernels
 // v0 = psi / |psi|; resets the state (err[0] = 1)
 void krylov_start(KrylovState *st, const double2 *psi, double2 *v0, int64_t n, double2 *parts);
+// Support of the Krylov vectors: v_j is zero beyond n[j] complex elements
+// (its blocks are a prefix of the layout, the blocks reached within j
+// applications of H_eff).
+struct KrylovLens {
+    int64_t n[kMaxKrylov + 1];
+};
 // after hv = (dt/2) H v_k: Gram-Schmidt against v_{k-1} (k > 0) and v_k,
-// norm, stop test, v_{k+1} = hv / |hv|
+// norm, stop test, v_{k+1} = hv / |hv|, each on the vectors' supports
 void krylov_step(KrylovState *st, int k, double2 *hv, const double2 *vprev, const double2 *vk, double2 *vnext,
-                 int64_t n, double2 *parts, double tol, int max_iter);
-// coefficients from the tridiagonal exponential, then out = sum_i c_i v_i
-void krylov_finish(KrylovState *st, double2 *const *dV, double2 *out, int64_t n, int reverse);
+                 const KrylovLens &nl, double2 *parts, double tol, int max_iter);
+// coefficients from the tridiagonal exponential, then out = sum_i c_i v_i on
+// the support of v_{iters-1}
+void krylov_finish(KrylovState *st, double2 *const *dV, double2 *out, const KrylovLens &nl, int reverse);
 // sum |x|^2 into a device double (deterministic)
 void vec_norm2(const double2 *x, int64_t n, double2 *parts, double *result);
 

@@ -26,15 +26,18 @@ __global__ void __launch_bounds__(256) k_gemm_fp64(const GemmTile *__restrict__ 
                                                    const GemmSeg *__restrict__ segs,
                                                    const double2 *__restrict__ A,
                                                    const double2 *__restrict__ B, double2 *__restrict__ C,
-                                                   double alpha, const int *skip) {
+                                                   double alpha, const int *skip, int step, int write_inactive) {
     if (skip && *skip) return;
     __shared__ double2 As[TK][TM + 1];
     __shared__ double2 Bs[TK][TN + 1];
     const GemmTile t = tiles[blockIdx.x];
     const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
     double2 acc[2][2] = {};
+    bool any = false;
     for (int s = t.seg_begin; s < t.seg_end; ++s) {
         const GemmSeg g = segs[s];
+        if (g.entry > step) continue;  // uniform over the CTA
+        any = true;
         const double2 *a = A + g.a_off;
         const double2 *b = B + g.b_off;
         for (int k0 = 0; k0 < g.K; k0 += TK) {
@@ -78,6 +81,7 @@ __global__ void __launch_bounds__(256) k_gemm_fp64(const GemmTile *__restrict__ 
             __syncthreads();
         }
     }
+    if (!any && !write_inactive) return;
 #pragma unroll
     for (int i = 0; i < 2; ++i)
 #pragma unroll
@@ -96,10 +100,15 @@ constexpr int MIX_CHUNK = 1024;
 __global__ void __launch_bounds__(256) k_mix(const MixItem *__restrict__ items, const MixJob *__restrict__ jobs,
                                              const MixTerm *__restrict__ terms, const double2 *__restrict__ in,
                                              const double2 *__restrict__ W, double2 *__restrict__ out,
-                                             const int *skip) {
+                                             const int *skip, int step, int write_inactive) {
     if (skip && *skip) return;
     const MixItem it = items[blockIdx.x];
     const MixJob jb = jobs[it.job];
+    if (!write_inactive) {
+        bool any = false;
+        for (int ti = jb.term_begin; ti < jb.term_end; ++ti) any = any || terms[ti].entry <= step;
+        if (!any) return;
+    }
     for (int j = threadIdx.x; j < MIX_CHUNK; j += blockDim.x) {
         int64_t e = it.start + j;
         if (e >= jb.count) break;
@@ -110,6 +119,7 @@ __global__ void __launch_bounds__(256) k_mix(const MixItem *__restrict__ items, 
         double2 acc = make_double2(0.0, 0.0);
         for (int ti = jb.term_begin; ti < jb.term_end; ++ti) {
             const MixTerm tm = terms[ti];
+            if (tm.entry > step) continue;
             const double2 *w = W + tm.w_off + (k2 * tm.K) * jb.wr + r;
             const double2 *x = in + tm.in_off + (k * tm.K) * jb.rest + n;
             for (int kk = 0; kk < tm.K; ++kk) cfma(acc, w[(int64_t)kk * jb.wr], x[(int64_t)kk * jb.rest]);
@@ -159,18 +169,19 @@ int grid_for(int64_t n, int threads) {
 }  // namespace
 
 void launch_gemm_fp64(const GemmPlan &p, const double2 *A, const double2 *B, double2 *C, double alpha,
-                      const int *skip) {
+                      const int *skip, int step) {
     if (p.tiles.empty()) return;
-    k_gemm_fp64<<<(unsigned)p.tiles.size(), 256, 0, ctx().stream>>>(p.d_tiles.as<GemmTile>(), p.d_segs.as<GemmSeg>(),
-                                                                     A, B, C, alpha, skip);
+    k_gemm_fp64<<<(unsigned)p.tiles.size(), 256, 0, ctx().stream>>>(
+        p.d_tiles.as<GemmTile>(), p.d_segs.as<GemmSeg>(), A, B, C, alpha, skip, step, p.write_inactive ? 1 : 0);
     counted();
     KV_CUDA(cudaGetLastError());
 }
 
-void launch_mix(const MixPlan &p, const double2 *in, const double2 *W, double2 *out, const int *skip) {
+void launch_mix(const MixPlan &p, const double2 *in, const double2 *W, double2 *out, const int *skip, int step) {
     if (p.items.empty()) return;
     k_mix<<<(unsigned)p.items.size(), 256, 0, ctx().stream>>>(p.d_items.as<MixItem>(), p.d_jobs.as<MixJob>(),
-                                                               p.d_terms.as<MixTerm>(), in, W, out, skip);
+                                                               p.d_terms.as<MixTerm>(), in, W, out, skip, step,
+                                                               p.write_inactive ? 1 : 0);
     counted();
     KV_CUDA(cudaGetLastError());
 }

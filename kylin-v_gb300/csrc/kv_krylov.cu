@@ -83,20 +83,24 @@ __global__ void __launch_bounds__(KT) k_dot_part(const KrylovState *st, const do
     if (threadIdx.x == 0) parts[blockIdx.x] = r;
 }
 
-// c = reduce(pin) (= overlap(v, hv) = <hv|v>);  hv -= c v;  pout[b] = sum conj(hv) w
-// (w == nullptr: pout[b] = sum |hv|^2).  slot receives c.
+// c = reduce(pin) (= overlap(v, hv) = <hv|v>);  hv -= c v on [0, n_sub) (v is
+// zero beyond);  pout[b] = sum_{i < n_dot} conj(hv) w  (w == nullptr: sum |hv|^2).
+// slot receives c.
 __global__ void __launch_bounds__(KT) k_sub(KrylovState *st, double2 *hv, const double2 *v, const double2 *w,
-                                            int64_t n, const double2 *pin, double2 *pout, int nparts,
-                                            double2 *slot) {
+                                            int64_t n_sub, int64_t n_dot, const double2 *pin, double2 *pout,
+                                            int nparts, double2 *slot) {
     if (st->done) return;
     const double2 c = reduce_partials(pin, nparts);
     if (blockIdx.x == 0 && threadIdx.x == 0) *slot = c;
     double2 s = make_double2(0.0, 0.0);
-    for (int64_t i = blockIdx.x * (int64_t)KT + threadIdx.x; i < n; i += (int64_t)gridDim.x * KT) {
-        double2 h = hv[i], x = v[i];
-        h.x -= c.x * x.x - c.y * x.y;
-        h.y -= c.x * x.y + c.y * x.x;
-        hv[i] = h;
+    for (int64_t i = blockIdx.x * (int64_t)KT + threadIdx.x; i < n_dot; i += (int64_t)gridDim.x * KT) {
+        double2 h = hv[i];
+        if (i < n_sub) {
+            const double2 x = v[i];
+            h.x -= c.x * x.x - c.y * x.y;
+            h.y -= c.x * x.y + c.y * x.x;
+            hv[i] = h;
+        }
         if (w) s = cadd(s, cdotc(h, w[i]));
         else s.x += h.x * h.x + h.y * h.y;
     }
@@ -238,11 +242,16 @@ __global__ void __launch_bounds__(32) k_tridiag_exp(KrylovState *st, int reverse
     }
 }
 
-__global__ void __launch_bounds__(KT) k_combine(const KrylovState *st, double2 *const *V, double2 *out, int64_t n) {
+// out = sum_{j < iters} c_j V_j on [0, nl[iters - 1]) (V_j is zero beyond nl[j])
+__global__ void __launch_bounds__(KT) k_combine(const KrylovState *st, double2 *const *V, double2 *out,
+                                                KrylovLens nl) {
     const int m = st->iters;
+    if (m <= 0) return;
+    const int64_t n = nl.n[m - 1];
     for (int64_t i = blockIdx.x * (int64_t)KT + threadIdx.x; i < n; i += (int64_t)gridDim.x * KT) {
         double2 acc = make_double2(0.0, 0.0);
         for (int j = 0; j < m; ++j) {
+            if (i >= nl.n[j]) continue;
             const double2 c = st->coef[j], v = V[j][i];
             acc.x += c.x * v.x - c.y * v.y;
             acc.y += c.x * v.y + c.y * v.x;
@@ -270,30 +279,31 @@ void krylov_start(KrylovState *st, const double2 *psi, double2 *v0, int64_t n, d
 }
 
 void krylov_step(KrylovState *st, int k, double2 *hv, const double2 *vprev, const double2 *vk, double2 *vnext,
-                 int64_t n, double2 *parts, double tol, int max_iter) {
+                 const KrylovLens &nl, double2 *parts, double tol, int max_iter) {
     const int np = reduce_parts();
     double2 *P0 = parts, *P1 = parts + np;
     cudaStream_t s = ctx().stream;
+    const int64_t n_prev = k > 0 ? nl.n[k - 1] : 0, n_k = nl.n[k], n_next = nl.n[k + 1];
     if (k > 0) {
-        k_dot_part<<<np, KT, 0, s>>>(st, hv, vprev, n, P0);
-    counted();
-        k_sub<<<np, KT, 0, s>>>(st, hv, vprev, vk, n, P0, P1, np, &st->beta[k - 1]);
-    counted();
+        k_dot_part<<<np, KT, 0, s>>>(st, hv, vprev, n_prev, P0);
+        counted();
+        k_sub<<<np, KT, 0, s>>>(st, hv, vprev, vk, n_prev, n_k, P0, P1, np, &st->beta[k - 1]);
+        counted();
     } else {
-        k_dot_part<<<np, KT, 0, s>>>(st, hv, vk, n, P1);
-    counted();
+        k_dot_part<<<np, KT, 0, s>>>(st, hv, vk, n_k, P1);
+        counted();
     }
-    k_sub<<<np, KT, 0, s>>>(st, hv, vk, nullptr, n, P1, P0, np, &st->alpha[k]);
+    k_sub<<<np, KT, 0, s>>>(st, hv, vk, nullptr, n_k, n_next, P1, P0, np, &st->alpha[k]);
     counted();
-    k_normalize<<<np, KT, 0, s>>>(st, hv, vnext, n, P0, np, k, tol, max_iter);
+    k_normalize<<<np, KT, 0, s>>>(st, hv, vnext, n_next, P0, np, k, tol, max_iter);
     counted();
     KV_CUDA(cudaGetLastError());
 }
 
-void krylov_finish(KrylovState *st, double2 *const *dV, double2 *out, int64_t n, int reverse) {
+void krylov_finish(KrylovState *st, double2 *const *dV, double2 *out, const KrylovLens &nl, int reverse) {
     k_tridiag_exp<<<1, 32, 0, ctx().stream>>>(st, reverse);
     counted();
-    k_combine<<<reduce_parts(), KT, 0, ctx().stream>>>(st, dV, out, n);
+    k_combine<<<reduce_parts(), KT, 0, ctx().stream>>>(st, dV, out, nl);
     counted();
     KV_CUDA(cudaGetLastError());
 }

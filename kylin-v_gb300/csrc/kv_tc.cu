@@ -117,10 +117,11 @@ __device__ __forceinline__ __half2 digits2(int d0, int d1) {
 template <int TR>
 __global__ void __launch_bounds__(256) k_slice(const SliceJob *__restrict__ jobs, const int2 *__restrict__ items,
                                                const double2 *__restrict__ src, __half *__restrict__ dst,
-                                               int *__restrict__ exps, double alpha, const int *skip) {
+                                               int *__restrict__ exps, double alpha, const int *skip, int step) {
     if (skip && *skip) return;
     const int2 it = items[blockIdx.x];
     const SliceJob j = jobs[it.x];
+    if (j.entry > step) return;  // no active segment reads this block
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int r = it.y + warp;
     const int prow = ((j.rows + TR - 1) / TR) * TR;
@@ -290,8 +291,15 @@ __device__ __forceinline__ long long combine(const float *p) {
 __global__ void __launch_bounds__(192, 1) k_gemm_tc(const GemmTile *__restrict__ tiles, const SegX *__restrict__ segs,
                                                     const __half *__restrict__ Apl, const __half *__restrict__ Bpl,
                                                     const int *__restrict__ Aexp, const int *__restrict__ Bexp,
-                                                    double2 *__restrict__ C, const int *skip, int *err) {
+                                                    double2 *__restrict__ C, const int *skip, int *err, int step,
+                                                    int write_inactive) {
     if (skip && *skip) return;
+    {  // tiles without an active segment at this step: zeros, or nothing for intermediates
+        const GemmTile t0 = tiles[blockIdx.x];
+        bool any = false;
+        for (int s = t0.seg_begin; s < t0.seg_end && !any; ++s) any = segs[s].entry <= step;
+        if (!any && !write_inactive) return;
+    }
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t *sA = smem;
@@ -334,6 +342,7 @@ __global__ void __launch_bounds__(192, 1) k_gemm_tc(const GemmTile *__restrict__
             bool ok = true;
             for (int s = t.seg_begin; s < t.seg_end && ok; ++s) {
                 const SegX g = segs[s];
+                if (g.entry > step) continue;
                 const __half *ap = Apl + g.a_pan + (int64_t)rt * g.nkc * A_PANEL;
                 const __half *bp = Bpl + g.b_pan + (int64_t)nt * g.nkc * B_PANEL;
                 for (int kc = 0; kc < g.nkc; ++kc, ++it) {
@@ -357,6 +366,7 @@ __global__ void __launch_bounds__(192, 1) k_gemm_tc(const GemmTile *__restrict__
             int it = 0, grp = 0;
             bool ok = true;
             for (int s = t.seg_begin; s < t.seg_end && ok; ++s) {
+                if (segs[s].entry > step) continue;
                 const int nkc = segs[s].nkc;
                 for (int kc0 = 0; kc0 < nkc && ok; kc0 += GKC, ++grp) {
                     // the epilogue has read the previous group's accumulators
@@ -401,10 +411,12 @@ __global__ void __launch_bounds__(192, 1) k_gemm_tc(const GemmTile *__restrict__
         const int m = q * 32 + lane;
         const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16);
         int erow = kZeroExp;
-        for (int s = t.seg_begin; s < t.seg_end; ++s) erow = max(erow, Aexp[segs[s].a_exp + t.m0 + m]);
+        for (int s = t.seg_begin; s < t.seg_end; ++s)
+            if (segs[s].entry <= step) erow = max(erow, Aexp[segs[s].a_exp + t.m0 + m]);
         if (warp == 2) {
             int ec = kZeroExp;
-            for (int s = t.seg_begin; s < t.seg_end; ++s) ec = max(ec, Bexp[segs[s].b_exp + t.n0 + lane]);
+            for (int s = t.seg_begin; s < t.seg_end; ++s)
+                if (segs[s].entry <= step) ec = max(ec, Bexp[segs[s].b_exp + t.n0 + lane]);
             s_ecol[lane] = ec;
         }
         epi_bar();  // the only barrier of the epilogue warps: reached by all four unconditionally
@@ -415,6 +427,7 @@ __global__ void __launch_bounds__(192, 1) k_gemm_tc(const GemmTile *__restrict__
         int grp = 0;
         for (int sl = 0; sl < nseg && ok; ++sl) {
             const SegX g = segs[t.seg_begin + sl];
+            if (g.entry > step) continue;
             const int *fcol = Bexp + g.b_exp + t.n0;
             const int shr = erow - Aexp[g.a_exp + t.m0 + m];
             for (int kc0 = 0; kc0 < g.nkc; kc0 += GKC, ++grp) {
@@ -507,6 +520,7 @@ void plan_mixed(GemmPlan &g) {
             j.conj = (sg.opa == 1 || sg.opa == 3) ? 1 : 0;
             j.exp_off = (int)g.a_exps;
             j.nkc = nkc;
+            j.entry = kAllSteps;
             const int nrt = (M + BM - 1) / BM;
             g.a_planes += (int64_t)nrt * nkc * A_PANEL;
             g.a_exps += (int64_t)nrt * BM;
@@ -525,6 +539,7 @@ void plan_mixed(GemmPlan &g) {
             j.conj = (sg.opb == 2 || sg.opb == 3) ? 1 : 0;
             j.exp_off = (int)g.b_exps;
             j.nkc = nkc;
+            j.entry = kAllSteps;
             const int nnt = (N + BN - 1) / BN;
             g.b_planes += (int64_t)nnt * nkc * B_PANEL;
             g.b_exps += (int64_t)nnt * BN;
@@ -534,7 +549,9 @@ void plan_mixed(GemmPlan &g) {
         const SliceJob &ja = g.ajobs[ia->second], &jb = g.bjobs[ib->second];
         KV_REQUIRE(ja.rows == M && jb.rows == N && ja.K == sg.K && jb.K == sg.K, KV_EINVAL,
                    "internal: inconsistent block views in a mixed-precision plan");
-        g.xsegs[s] = SegX{ja.dst_off, jb.dst_off, nkc, ja.exp_off, jb.exp_off, 0};
+        g.xsegs[s] = SegX{ja.dst_off, jb.dst_off, nkc, ja.exp_off, jb.exp_off, sg.entry};
+        g.ajobs[ia->second].entry = std::min(g.ajobs[ia->second].entry, sg.entry);
+        g.bjobs[ib->second].entry = std::min(g.bjobs[ib->second].entry, sg.entry);
     }
     g.aitems.clear();
     g.bitems.clear();
@@ -551,7 +568,7 @@ void plan_mixed(GemmPlan &g) {
 }
 
 void launch_gemm_mixed(const GemmPlan &p, const double2 *A, const double2 *B, double2 *C, double alpha,
-                       const int *skip) {
+                       const int *skip, int step) {
     if (p.tiles.empty()) return;
     KV_REQUIRE(p.tile_m == BM && p.tile_n == BN && p.xsegs.size() == p.segs.size(), KV_EINVAL,
                "internal: GEMM plan not prepared for the tensor-core path");
@@ -567,19 +584,19 @@ void launch_gemm_mixed(const GemmPlan &p, const double2 *A, const double2 *B, do
     int n = 0;
     if (!p.aitems.empty()) {
         k_slice<BM><<<(unsigned)p.aitems.size(), 256, 0, c.stream>>>(p.d_ajobs.as<SliceJob>(), p.d_aitems.as<int2>(),
-                                                                     A, ap.as<__half>(), ae.as<int>(), 1.0, skip);
+                                                                     A, ap.as<__half>(), ae.as<int>(), 1.0, skip, step);
         KV_CUDA(cudaGetLastError());
         ++n;
     }
     if (!p.bitems.empty()) {
         k_slice<BN><<<(unsigned)p.bitems.size(), 256, 0, c.stream>>>(p.d_bjobs.as<SliceJob>(), p.d_bitems.as<int2>(),
-                                                                     B, bp.as<__half>(), be.as<int>(), alpha, skip);
+                                                                     B, bp.as<__half>(), be.as<int>(), alpha, skip, step);
         KV_CUDA(cudaGetLastError());
         ++n;
     }
     k_gemm_tc<<<(unsigned)p.tiles.size(), 192, SMEM_BYTES, c.stream>>>(
         p.d_tiles.as<GemmTile>(), p.d_xsegs.as<SegX>(), ap.as<__half>(), bp.as<__half>(), ae.as<int>(), be.as<int>(),
-        C, skip, g_err);
+        C, skip, g_err, step, p.write_inactive ? 1 : 0);
     KV_CUDA(cudaGetLastError());
     counted(n + 1);
     // the slices are freed stream-ordered after the GEMM

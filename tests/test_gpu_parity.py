@@ -64,6 +64,9 @@ def test_lanczos_expm(gpu, case, d):
     assert U.tensor_diff(k2.to_host(), rd("k2")) < 1e-12
     k0, _ = gpu.local_krylov(0, rd("envL_next"), rd("svd21_V"), None, None, R, 0.05, 11, 1e-8, reverse=True)
     assert U.tensor_diff(k0.to_host(), rd("k0")) < 1e-12
+    # the same blocks as the reference's sum of Krylov vectors (no more, no fewer)
+    for got, name in ((k1, "k1"), (k2, "k2"), (k0, "k0")):
+        assert set(got.to_host().as_dict()) == set(rd(name).as_dict()), name
     # the Krylov dimension equals the oracle's
     _, it_o = O.local_krylov(1, L, A, W, None, R, 0.05, 11, 1e-8)
     _, it_g = gpu.local_krylov(1, L, A, W, None, R, 0.05, 11, 1e-8)
@@ -127,3 +130,23 @@ def test_tdvp_trajectory(gpu, case, ti):
         assert np.abs(pops - ref[k][3:3 + len(dens)]).max() < 1e-9, k
         maxb = max(sum(x.to_host().legs()[2].values()) for x in s[:-1])
         assert maxb == int(ref[k][-1])
+
+
+@pytest.mark.parametrize("case", sorted(U.manifest()))
+def test_sweep_reference_flops(gpu, case):
+    """The flops a sweep credits (8*M*N*K over every zgemm the reference issues,
+    Lanczos iterations as actually run) equal the oracle's count of its own
+    zgemm calls for the same sweeps."""
+    O = U.load_oracle()
+    ch, mps, mpo, tr = _traj_case(case, 0)
+    stg = [int(x) for x in tr["stage"].strip("[]").split(",")]
+    mode = 2 if stg[1] else 1
+    t = gpu.TDVP(mps, mpo, tr["tol_svd"], 1e-8, tr["maxD"], 11, 0.05)
+    o = O.Tdvp(mps, mpo, tr["tol_svd"], 1e-8, tr["maxD"], 11, 0.05)
+    for _ in range(2):
+        O.flops(True)
+        o.sweep(mode)
+        of = O.flops(True)
+        t.two_site() if mode == 2 else t.one_site()
+        gf = t.stats()["ref_flops"]
+        assert of > 0 and abs(gf - of) <= 1e-9 * of, (gf, of)
