@@ -918,8 +918,8 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
     }
     // ---- mixed mode: FP64 polish.  The kept factor is rebuilt in FP64 from the
     // sector matrix and the FP32 singular vectors of the other side,
-    //   L->R: X = A_s V_k   R->L: X = A_s^H U_k,
-    // made orthonormal by shifted Cholesky-QR3, and the other factor is the
+    //   L->R: X = A_s V_k S_k^-1   R->L: X = A_s^H U_k S_k^-1,
+    // made orthonormal by Cholesky-QR2, and the other factor is the
     // exact projection (Y = X^H A_s, or A_s X).  With no truncation the
     // factorisation is exact to FP64 rounding; the FP32 error only enters the
     // choice of the discarded directions.
@@ -947,7 +947,7 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
     DevBuf Y(std::max<int64_t>(1, y_elems) * sizeof(double2)), Wb(std::max<int64_t>(1, w_elems) * sizeof(double2));
     DevBuf cst(std::max<size_t>(1, pol.size()) * sizeof(int)), cdiag(std::max<size_t>(1, pol.size()) * sizeof(double));
     KV_CUDA(cudaMemsetAsync(cst.p, 0, std::max<size_t>(1, pol.size()) * sizeof(int), ctx().stream));
-    svd_extract(dpol, (int)pol.size(), P, Us.as<float2>(), Wb.as<double2>());
+    svd_extract(dpol, (int)pol.size(), P, Us.as<float2>(), S.as<double>(), Wb.as<double2>());
     const int tm = kTileM(KV_FP64), tn = kTileN(KV_FP64);
     auto add_gemm = [&](GemmPlan &g, int64_t c_off, int M, int N, GemmSeg seg) {
         const int sb = (int)g.segs.size();
@@ -972,11 +972,11 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
     gram.upload();
     std::vector<int> item_pol, item_row0;
     for (size_t i = 0; i < pol.size(); ++i)
-        for (int r0 = 0; r0 < pol[i].rows; r0 += 64) { item_pol.push_back((int)i); item_row0.push_back(r0); }
-    // shifted CholeskyQR3: the columns of X have norms ~ s_j (condition up to
-    // ~1e5 at the floor); a shifted first pass keeps the factorisation defined,
-    // two plain passes restore FP64 orthonormality; the span never changes
-    for (int pass = 0; pass < 3; ++pass) {
+        for (int r0 = 0; r0 < pol[i].rows; r0 += kTrsmRows) { item_pol.push_back((int)i); item_row0.push_back(r0); }
+    // Cholesky-QR2: X = A_s W Sigma^-1 is orthonormal up to the FP32 error of
+    // W, so two passes give FP64 orthonormality (the first with a 1e-14
+    // relative shift to keep it defined); the span never changes
+    for (int pass = 0; pass < 2; ++pass) {
         launch_gemm_fp64(gram, X.as<double2>(), X.as<double2>(), Gm.as<double2>(), 1.0, nullptr);
         svd_chol(dpol, (int)pol.size(), Gm.as<double2>(), cst.as<int>(), cdiag.as<double>(), pass == 0 ? 1e-14 : 0.0);
         svd_trsm(dpol, item_pol, item_row0, Gm.as<double2>(), X.as<double2>());

@@ -116,10 +116,12 @@ __global__ void __launch_bounds__(NT) k_svd_jacobi(const SvdSector *__restrict__
 // Mixed mode: one-sided Jacobi in FP32 without accumulated rotations.  T is
 // oriented so that the singular vectors wanted afterwards are its own columns
 // (they converge to sigma_j w_j); T stays in shared memory when p*q <=
-// smem_elems.  Columns below 1e-7 of ||T||_F are numerically zero in FP32 and
-// are not rotated (this also lets wide T, q > p, converge: its q - p surplus
-// columns go to zero).
-template <int NT>
+// smem_elems.  Each column pair of a round is handled by a group of G lanes
+// (G = 16: two pairs per warp; a group's 16 consecutive rows are one full
+// pass over the shared-memory banks).  Columns below 1e-7 of ||T||_F are
+// numerically zero in FP32 and are not rotated (this also lets wide T, q > p,
+// converge: its q - p surplus columns go to zero).
+template <int NT, int G>
 __global__ void __launch_bounds__(NT) k_svd_jacobi_w(const SvdSector *__restrict__ secs, float2 *__restrict__ T,
                                                      int *status, int max_sweeps, float tol, int smem_elems) {
     extern __shared__ float2 sT[];
@@ -128,6 +130,8 @@ __global__ void __launch_bounds__(NT) k_svd_jacobi_w(const SvdSector *__restrict
     const SvdSector s = secs[blockIdx.x];
     const int p = s.p, q = s.q;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = NT / 32;
+    const int gl = threadIdx.x % G, grp = threadIdx.x / G, ngrp = NT / G;
+    const unsigned gmask = (G == 32) ? 0xFFFFFFFFu : (((1u << G) - 1u) << (lane & ~(G - 1)));
     float2 *g = T + s.t_off;
     const int64_t n = (int64_t)p * q;
     const bool in_smem = n <= smem_elems;
@@ -144,32 +148,41 @@ __global__ void __launch_bounds__(NT) k_svd_jacobi_w(const SvdSector *__restrict
     float tot = 0.f;
     for (int w = 0; w < nw; ++w) tot += red[w];
     const float zt = 1e-14f * tot;  // (1e-7 ||T||_F)^2
-    const int qe = q + (q & 1);
+    const int qe = q + (q & 1), m1 = qe - 1;
     int sweep = 0;
     bool converged = (q < 2);
     for (; sweep < max_sweeps && !converged; ++sweep) {
         if (threadIdx.x == 0) rotated = 0;
         __syncthreads();
-        for (int r = 0; r < qe - 1; ++r) {
-            for (int pi = warp; pi < qe / 2; pi += nw) {
-                int c0, c1;
-                kvj::tournament_pair(qe, r, pi, c0, c1);
-                if (c1 >= q) continue;
+        for (int r = 0; r < m1; ++r) {
+            for (int pi = grp; pi < qe / 2; pi += ngrp) {
+                // round-robin pairing (position 0 fixed, the rest rotate by r)
+                int c0 = 0, c1;
+                if (pi > 0) { c0 = pi - 1 + r; if (c0 >= m1) c0 -= m1; ++c0; }
+                c1 = qe - 2 - pi + r; if (c1 >= m1) c1 -= m1; ++c1;
+                if (c0 > c1) { const int x = c0; c0 = c1; c1 = x; }
+                if (c1 >= q) continue;  // uniform within the group
                 float2 *x = t + (int64_t)c0 * p, *y = t + (int64_t)c1 * p;
                 float a = 0, b = 0, cr = 0, ci = 0;
-                for (int i = lane; i < p; i += 32) {
+                for (int i = gl; i < p; i += G) {
                     const float2 xi = x[i], yi = y[i];
                     a += xi.x * xi.x + xi.y * xi.y;
                     b += yi.x * yi.x + yi.y * yi.y;
                     cr += xi.x * yi.x + xi.y * yi.y;
                     ci += xi.x * yi.y - xi.y * yi.x;
                 }
-                warp_sum3<float>(a, b, cr, ci);
+#pragma unroll
+                for (int o = G / 2; o > 0; o >>= 1) {
+                    a += __shfl_xor_sync(gmask, a, o, G);
+                    b += __shfl_xor_sync(gmask, b, o, G);
+                    cr += __shfl_xor_sync(gmask, cr, o, G);
+                    ci += __shfl_xor_sync(gmask, ci, o, G);
+                }
                 if (!(a > zt) || !(b > zt)) continue;
                 kvj::Rot<float> rot;
                 if (!kvj::make_rotation<float>(a, b, cr, ci, tol, rot)) continue;
-                if (lane == 0) rotated = 1;
-                for (int i = lane; i < p; i += 32) {
+                if (gl == 0) rotated = 1;
+                for (int i = gl; i < p; i += G) {
                     float2 xi = x[i], yi = y[i];
                     kvj::rotate_pair(rot, xi.x, xi.y, yi.x, yi.y);
                     x[i] = xi;
@@ -232,16 +245,20 @@ __global__ void k_to_f32(const double2 *__restrict__ in, float2 *__restrict__ ou
 
 // ------------------------------------------------------- FP64 polish
 // The first k sorted Jacobi columns (the kept singular vectors of the side
-// T's columns live in) as a row-major FP64 matrix W (p x k).
+// T's columns live in), each divided by its singular value, as a row-major
+// FP64 matrix W (p x k): A W then has columns of norm ~1 (a well-conditioned
+// start for Cholesky-QR).
 __global__ void k_svd_extract(const SvdPolish *__restrict__ pol, const SvdSector *__restrict__ secs,
-                              const float2 *__restrict__ Us, double2 *__restrict__ W) {
+                              const float2 *__restrict__ Us, const double *__restrict__ S, double2 *__restrict__ W) {
     const SvdPolish d = pol[blockIdx.x];
     const SvdSector s = secs[d.sector];
     const int k = d.k;
     for (int64_t e = threadIdx.x; e < (int64_t)s.p * k; e += blockDim.x) {
         const int i = (int)(e / k), j = (int)(e % k);
         const float2 v = Us[s.t_off + (int64_t)j * s.p + i];
-        W[d.w_off + e] = make_double2(v.x, v.y);
+        const double sj = S[s.s_off + j];
+        const double inv = sj > 0.0 ? 1.0 / sj : 1.0;
+        W[d.w_off + e] = make_double2(v.x * inv, v.y * inv);
     }
 }
 
@@ -407,7 +424,7 @@ void svd_jacobi_f32(const SvdPlan &p, const double2 *T64, float2 *T, int *status
         int optin = 0;
         KV_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx().device));
         smem_bytes = std::max(0, optin - 4096);
-        KV_CUDA(cudaFuncSetAttribute(k_svd_jacobi_w<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
+        KV_CUDA(cudaFuncSetAttribute(k_svd_jacobi_w<1024, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
     }
     int64_t max_pq = 0;
     for (auto &s : p.secs) max_pq = std::max<int64_t>(max_pq, (int64_t)s.p * s.q);
@@ -415,7 +432,7 @@ void svd_jacobi_f32(const SvdPlan &p, const double2 *T64, float2 *T, int *status
     const int elems = (int)std::min<int64_t>(max_pq, cap);
     k_to_f32<<<std::max(1, ctx().num_sms * 4), 256, 0, ctx().stream>>>(T64, T, p.t_elems);
     counted();
-    k_svd_jacobi_w<1024><<<(unsigned)p.secs.size(), 1024, (size_t)elems * sizeof(float2), ctx().stream>>>(
+    k_svd_jacobi_w<1024, 16><<<(unsigned)p.secs.size(), 1024, (size_t)elems * sizeof(float2), ctx().stream>>>(
         p.d_secs.as<SvdSector>(), T, status, max_sweeps, tol, elems);
     counted();
     KV_CUDA(cudaGetLastError());
@@ -429,9 +446,9 @@ void svd_finalize_f32(const SvdPlan &p, const float2 *T, float2 *Us, double *S) 
     KV_CUDA(cudaGetLastError());
 }
 
-void svd_extract(const DevBuf &pol, int npol, const SvdPlan &p, const float2 *Us, double2 *W) {
+void svd_extract(const DevBuf &pol, int npol, const SvdPlan &p, const float2 *Us, const double *S, double2 *W) {
     if (npol == 0) return;
-    k_svd_extract<<<npol, 256, 0, ctx().stream>>>(pol.as<SvdPolish>(), p.d_secs.as<SvdSector>(), Us, W);
+    k_svd_extract<<<npol, 256, 0, ctx().stream>>>(pol.as<SvdPolish>(), p.d_secs.as<SvdSector>(), Us, S, W);
     counted();
     KV_CUDA(cudaGetLastError());
 }
@@ -447,8 +464,8 @@ void svd_trsm(const DevBuf &pol, const std::vector<int> &item_pol, const std::ve
               const double2 *G, double2 *X) {
     if (item_pol.empty()) return;
     DevBuf ip = upload_vec(item_pol), ir = upload_vec(item_row0);
-    k_trsm_rows<<<(unsigned)item_pol.size(), 64, 0, ctx().stream>>>(pol.as<SvdPolish>(), ip.as<int>(), ir.as<int>(),
-                                                                    G, X);
+    k_trsm_rows<<<(unsigned)item_pol.size(), kTrsmRows, 0, ctx().stream>>>(pol.as<SvdPolish>(), ip.as<int>(),
+                                                                           ir.as<int>(), G, X);
     counted();
     KV_CUDA(cudaGetLastError());
 }
