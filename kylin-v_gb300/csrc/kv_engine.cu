@@ -63,18 +63,15 @@ void upload_bytes(void *dst, const void *src, size_t n) {
 
 void Meta::layout() {
     int64_t off = 0;
-    index.clear();
-    index.reserve(blocks.size() * 2);
-    for (size_t j = 0; j < blocks.size(); ++j) {
-        auto &b = blocks[j];
+    for (auto &b : blocks) {
         int64_t s = 1;
         for (int i = 0; i < rank; ++i) s *= b.shape[i];
         b.size = s;
         b.off = off;
         off += s;
-        index.emplace(leg_key(b, 0, rank), (int)j);
     }
     nelem = off;
+    rebuild_index();
 }
 
 TensorP DTensor::make(const Meta &m, bool zero) {
@@ -140,7 +137,7 @@ static int64_t prod_range(const BlockMeta &b, int lo, int hi) {
 // product<N1,N2,nc> planning, holstein/product.h:61-201: pairs match on equal
 // shape and charge of all nc contracted legs; output blocks are numbered by
 // first appearance of (shape, charges); every pair is one zgemm.
-ProductPlan plan_product(const Meta &A, const Meta &B, int nc, int opA, int opB) {
+ProductPlan plan_product(const Meta &A, const Meta &B, int nc, int opA, int opB, bool keys_only) {
     KV_REQUIRE(opA == KV_OP_N || opA == KV_OP_C, KV_EINVAL, "opA must be N or C");
     KV_REQUIRE(opB == KV_OP_N || opB == KV_OP_T, KV_EINVAL, "opB must be N or T");
     const int n1 = A.rank, n2 = B.rank, nr = n1 + n2 - 2 * nc;
@@ -161,19 +158,19 @@ ProductPlan plan_product(const Meta &A, const Meta &B, int nc, int opA, int opB)
     for (int ax = 0; ax < nc; ++ax)
         KV_REQUIRE(A.dirs[iax1 + ax] * f1 == -B.dirs[iax2 + ax], KV_EMISMATCH,
                    "contracted legs' directions mismatch");
-    std::vector<std::vector<GemmSeg>> per_out;
-    std::vector<std::pair<int, int>> mn;  // M, N per output block
-    // B blocks by (shape, charge) of their contracted legs, in block order
-    std::unordered_map<LegKey, std::vector<int>, LegKeyHash> bidx;
-    for (size_t j = 0; j < B.blocks.size(); ++j) bidx[leg_key(B.blocks[j], iax2, iax2 + nc)].push_back((int)j);
-    P.out.index.reserve(A.blocks.size() * 4);
+    // B blocks grouped by (shape, charge) of their contracted legs, in block order
+    LegIndex bidx;
+    bidx.build(B.blocks, iax2, iax2 + nc);
+    std::vector<GemmSeg> segs;
+    std::vector<std::pair<int, int>> pr;
+    std::vector<int> seg_out;
+    P.out.slots.reserve(4 * A.blocks.size());
     for (size_t i = 0; i < A.blocks.size(); ++i) {
         const BlockMeta &a = A.blocks[i];
-        LegKey ka = leg_key(a, iax1, iax1 + nc);
-        // leg_key packs legs from position 0, so keys of A's and B's contracted legs compare directly
-        auto it = bidx.find(ka);
-        if (it == bidx.end()) continue;
-        for (int j : it->second) {
+        const int grp = bidx.find(a, iax1);
+        if (grp < 0) continue;
+        for (int gi = bidx.start[grp]; gi < bidx.start[grp + 1]; ++gi) {
+            const int j = bidx.items[gi];
             const BlockMeta &b = B.blocks[j];
             BlockMeta o;
             int nrow = 1, ncol = 1;
@@ -192,11 +189,10 @@ ProductPlan plan_product(const Meta &A, const Meta &B, int nc, int opA, int opB)
             const int nk = (int)(prod_range(a, 0, n1) / nrow);
             const int before = (int)P.out.blocks.size();
             const int pos = P.out.add(o);
-            if (pos == before) {
-                per_out.emplace_back();
-                P.pairs.emplace_back();
-                mn.push_back({nrow, ncol});
-            }
+            if (pos == before) P.mn.push_back({nrow, ncol});
+            P.gemm.ref_flops += 8.0 * nrow * (double)ncol * nk;
+            P.gemm.max_k = std::max(P.gemm.max_k, nk);
+            if (keys_only) continue;
             GemmSeg sg;
             sg.a_off = a.off;
             sg.b_off = b.off;
@@ -205,15 +201,25 @@ ProductPlan plan_product(const Meta &A, const Meta &B, int nc, int opA, int opB)
             sg.opb = (opB == KV_OP_N) ? 0 : 1;
             sg.lda = (opA == KV_OP_N) ? nk : nrow;
             sg.ldb = (opB == KV_OP_N) ? ncol : nk;
-            per_out[pos].push_back(sg);
-            P.pairs[pos].push_back({(int)i, j});
-            P.gemm.ref_flops += 8.0 * nrow * (double)ncol * nk;
-            P.gemm.max_k = std::max(P.gemm.max_k, nk);
+            segs.push_back(sg);
+            pr.push_back({(int)i, j});
+            seg_out.push_back(pos);
         }
     }
     P.out.layout();
-    P.per_out = std::move(per_out);
-    P.mn = std::move(mn);
+    // segments grouped by output block, each group in discovery order
+    const size_t nout = P.out.blocks.size();
+    P.out_start.assign(nout + 1, 0);
+    for (int o : seg_out) ++P.out_start[o + 1];
+    for (size_t o = 0; o < nout; ++o) P.out_start[o + 1] += P.out_start[o];
+    P.segs.resize(segs.size());
+    P.pairs.resize(segs.size());
+    std::vector<int> fill(P.out_start.begin(), P.out_start.end() - 1);
+    for (size_t x = 0; x < segs.size(); ++x) {
+        const int at = fill[seg_out[x]]++;
+        P.segs[at] = segs[x];
+        P.pairs[at] = pr[x];
+    }
     return P;
 }
 
@@ -222,14 +228,12 @@ ProductPlan plan_product(const Meta &A, const Meta &B, int nc, int opA, int opB)
 void build_tiles(ProductPlan &P, const std::vector<int64_t> &target_off, int tile_m, int tile_n) {
     GemmPlan &g = P.gemm;
     g.tiles.clear();
-    g.segs.clear();
+    g.segs = P.segs;
     g.tile_m = tile_m;
     g.tile_n = tile_n;
-    for (size_t b = 0; b < P.per_out.size(); ++b) {
+    for (size_t b = 0; b + 1 < P.out_start.size(); ++b) {
         const int M = P.mn[b].first, N = P.mn[b].second;
-        const int sb = (int)g.segs.size();
-        for (auto &s : P.per_out[b]) g.segs.push_back(s);
-        const int se = (int)g.segs.size();
+        const int sb = P.out_start[b], se = P.out_start[b + 1];
         for (int m0 = 0; m0 < M; m0 += tile_m)
             for (int n0 = 0; n0 < N; n0 += tile_n) g.tiles.push_back({target_off[b], N, M, N, m0, n0, sb, se});
     }
@@ -253,21 +257,23 @@ double ref_product_flops(const Meta &A, const Meta &B, int nc, int opA, int opB,
     const int n1 = A.rank, n2 = B.rank;
     const int iax1 = (opA == KV_OP_N) ? n1 - nc : 0;
     const int iax2 = (opB == KV_OP_N) ? 0 : n2 - nc;
-    std::unordered_map<LegKey, double, LegKeyHash> bsum;  // sum of uncontracted sizes of B per key
+    LegIndex bidx;
+    bidx.build(B.blocks, iax2, iax2 + nc);
+    std::vector<double> bsum(bidx.rep.size(), 0.0);  // sum of uncontracted sizes of B per key
     for (size_t bi = 0; bi < B.blocks.size(); ++bi) {
         const BlockMeta &b = B.blocks[bi];
         int64_t sz = 1;
         for (int i = 0; i < n2; ++i) sz *= b.shape[i];
-        bsum[leg_key(b, iax2, iax2 + nc)] += (multB ? (*multB)[bi] : 1.0) * (double)(sz / prod_range(b, iax2, iax2 + nc));
+        bsum[bidx.find(b, iax2)] += (multB ? (*multB)[bi] : 1.0) * (double)(sz / prod_range(b, iax2, iax2 + nc));
     }
     double f = 0.0;
     for (size_t ai = 0; ai < A.blocks.size(); ++ai) {
         const BlockMeta &a = A.blocks[ai];
-        auto it = bsum.find(leg_key(a, iax1, iax1 + nc));
-        if (it == bsum.end()) continue;
+        const int g = bidx.find(a, iax1);
+        if (g < 0) continue;
         int64_t sz = 1;
         for (int i = 0; i < n1; ++i) sz *= a.shape[i];
-        f += (multA ? (*multA)[ai] : 1.0) * 8.0 * (double)sz * it->second;
+        f += (multA ? (*multA)[ai] : 1.0) * 8.0 * (double)sz * bsum[g];
     }
     return f;
 }
@@ -277,25 +283,28 @@ double ref_product_flops(const Meta &A, const Meta &B, int nc, int opA, int opB,
 // legs lead, lead+1 of lm (w_l, sigma) contract with legs 1, 2 of W; W's legs
 // 0, 3 (sigma', w_r) replace them.  Equal output blocks are merged here (the
 // reference keeps them apart and the following product<> sums them).
-MixPlanFull plan_mix(const Meta &lm, const Meta &W, int lead, const std::vector<double> *mult_in) {
+MixPlanFull plan_mix(const Meta &lm, const Meta &W, int lead, const std::vector<double> *mult_in, bool keys_only) {
     MixPlanFull R;
     R.out.rank = lm.rank;
     R.out.dirs = lm.dirs;
     R.out.dirs[lead] = W.dirs[0];
     R.out.dirs[lead + 1] = W.dirs[3];
-    std::vector<std::vector<MixTerm>> terms;
-    std::vector<std::vector<int>> tin;
-    std::vector<std::vector<double>> tco;
+    struct Flat {
+        int pos, in;
+        MixTerm term;
+        double coef;
+    };
+    std::vector<Flat> flat;
     std::vector<std::array<int, 3>> geo;  // so, wr, rest
-    std::unordered_map<LegKey, std::vector<int>, LegKeyHash> widx;
-    for (size_t j = 0; j < W.blocks.size(); ++j) widx[leg_key(W.blocks[j], 1, 3)].push_back((int)j);
+    LegIndex widx;
+    widx.build(W.blocks, 1, 3);
     for (size_t ai = 0; ai < lm.blocks.size(); ++ai) {
         const BlockMeta &a = lm.blocks[ai];
         const double mi = mult_in ? (*mult_in)[ai] : 1.0;
-        auto wit = widx.find(leg_key(a, lead, lead + 2));
-        if (wit == widx.end()) continue;
-        for (int wj : wit->second) {
-            const BlockMeta &w = W.blocks[wj];
+        const int grp = widx.find(a, lead);
+        if (grp < 0) continue;
+        for (int gi = widx.start[grp]; gi < widx.start[grp + 1]; ++gi) {
+            const BlockMeta &w = W.blocks[widx.items[gi]];
             BlockMeta o = a;
             o.shape[lead] = w.shape[0];
             o.qn[lead] = w.qn[0];
@@ -305,24 +314,36 @@ MixPlanFull plan_mix(const Meta &lm, const Meta &W, int lead, const std::vector<
             const int before = (int)R.out.blocks.size();
             const int pos = R.out.add(o);
             if (pos == before) {
-                terms.emplace_back();
-                tin.emplace_back();
-                tco.emplace_back();
                 geo.push_back({w.shape[0], w.shape[3], rest});
                 R.mult.push_back(0.0);
             }
             R.mult[pos] += mi;  // the reference keeps each matched pair as its own block
             const int K = a.shape[lead] * a.shape[lead + 1];
-            terms[pos].push_back({a.off, w.off, K});
             const double nk = (double)prod_range(a, 0, lead);
             const double coef = 8.0 * nk * w.shape[0] * (double)w.shape[3] * rest * K;
-            tin[pos].push_back((int)ai);
-            tco[pos].push_back(coef);
             R.ref_flops += mi * coef;
+            if (!keys_only) flat.push_back({pos, (int)ai, MixTerm{a.off, w.off, K}, coef});
         }
     }
     R.out.layout();
-    for (size_t b = 0; b < R.out.blocks.size(); ++b) {
+    if (keys_only) return R;
+    const size_t nout = R.out.blocks.size();
+    std::vector<int> start(nout + 1, 0);
+    for (auto &f : flat) ++start[f.pos + 1];
+    for (size_t b = 0; b < nout; ++b) start[b + 1] += start[b];
+    R.mix.terms.resize(flat.size());
+    R.term_in.resize(flat.size());
+    R.term_coef.resize(flat.size());
+    {
+        std::vector<int> fill(start.begin(), start.end() - 1);
+        for (auto &f : flat) {
+            const int at = fill[f.pos]++;
+            R.mix.terms[at] = f.term;
+            R.term_in[at] = f.in;
+            R.term_coef[at] = f.coef;
+        }
+    }
+    for (size_t b = 0; b < nout; ++b) {
         MixJob j;
         j.out_off = R.out.blocks[b].off;
         j.count = R.out.blocks[b].size;
@@ -330,13 +351,8 @@ MixPlanFull plan_mix(const Meta &lm, const Meta &W, int lead, const std::vector<
         j.so = geo[b][0];
         j.wr = geo[b][1];
         j.rest = geo[b][2];
-        j.term_begin = (int)R.mix.terms.size();
-        for (size_t x = 0; x < terms[b].size(); ++x) {
-            R.mix.terms.push_back(terms[b][x]);
-            R.term_in.push_back(tin[b][x]);
-            R.term_coef.push_back(tco[b][x]);
-        }
-        j.term_end = (int)R.mix.terms.size();
+        j.term_begin = start[b];
+        j.term_end = start[b + 1];
         const int job = (int)R.mix.jobs.size();
         R.mix.jobs.push_back(j);
         for (int64_t s = 0; s < j.count; s += 1024) R.mix.items.push_back({job, s});
@@ -433,10 +449,10 @@ HeffPlan plan_heff(int nsite, const Meta &L, const Meta &psi, const Meta *W1, co
     Meta fresh = psi;  // blocks whose images under H_eff are not yet in K
     fresh.layout();
     for (int reached = 1; reached <= H.napply && !fresh.blocks.empty(); ++reached) {
-        Meta last = plan_product(L, fresh, 1, KV_OP_N, KV_OP_N).out;
-        if (nsite >= 1) last = plan_mix(last, *W1, 1).out;
-        if (nsite == 2) last = plan_mix(last, *W2, 2).out;
-        const Meta out = plan_product(last, R, 2, KV_OP_N, KV_OP_T).out;
+        Meta last = plan_product(L, fresh, 1, KV_OP_N, KV_OP_N, true).out;
+        if (nsite >= 1) last = plan_mix(last, *W1, 1, nullptr, true).out;
+        if (nsite == 2) last = plan_mix(last, *W2, 2, nullptr, true).out;
+        const Meta out = plan_product(last, R, 2, KV_OP_N, KV_OP_T, true).out;
         Meta next;
         next.rank = K.rank;
         next.dirs = K.dirs;
@@ -461,10 +477,10 @@ HeffPlan plan_heff(int nsite, const Meta &L, const Meta &psi, const Meta *W1, co
     Kin.layout();
     H.p1 = plan_product(L, Kin, 1, KV_OP_N, KV_OP_N);
     std::vector<int> e_last(H.p1.out.blocks.size(), kAllSteps);
-    for (size_t b = 0; b < H.p1.per_out.size(); ++b)
-        for (size_t x = 0; x < H.p1.per_out[b].size(); ++x) {
-            const int e = entry[H.p1.pairs[b][x].second];
-            H.p1.per_out[b][x].entry = e;
+    for (size_t b = 0; b < H.p1.out.blocks.size(); ++b)
+        for (int x = H.p1.out_start[b]; x < H.p1.out_start[b + 1]; ++x) {
+            const int e = entry[H.p1.pairs[x].second];
+            H.p1.segs[x].entry = e;
             e_last[b] = std::min(e_last[b], e);
         }
     // a mixing term is live from its input block's entry; an output block from its first live term
@@ -490,18 +506,17 @@ HeffPlan plan_heff(int nsite, const Meta &L, const Meta &psi, const Meta *W1, co
         last = &H.m2.out;
     }
     H.p2 = plan_product(*last, R, 2, KV_OP_N, KV_OP_T);
-    for (size_t b = 0; b < H.p2.per_out.size(); ++b)
-        for (size_t x = 0; x < H.p2.per_out[b].size(); ++x) H.p2.per_out[b][x].entry = e_last[H.p2.pairs[b][x].first];
+    for (size_t x = 0; x < H.p2.segs.size(); ++x) H.p2.segs[x].entry = e_last[H.p2.pairs[x].first];
     // reference flops of iteration k: the pairs and terms live at k, MPO-mixing
     // outputs counted once per matched reference block (the reference does not
     // merge them, holstein/product.h:203-477)
     for (int k = 0; k < max_iter; ++k) {
         Flops f;
         std::vector<double> mult(H.p1.out.blocks.size(), 0.0);
-        for (size_t b = 0; b < H.p1.per_out.size(); ++b)
-            for (auto &sg : H.p1.per_out[b])
-                if (sg.entry <= k) {
-                    f.gemm += 8.0 * H.p1.mn[b].first * (double)H.p1.mn[b].second * sg.K;
+        for (size_t b = 0; b < H.p1.out.blocks.size(); ++b)
+            for (int x = H.p1.out_start[b]; x < H.p1.out_start[b + 1]; ++x)
+                if (H.p1.segs[x].entry <= k) {
+                    f.gemm += 8.0 * H.p1.mn[b].first * (double)H.p1.mn[b].second * H.p1.segs[x].K;
                     mult[b] = 1.0;
                 }
         for (MixPlanFull *m : {nsite >= 1 ? &H.m1 : nullptr, nsite == 2 ? &H.m2 : nullptr}) {
@@ -516,11 +531,11 @@ HeffPlan plan_heff(int nsite, const Meta &L, const Meta &psi, const Meta *W1, co
                     }
             mult = std::move(mo);
         }
-        for (size_t b = 0; b < H.p2.per_out.size(); ++b)
-            for (size_t x = 0; x < H.p2.per_out[b].size(); ++x) {
-                const GemmSeg &sg = H.p2.per_out[b][x];
+        for (size_t b = 0; b < H.p2.out.blocks.size(); ++b)
+            for (int x = H.p2.out_start[b]; x < H.p2.out_start[b + 1]; ++x) {
+                const GemmSeg &sg = H.p2.segs[x];
                 if (sg.entry <= k)
-                    f.gemm += mult[H.p2.pairs[b][x].first] * 8.0 * H.p2.mn[b].first * (double)H.p2.mn[b].second * sg.K;
+                    f.gemm += mult[H.p2.pairs[x].first] * 8.0 * H.p2.mn[b].first * (double)H.p2.mn[b].second * sg.K;
             }
         H.iter_flops.push_back(f);
     }
@@ -971,6 +986,8 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
     for (auto &pl : pol) add_gemm(gram, pl.g_off, pl.k, pl.k, GemmSeg{pl.x_off, pl.x_off, pl.rows, pl.k, pl.k, 1, 0});
     gram.upload();
     std::vector<int> item_pol, item_row0;
+    int kmax = 1;
+    for (auto &pl : pol) kmax = std::max(kmax, pl.k);
     for (size_t i = 0; i < pol.size(); ++i)
         for (int r0 = 0; r0 < pol[i].rows; r0 += kTrsmRows) { item_pol.push_back((int)i); item_row0.push_back(r0); }
     // Cholesky-QR2: X = A_s W Sigma^-1 is orthonormal up to the FP32 error of
@@ -979,7 +996,7 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
     for (int pass = 0; pass < 2; ++pass) {
         launch_gemm_fp64(gram, X.as<double2>(), X.as<double2>(), Gm.as<double2>(), 1.0, nullptr);
         svd_chol(dpol, (int)pol.size(), Gm.as<double2>(), cst.as<int>(), cdiag.as<double>(), pass == 0 ? 1e-14 : 0.0);
-        svd_trsm(dpol, item_pol, item_row0, Gm.as<double2>(), X.as<double2>());
+        svd_trsm(dpol, item_pol, item_row0, Gm.as<double2>(), X.as<double2>(), kmax);
     }
     GemmPlan proj;
     for (auto &pl : pol) {

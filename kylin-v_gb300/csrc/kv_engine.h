@@ -22,9 +22,11 @@ struct Flops {
 struct ProductPlan {
     Meta out;
     GemmPlan gemm;
-    std::vector<std::vector<GemmSeg>> per_out;  // segments per output block
-    std::vector<std::vector<std::pair<int, int>>> pairs;  // (A block, B block) of each segment
-    std::vector<std::pair<int, int>> mn;        // (M, N) per output block
+    // segments grouped by output block: block b owns segs[out_start[b] .. out_start[b+1])
+    std::vector<GemmSeg> segs;
+    std::vector<std::pair<int, int>> pairs;  // (A block, B block) of each segment
+    std::vector<int> out_start;
+    std::vector<std::pair<int, int>> mn;     // (M, N) per output block
 };
 
 struct MixPlanFull {
@@ -54,9 +56,11 @@ struct SvdOut {
     std::vector<double> kept_s;
 };
 
-ProductPlan plan_product(const Meta &A, const Meta &B, int nc, int opA, int opB);
+// keys_only: the output structure (and reference flops) without segment lists
+ProductPlan plan_product(const Meta &A, const Meta &B, int nc, int opA, int opB, bool keys_only = false);
 void build_tiles(ProductPlan &P, const std::vector<int64_t> &target_off, int tile_m, int tile_n);
-MixPlanFull plan_mix(const Meta &lm, const Meta &W, int lead, const std::vector<double> *mult_in = nullptr);
+MixPlanFull plan_mix(const Meta &lm, const Meta &W, int lead, const std::vector<double> *mult_in = nullptr,
+                     bool keys_only = false);
 double ref_product_flops(const Meta &A, const Meta &B, int nc, int opA, int opB, const std::vector<double> *multA,
                          const std::vector<double> *multB);
 HeffPlan plan_heff(int nsite, const Meta &L, const Meta &psi, const Meta *W1, const Meta *W2, const Meta &R,

@@ -115,40 +115,99 @@ struct BlockMeta {
     int64_t size = 0;  // complex elements
 };
 
-// Exact (shape, charge) key of some legs of a block, hashable.
-struct LegKey {
-    std::array<int, 2 * kMaxRank> v{};
-    bool operator==(const LegKey &o) const { return v == o.v; }
-};
-struct LegKeyHash {
-    size_t operator()(const LegKey &k) const {
-        uint64_t h = 1469598103934665603ull;
-        for (int x : k.v) { h ^= (uint64_t)(uint32_t)x; h *= 1099511628211ull; }
-        return (size_t)h;
+// (shape, charge) of legs [lo, hi) of a block: hash and equality.
+inline uint64_t legs_hash(const BlockMeta &b, int lo, int hi) {
+    uint64_t h = 0x9E3779B97F4A7C15ull ^ (uint64_t)(hi - lo);
+    for (int i = lo; i < hi; ++i) {
+        h ^= ((uint64_t)(uint32_t)b.shape[i] << 32) | (uint64_t)(uint32_t)b.qn[i];
+        h *= 0xBF58476D1CE4E5B9ull;
+        h ^= h >> 31;
+    }
+    return h;
+}
+inline bool legs_equal(const BlockMeta &a, int alo, const BlockMeta &b, int blo, int n) {
+    for (int i = 0; i < n; ++i)
+        if (a.shape[alo + i] != b.shape[blo + i] || a.qn[alo + i] != b.qn[blo + i]) return false;
+    return true;
+}
+
+// Blocks grouped by the (shape, charge) of legs [lo, hi), each group in block
+// order (open addressing over the groups, CSR lists of members).
+struct LegIndex {
+    const std::vector<BlockMeta> *blk = nullptr;
+    int lo = 0, n = 0;
+    std::vector<int> slot;   // group id or -1
+    std::vector<int> rep;    // first member of each group
+    std::vector<int> start;  // members of group g: items[start[g] .. start[g+1])
+    std::vector<int> items;
+    void build(const std::vector<BlockMeta> &blocks, int lo_, int hi_) {
+        blk = &blocks;
+        lo = lo_;
+        n = hi_ - lo_;
+        size_t cap = 16;
+        while (cap < 2 * blocks.size()) cap <<= 1;
+        slot.assign(cap, -1);
+        rep.clear();
+        std::vector<int> gid(blocks.size());
+        for (size_t j = 0; j < blocks.size(); ++j) {
+            size_t h = (size_t)legs_hash(blocks[j], lo, lo + n) & (cap - 1);
+            while (slot[h] >= 0 && !legs_equal(blocks[rep[slot[h]]], lo, blocks[j], lo, n)) h = (h + 1) & (cap - 1);
+            if (slot[h] < 0) {
+                slot[h] = (int)rep.size();
+                rep.push_back((int)j);
+            }
+            gid[j] = slot[h];
+        }
+        start.assign(rep.size() + 1, 0);
+        for (int g : gid) ++start[g + 1];
+        for (size_t g = 0; g < rep.size(); ++g) start[g + 1] += start[g];
+        items.resize(blocks.size());
+        std::vector<int> fill(start.begin(), start.end() - 1);
+        for (size_t j = 0; j < blocks.size(); ++j) items[fill[gid[j]]++] = (int)j;
+    }
+    // group whose key equals legs [xlo, xlo + n) of x, or -1
+    int find(const BlockMeta &x, int xlo) const {
+        const size_t cap = slot.size();
+        size_t h = (size_t)legs_hash(x, xlo, xlo + n) & (cap - 1);
+        while (slot[h] >= 0) {
+            if (legs_equal((*blk)[rep[slot[h]]], lo, x, xlo, n)) return slot[h];
+            h = (h + 1) & (cap - 1);
+        }
+        return -1;
     }
 };
-inline LegKey leg_key(const BlockMeta &b, int lo, int hi) {
-    LegKey k;
-    for (int i = lo; i < hi; ++i) { k.v[2 * (i - lo)] = b.shape[i]; k.v[2 * (i - lo) + 1] = b.qn[i]; }
-    return k;
-}
 
 struct Meta {
     int rank = 0;
     std::array<int, kMaxRank> dirs{};
     std::vector<BlockMeta> blocks;
     int64_t nelem = 0;
-    std::unordered_map<LegKey, int, LegKeyHash> index;  // full (shape, qn) key -> block
+    // open-addressing index of the full (shape, charge) key; valid while
+    // nindexed == blocks.size()
+    std::vector<int> slots;
+    size_t nindexed = 0;
     void layout();  // contiguous offsets in block order, rebuilds the index
-    bool same_key(const BlockMeta &a, const BlockMeta &b) const {
-        for (int i = 0; i < rank; ++i)
-            if (a.shape[i] != b.shape[i] || a.qn[i] != b.qn[i]) return false;
-        return true;
+    void rebuild_index() {
+        size_t cap = 16;
+        while (cap < 2 * blocks.size()) cap <<= 1;
+        slots.assign(cap, -1);
+        for (size_t j = 0; j < blocks.size(); ++j) {
+            size_t h = (size_t)legs_hash(blocks[j], 0, rank) & (cap - 1);
+            while (slots[h] >= 0) h = (h + 1) & (cap - 1);
+            slots[h] = (int)j;
+        }
+        nindexed = blocks.size();
     }
+    bool same_key(const BlockMeta &a, const BlockMeta &b) const { return legs_equal(a, 0, b, 0, rank); }
     int find(const BlockMeta &b) const {
-        if (index.size() == blocks.size()) {
-            auto it = index.find(leg_key(b, 0, rank));
-            return it == index.end() ? -1 : it->second;
+        if (nindexed == blocks.size() && !slots.empty()) {
+            const size_t cap = slots.size();
+            size_t h = (size_t)legs_hash(b, 0, rank) & (cap - 1);
+            while (slots[h] >= 0) {
+                if (same_key(blocks[slots[h]], b)) return slots[h];
+                h = (h + 1) & (cap - 1);
+            }
+            return -1;
         }
         for (size_t i = 0; i < blocks.size(); ++i)
             if (same_key(blocks[i], b)) return (int)i;
@@ -156,11 +215,19 @@ struct Meta {
     }
     // append b if its key is new; returns its index
     int add(const BlockMeta &b) {
-        LegKey k = leg_key(b, 0, rank);
-        auto it = index.find(k);
-        if (it != index.end()) return it->second;
+        if (nindexed != blocks.size() || slots.empty()) rebuild_index();
+        size_t cap = slots.size();
+        size_t h = (size_t)legs_hash(b, 0, rank) & (cap - 1);
+        while (slots[h] >= 0) {
+            if (same_key(blocks[slots[h]], b)) return slots[h];
+            h = (h + 1) & (cap - 1);
+        }
         blocks.push_back(b);
-        index.emplace(k, (int)blocks.size() - 1);
+        if (2 * blocks.size() > cap) rebuild_index();
+        else {
+            slots[h] = (int)blocks.size() - 1;
+            nindexed = blocks.size();
+        }
         return (int)blocks.size() - 1;
     }
 };

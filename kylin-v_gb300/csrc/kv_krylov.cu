@@ -133,116 +133,90 @@ __global__ void __launch_bounds__(KT) k_normalize(KrylovState *st, const double2
 
 // T = tridiag(Re alpha, beta upper); c = Z exp(img Lambda) Z^H e0 with
 // img = -i (forward) or +i (reverse): holstein/exponential.h:163-183.
-// One warp: cyclic two-sided complex Jacobi (the rotations of kv_jacobi.cuh),
-// lane 0 forms each rotation, the lanes update the two rows, the two columns
-// and the eigenvector columns in parallel.
+// The phases of the off-diagonal go into a diagonal unitary, T = P S P^H with
+// S real symmetric tridiagonal (off-diagonal |beta_k|, p_0 = 1,
+// p_{k+1} = p_k conj(beta_k)/|beta_k|), so c = P Z_S exp(img Lambda) Z_S^T e0.
+// S is diagonalised by implicit-shift QL (Wilkinson-type shift, Givens chase;
+// the textbook tridiagonal QL method).  One warp: every lane runs the same
+// scalar recurrence on its own copy of the diagonals, so no lane waits on
+// another, and lane k applies each rotation to row k of the eigenvector
+// matrix; the eigenvalues' phases and the sum over eigenvectors are
+// lane-parallel.  FP64 throughout.
 __global__ void __launch_bounds__(32) k_tridiag_exp(KrylovState *st, int reverse) {
-    __shared__ double2 H[kMaxKrylov][kMaxKrylov + 1];
-    __shared__ double2 Z[kMaxKrylov][kMaxKrylov + 1];
-    __shared__ double2 ph[kMaxKrylov];
-    __shared__ double rot[3];  // cs, s_re, s_im
-    __shared__ int any_rot;
     const int lane = threadIdx.x;
     const int n = st->iters;
     if (n <= 0) return;
-    for (int i = 0; i < n; ++i)
-        if (lane < n) {
-            double2 h = make_double2(0.0, 0.0);
-            if (i == lane) h.x = st->alpha[i].x;
-            else if (lane == i + 1) h = st->beta[i];                                  // upper (i, i+1)
-            else if (i == lane + 1) h = make_double2(st->beta[lane].x, -st->beta[lane].y);  // lower
-            H[i][lane] = h;
-            Z[i][lane] = make_double2(i == lane ? 1.0 : 0.0, 0.0);
-        }
-    __syncwarp();
-    // off-diagonal entries below 1e-15 ||T||_F are below FP64 resolution of
-    // the eigen-decomposition and are not rotated (quadratic convergence: a
-    // handful of sweeps)
-    double fro = 0.0;
+    double d[kMaxKrylov], e[kMaxKrylov], z[kMaxKrylov];
     for (int i = 0; i < n; ++i) {
-        const double2 h = lane < n ? H[i][lane] : make_double2(0.0, 0.0);
-        fro += h.x * h.x + h.y * h.y;
+        d[i] = st->alpha[i].x;
+        const double2 b = st->beta[i];
+        e[i] = (i + 1 < n) ? sqrt(b.x * b.x + b.y * b.y) : 0.0;
+        z[i] = (i == lane) ? 1.0 : 0.0;  // row `lane` of the eigenvector matrix
     }
-    for (int o = 16; o; o >>= 1) fro += __shfl_xor_sync(0xFFFFFFFFu, fro, o);
-    const double thr = 1e-15 * sqrt(fro);
-    for (int sweep = 0; sweep < 60; ++sweep) {
-        if (lane == 0) any_rot = 0;
-        __syncwarp();
-        for (int p = 0; p < n - 1; ++p)
-            for (int q = p + 1; q < n; ++q) {
-                if (lane == 0) {
-                    const double a = H[p][p].x, b = H[q][q].x;
-                    const double cr = H[p][q].x, ci = H[p][q].y;
-                    const double ac = sqrt(cr * cr + ci * ci);
-                    kvj::Rot<double> r;
-                    r.cs = 0.0;
-                    if (ac > 1e-300 && ac > thr) {
-                        const double z = (b - a) / (2.0 * ac);
-                        const double t = (z >= 0.0 ? 1.0 : -1.0) / (fabs(z) + sqrt(1.0 + z * z));
-                        r.cs = 1.0 / sqrt(1.0 + t * t);
-                        const double sn = t * r.cs;
-                        r.s_re = sn * cr / ac;
-                        r.s_im = sn * ci / ac;
-                        any_rot = 1;
-                    }
-                    rot[0] = r.cs;
-                    rot[1] = r.s_re;
-                    rot[2] = r.s_im;
+    const double eps = 2.220446049250313e-16;
+    for (int l = 0; l < n; ++l) {
+        for (int iter = 0; iter < 64; ++iter) {
+            int m = l;
+            for (; m < n - 1; ++m)
+                if (fabs(e[m]) <= eps * (fabs(d[m]) + fabs(d[m + 1]))) break;
+            if (m == l) break;
+            // shift from the leading 2x2 block: the eigenvalue of it closer to d[l]
+            double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+            double r = hypot(g, 1.0);
+            g = d[m] - d[l] + e[l] / (g + copysign(r, g));
+            double sn = 1.0, cs = 1.0, p = 0.0;
+            int i = m - 1;
+            for (; i >= l; --i) {
+                const double f = sn * e[i], b = cs * e[i];
+                r = hypot(f, g);
+                e[i + 1] = r;
+                if (r == 0.0) {  // split: the chase stops early
+                    d[i + 1] -= p;
+                    e[m] = 0.0;
+                    break;
                 }
-                __syncwarp();
-                kvj::Rot<double> r;
-                r.cs = rot[0];
-                r.s_re = rot[1];
-                r.s_im = rot[2];
-                __syncwarp();  // every lane has read rot before lane 0 writes the next one
-                if (r.cs == 0.0) continue;  // warp-uniform: no rotation for this pair
-                if (lane < n) {  // columns p, q  (H <- H J)
-                    double2 x = H[lane][p], y = H[lane][q];
-                    kvj::rotate_pair(r, x.x, x.y, y.x, y.y);
-                    H[lane][p] = x;
-                    H[lane][q] = y;
-                }
-                __syncwarp();
-                if (lane < n) {  // rows p, q  (H <- J^H H)
-                    double xr = H[p][lane].x, xi = -H[p][lane].y, yr = H[q][lane].x, yi = -H[q][lane].y;
-                    kvj::rotate_pair(r, xr, xi, yr, yi);
-                    H[p][lane] = make_double2(xr, -xi);
-                    H[q][lane] = make_double2(yr, -yi);
-                    double2 zx = Z[lane][p], zy = Z[lane][q];  // Z <- Z J
-                    kvj::rotate_pair(r, zx.x, zx.y, zy.x, zy.y);
-                    Z[lane][p] = zx;
-                    Z[lane][q] = zy;
-                }
-                __syncwarp();
-                if (lane == 0) {
-                    H[p][q] = H[q][p] = make_double2(0.0, 0.0);
-                    H[p][p].y = H[q][q].y = 0.0;
-                }
-                __syncwarp();
+                sn = f / r;
+                cs = g / r;
+                g = d[i + 1] - p;
+                r = (d[i] - g) * sn + 2.0 * cs * b;
+                p = sn * r;
+                d[i + 1] = g + p;
+                g = cs * r - b;
+                const double zf = z[i + 1];
+                z[i + 1] = sn * z[i] + cs * zf;
+                z[i] = cs * z[i] - sn * zf;
             }
-        __syncwarp();
-        if (!any_rot) break;
+            if (r == 0.0 && i >= l) continue;
+            d[l] -= p;
+            e[l] = g;
+            e[m] = 0.0;
+        }
+    }
+    // p_lane: product of the off-diagonal phases above this row
+    double pr = 1.0, pi = 0.0;
+    for (int k = 0; k < lane && k + 1 < n; ++k) {
+        const double2 b = st->beta[k];
+        const double ab = sqrt(b.x * b.x + b.y * b.y);
+        if (ab > 0.0) {
+            const double cr = b.x / ab, ci = -b.y / ab;  // conj(beta_k)/|beta_k|
+            const double t = pr * cr - pi * ci;
+            pi = pr * ci + pi * cr;
+            pr = t;
+        }
     }
     const double sg = reverse ? 1.0 : -1.0;
-    if (lane < n) {
-        const double lam = H[lane][lane].x;
-        ph[lane] = make_double2(cos(lam), sg * sin(lam));  // exp(img lambda)
+    double cr = 0.0, ci = 0.0;
+    for (int j = 0; j < n; ++j) {
+        const double z0 = __shfl_sync(0xFFFFFFFFu, z[j], 0);  // Z_S[0][j]
+        double sj, cj;
+        sincos(d[j], &sj, &cj);
+        const double w = z[j] * z0;
+        cr += w * cj;
+        ci += w * sg * sj;
     }
-    __syncwarp();
-    if (lane < n) {
-        double cr = 0.0, ci = 0.0;
-        for (int j = 0; j < n; ++j) {
-            const double2 z = Z[lane][j], e = ph[j];
-            const double z0r = Z[0][j].x, z0i = -Z[0][j].y;  // conj(Z[0, j])
-            const double pr = z.x * e.x - z.y * e.y, pi = z.x * e.y + z.y * e.x;
-            cr += pr * z0r - pi * z0i;
-            ci += pr * z0i + pi * z0r;
-        }
-        st->coef[lane] = make_double2(cr, ci);
-    }
+    if (lane < n) st->coef[lane] = make_double2(pr * cr - pi * ci, pr * ci + pi * cr);
 }
 
-// out = sum_{j < iters} c_j V_j on [0, nl[iters - 1]) (V_j is zero beyond nl[j])
 __global__ void __launch_bounds__(KT) k_combine(const KrylovState *st, double2 *const *V, double2 *out,
                                                 KrylovLens nl) {
     const int m = st->iters;

@@ -209,23 +209,24 @@ __global__ void __launch_bounds__(256) k_svd_finalize(const SvdSector *__restric
     using C = typename Cx<R>::T;
     const SvdSector s = secs[blockIdx.x];
     const int p = s.p, q = s.q;
-    extern __shared__ double sv[];  // q norms
+    extern __shared__ unsigned char sv_raw[];  // q norms, in the Jacobi's precision
+    R *sv = reinterpret_cast<R *>(sv_raw);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = 256 / 32;
     for (int j = warp; j < q; j += nw) {
-        double a = 0.0;
+        R a = 0;
         for (int i = lane; i < p; i += 32) {
             C x = T[s.t_off + (int64_t)j * p + i];
-            a += (double)x.x * x.x + (double)x.y * x.y;
+            a += x.x * x.x + x.y * x.y;
         }
         for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
         if (lane == 0) sv[j] = sqrt(a);
     }
     __syncthreads();
     for (int j = warp; j < q; j += nw) {
-        const double sj = sv[j];
+        const R sj = sv[j];
         int rank = 0;
         for (int i = 0; i < q; ++i) rank += (sv[i] > sj) || (sv[i] == sj && i < j);
-        const R inv = sj > 0.0 ? R(1.0 / sj) : R(0);
+        const R inv = sj > R(0) ? R(1) / sj : R(0);
         for (int i = lane; i < p; i += 32) {
             C x = T[s.t_off + (int64_t)j * p + i];
             x.x *= inv;
@@ -309,25 +310,41 @@ __global__ void k_chol(const SvdPolish *__restrict__ pol, double2 *__restrict__ 
     }
 }
 
-// X <- X R^{-1} row by row (R upper, from k_chol): y_c = (x_c - sum_{a<c} y_a R[a,c]) / R[c,c]
-__global__ void k_trsm_rows(const SvdPolish *__restrict__ pol, const int *__restrict__ item_pol,
-                            const int *__restrict__ item_row0, const double2 *__restrict__ G, double2 *__restrict__ X) {
+// X <- X R^{-1} row by row (R upper, from k_chol): y_c = (x_c - sum_{a<c} y_a R[a,c]) / R[c,c].
+// One warp per row (kTrsmRows rows per CTA): the solved y live in shared
+// memory, lanes split each inner sum, a shuffle tree reduces it.
+__global__ void __launch_bounds__(32 * kTrsmRows) k_trsm_rows(const SvdPolish *__restrict__ pol,
+                                                              const int *__restrict__ item_pol,
+                                                              const int *__restrict__ item_row0,
+                                                              const double2 *__restrict__ G, double2 *__restrict__ X) {
+    extern __shared__ double2 ys[];  // [kTrsmRows][kmax]
     const SvdPolish d = pol[item_pol[blockIdx.x]];
-    const int row = item_row0[blockIdx.x] + threadIdx.x;
-    if (row >= d.rows) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row = item_row0[blockIdx.x] + warp;
+    if (row >= d.rows) return;  // warp-uniform
     const int k = d.k;
     const double2 *r = G + d.g_off;
     double2 *x = X + d.x_off + (int64_t)row * k;
+    double2 *y = ys + (int64_t)warp * k;
     for (int c = 0; c < k; ++c) {
-        double2 v = x[c];
-        for (int a = 0; a < c; ++a) {
-            const double2 y = x[a], rac = r[(int64_t)a * k + c];
-            v.x -= y.x * rac.x - y.y * rac.y;
-            v.y -= y.x * rac.y + y.y * rac.x;
+        double sr = 0.0, si = 0.0;
+        for (int a = lane; a < c; a += 32) {
+            const double2 ya = y[a], rac = r[(int64_t)a * k + c];
+            sr += ya.x * rac.x - ya.y * rac.y;
+            si += ya.x * rac.y + ya.y * rac.x;
         }
-        const double inv = 1.0 / r[(int64_t)c * k + c].x;
-        x[c] = make_double2(v.x * inv, v.y * inv);
+        for (int o = 16; o > 0; o >>= 1) {
+            sr += __shfl_xor_sync(0xFFFFFFFFu, sr, o);
+            si += __shfl_xor_sync(0xFFFFFFFFu, si, o);
+        }
+        if (lane == 0) {
+            const double2 v = x[c];
+            const double inv = 1.0 / r[(int64_t)c * k + c].x;
+            y[c] = make_double2((v.x - sr) * inv, (v.y - si) * inv);
+        }
+        __syncwarp();
     }
+    for (int a = lane; a < k; a += 32) x[a] = y[a];
 }
 
 // output blocks from dense row-major factors: side 0 block[i, j] = M[(pos+i)*ld + j]
@@ -461,11 +478,18 @@ void svd_chol(const DevBuf &pol, int npol, double2 *G, int *status, double *diag
 }
 
 void svd_trsm(const DevBuf &pol, const std::vector<int> &item_pol, const std::vector<int> &item_row0,
-              const double2 *G, double2 *X) {
+              const double2 *G, double2 *X, int kmax) {
     if (item_pol.empty()) return;
+    const size_t smem = (size_t)kTrsmRows * std::max(1, kmax) * sizeof(double2);
+    KV_REQUIRE(smem <= 200 * 1024, KV_EINVAL, "SVD polish: kept dimension of one sector too large");
+    static size_t attr = 0;
+    if (smem > 48 * 1024 && smem > attr) {
+        KV_CUDA(cudaFuncSetAttribute(k_trsm_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr = smem;
+    }
     DevBuf ip = upload_vec(item_pol), ir = upload_vec(item_row0);
-    k_trsm_rows<<<(unsigned)item_pol.size(), kTrsmRows, 0, ctx().stream>>>(pol.as<SvdPolish>(), ip.as<int>(),
-                                                                           ir.as<int>(), G, X);
+    k_trsm_rows<<<(unsigned)item_pol.size(), 32 * kTrsmRows, smem, ctx().stream>>>(pol.as<SvdPolish>(), ip.as<int>(),
+                                                                                  ir.as<int>(), G, X);
     counted();
     KV_CUDA(cudaGetLastError());
 }

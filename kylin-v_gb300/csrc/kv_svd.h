@@ -54,11 +54,11 @@ void svd_gather(const SvdPlan &p, const double2 *A, double2 *T);
 void svd_jacobi_f32(const SvdPlan &p, const double2 *T64, float2 *T, int *status, int max_sweeps, float tol);
 void svd_finalize_f32(const SvdPlan &p, const float2 *T, float2 *Us, double *S);
 void svd_extract(const DevBuf &pol, int npol, const SvdPlan &p, const float2 *Us, const double *S, double2 *W);
-// rows of X per triangular-solve CTA (one thread per row; FP64 work spread over SMs)
-constexpr int kTrsmRows = 32;
+// rows of X per triangular-solve CTA (one warp per row)
+constexpr int kTrsmRows = 8;
 void svd_chol(const DevBuf &pol, int npol, double2 *G, int *status, double *diagv, double shift);
 void svd_trsm(const DevBuf &pol, const std::vector<int> &item_pol, const std::vector<int> &item_row0,
-              const double2 *G, double2 *X);
+              const double2 *G, double2 *X, int kmax);
 void svd_scatter_dense(const std::vector<SvdDense> &d, const double2 *M, double2 *out);
 void svd_jacobi(const SvdPlan &p, double2 *T, double2 *V, int *status, int max_sweeps, double tol);
 void svd_finalize(const SvdPlan &p, const double2 *T, const double2 *V, double2 *Us, double2 *Vs, double *S);

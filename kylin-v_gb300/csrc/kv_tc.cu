@@ -46,7 +46,7 @@
 
 #include <cstdint>
 #include <cstring>
-#include <map>
+#include <unordered_map>
 #include <utility>
 
 #include "kv_internal.h"
@@ -68,7 +68,7 @@ constexpr uint32_t TMEM_COLS = 512;            // NACC * BN = 480, rounded to a 
 constexpr int KDRAIN = 336;                    // K-steps accumulated exactly between drains
 constexpr int GKC = KDRAIN / BKC;              // K panels per drain group
 constexpr int FRAC = 29;
-constexpr int kZeroExp = -4000;                // exponent of an all-zero (or padding) row
+constexpr int kZeroExp = -4000;                // exponent of an all-zero row
 constexpr long long WAIT_LIMIT = 1ll << 22;
 constexpr int SMEM_BYTES = STAGES * (A_BYTES + B_BYTES) + 1024 + 512;
 
@@ -124,8 +124,9 @@ __global__ void __launch_bounds__(256) k_slice(const SliceJob *__restrict__ jobs
     if (j.entry > step) return;  // no active segment reads this block
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int r = it.y + warp;
-    const int prow = ((j.rows + TR - 1) / TR) * TR;
-    if (r >= prow) return;
+    // rows past the block (up to the panel's TR) are not written: they only
+    // reach output rows / columns the GEMM epilogue never stores
+    if (r >= j.rows) return;
     const int kpad = j.nkc * BKC;
     const double2 *s = src + j.src_off;
     const bool scale = alpha != 1.0;
@@ -136,13 +137,12 @@ __global__ void __launch_bounds__(256) k_slice(const SliceJob *__restrict__ jobs
         return v;
     };
     unsigned long long mx = 0;
-    if (r < j.rows)
-        for (int k = lane; k < j.K; k += 32) {
-            const double2 v = load(k);
-            const unsigned long long br = (unsigned long long)__double_as_longlong(v.x) & 0x7FFFFFFFFFFFFFFFull;
-            const unsigned long long bi = (unsigned long long)__double_as_longlong(v.y) & 0x7FFFFFFFFFFFFFFFull;
-            mx = max(mx, max(br, bi));
-        }
+    for (int k = lane; k < j.K; k += 32) {
+        const double2 v = load(k);
+        const unsigned long long br = (unsigned long long)__double_as_longlong(v.x) & 0x7FFFFFFFFFFFFFFFull;
+        const unsigned long long bi = (unsigned long long)__double_as_longlong(v.y) & 0x7FFFFFFFFFFFFFFFull;
+        mx = max(mx, max(br, bi));
+    }
 #pragma unroll
     for (int o = 16; o; o >>= 1) mx = max(mx, (unsigned long long)__shfl_xor_sync(0xFFFFFFFFu, mx, o));
     const int e = mx ? (int)(mx >> 52) - 1022 : kZeroExp;
@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(256) k_slice(const SliceJob *__restrict__ jobs
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             int xr = 0, xi = 0;
-            if (r < j.rows && k + h < j.K) {
+            if (k + h < j.K) {
                 const double2 v = load(k + h);
                 xr = fixq(v.x, e);
                 xi = fixq(v.y, e);
@@ -502,13 +502,16 @@ void plan_mixed(GemmPlan &g) {
     std::vector<std::pair<int, int>> seg_mn(g.segs.size(), {0, 0});
     for (auto &t : g.tiles)
         for (int s = t.seg_begin; s < t.seg_end; ++s) seg_mn[s] = {t.M, t.N};
-    std::map<std::pair<int64_t, int>, int> amap, bmap;
+    // one job per distinct (block offset, operation) of each operand
+    std::unordered_map<int64_t, int> amap, bmap;
+    amap.reserve(2 * g.segs.size());
+    bmap.reserve(2 * g.segs.size());
     for (size_t s = 0; s < g.segs.size(); ++s) {
         const GemmSeg &sg = g.segs[s];
         const int M = seg_mn[s].first, N = seg_mn[s].second;
         if (M == 0) continue;  // segment of no tile
         const int nkc = (sg.K + BKC - 1) / BKC;
-        auto ia = amap.find({sg.a_off, sg.opa});
+        auto ia = amap.find(sg.a_off * 4 + sg.opa);
         if (ia == amap.end()) {
             SliceJob j{};
             j.src_off = sg.a_off;
@@ -524,10 +527,10 @@ void plan_mixed(GemmPlan &g) {
             const int nrt = (M + BM - 1) / BM;
             g.a_planes += (int64_t)nrt * nkc * A_PANEL;
             g.a_exps += (int64_t)nrt * BM;
-            ia = amap.emplace(std::make_pair(sg.a_off, sg.opa), (int)g.ajobs.size()).first;
+            ia = amap.emplace(sg.a_off * 4 + sg.opa, (int)g.ajobs.size()).first;
             g.ajobs.push_back(j);
         }
-        auto ib = bmap.find({sg.b_off, sg.opb});
+        auto ib = bmap.find(sg.b_off * 4 + sg.opb);
         if (ib == bmap.end()) {
             SliceJob j{};
             j.src_off = sg.b_off;
@@ -543,7 +546,7 @@ void plan_mixed(GemmPlan &g) {
             const int nnt = (N + BN - 1) / BN;
             g.b_planes += (int64_t)nnt * nkc * B_PANEL;
             g.b_exps += (int64_t)nnt * BN;
-            ib = bmap.emplace(std::make_pair(sg.b_off, sg.opb), (int)g.bjobs.size()).first;
+            ib = bmap.emplace(sg.b_off * 4 + sg.opb, (int)g.bjobs.size()).first;
             g.bjobs.push_back(j);
         }
         const SliceJob &ja = g.ajobs[ia->second], &jb = g.bjobs[ib->second];
@@ -556,9 +559,9 @@ void plan_mixed(GemmPlan &g) {
     g.aitems.clear();
     g.bitems.clear();
     for (size_t i = 0; i < g.ajobs.size(); ++i)
-        for (int r0 = 0; r0 < (g.ajobs[i].rows + BM - 1) / BM * BM; r0 += 8) g.aitems.push_back({(int)i, r0});
+        for (int r0 = 0; r0 < g.ajobs[i].rows; r0 += 8) g.aitems.push_back({(int)i, r0});
     for (size_t i = 0; i < g.bjobs.size(); ++i)
-        for (int r0 = 0; r0 < (g.bjobs[i].rows + BN - 1) / BN * BN; r0 += 8) g.bitems.push_back({(int)i, r0});
+        for (int r0 = 0; r0 < g.bjobs[i].rows; r0 += 8) g.bitems.push_back({(int)i, r0});
     KV_REQUIRE(g.a_exps < (1ll << 31) && g.b_exps < (1ll << 31), KV_EINVAL, "mixed-precision plan too large");
     g.d_ajobs = upload_vec(g.ajobs);
     g.d_bjobs = upload_vec(g.bjobs);
