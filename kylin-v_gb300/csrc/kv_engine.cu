@@ -842,7 +842,10 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
     DevBuf status(std::max<size_t>(1, P.secs.size()) * sizeof(int));
     svd_gather(P, A.data(), T.as<double2>());
     if (mixed) {
-        svd_jacobi_f32(P, T.as<double2>(), T32.as<float2>(), status.as<int>(), 60, 3e-7f);
+        // tolerance 1e-5 on the columns' cosines: a residual c_ij <= 1e-5 s_i s_j
+        // tilts the kept subspace by ~1e-5 s_j / s_i, and the FP64 polish
+        // rebuilds the kept factor exactly from that subspace
+        svd_jacobi_f32(P, T.as<double2>(), T32.as<float2>(), status.as<int>(), 60, 1e-5f);
         svd_finalize_f32(P, T32.as<float2>(), Us.as<float2>(), S.as<double>());
     } else {
         svd_jacobi(P, T.as<double2>(), V.as<double2>(), status.as<int>(), 60, 1e-15);

@@ -127,6 +127,7 @@ __global__ void __launch_bounds__(NT) k_svd_jacobi_w(const SvdSector *__restrict
     extern __shared__ float2 sT[];
     __shared__ int rotated;
     __shared__ float red[NT / 32];
+    __shared__ float nrm[kJacobiMaxQ];  // |column|^2, recomputed every sweep, updated per rotation
     const SvdSector s = secs[blockIdx.x];
     const int p = s.p, q = s.q;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = NT / 32;
@@ -152,6 +153,15 @@ __global__ void __launch_bounds__(NT) k_svd_jacobi_w(const SvdSector *__restrict
     int sweep = 0;
     bool converged = (q < 2);
     for (; sweep < max_sweeps && !converged; ++sweep) {
+        for (int j = warp; j < q; j += nw) {
+            float a = 0.f;
+            for (int i = lane; i < p; i += 32) {
+                const float2 x = t[(int64_t)j * p + i];
+                a += x.x * x.x + x.y * x.y;
+            }
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+            if (lane == 0) nrm[j] = a;
+        }
         if (threadIdx.x == 0) rotated = 0;
         __syncthreads();
         for (int r = 0; r < m1; ++r) {
@@ -162,26 +172,36 @@ __global__ void __launch_bounds__(NT) k_svd_jacobi_w(const SvdSector *__restrict
                 c1 = qe - 2 - pi + r; if (c1 >= m1) c1 -= m1; ++c1;
                 if (c0 > c1) { const int x = c0; c0 = c1; c1 = x; }
                 if (c1 >= q) continue;  // uniform within the group
+                const float a = nrm[c0], b = nrm[c1];
+                if (!(a > zt) || !(b > zt)) continue;
                 float2 *x = t + (int64_t)c0 * p, *y = t + (int64_t)c1 * p;
-                float a = 0, b = 0, cr = 0, ci = 0;
+                float cr = 0, ci = 0;
                 for (int i = gl; i < p; i += G) {
                     const float2 xi = x[i], yi = y[i];
-                    a += xi.x * xi.x + xi.y * xi.y;
-                    b += yi.x * yi.x + yi.y * yi.y;
                     cr += xi.x * yi.x + xi.y * yi.y;
                     ci += xi.x * yi.y - xi.y * yi.x;
                 }
 #pragma unroll
                 for (int o = G / 2; o > 0; o >>= 1) {
-                    a += __shfl_xor_sync(gmask, a, o, G);
-                    b += __shfl_xor_sync(gmask, b, o, G);
                     cr += __shfl_xor_sync(gmask, cr, o, G);
                     ci += __shfl_xor_sync(gmask, ci, o, G);
                 }
-                if (!(a > zt) || !(b > zt)) continue;
+                // the rotation of kvj::make_rotation, keeping tan(theta) for the norm update:
+                // the new squared norms are a - tan |c| and b + tan |c|
+                const float ac = sqrtf(cr * cr + ci * ci);
+                if (!(ac > tol * sqrtf(a * b))) continue;
+                const float z = (b - a) / (2.f * ac);
+                const float tn = copysignf(1.f, z) / (fabsf(z) + sqrtf(1.f + z * z));
                 kvj::Rot<float> rot;
-                if (!kvj::make_rotation<float>(a, b, cr, ci, tol, rot)) continue;
-                if (gl == 0) rotated = 1;
+                rot.cs = 1.f / sqrtf(1.f + tn * tn);
+                const float sn = tn * rot.cs;
+                rot.s_re = sn * cr / ac;
+                rot.s_im = sn * ci / ac;
+                if (gl == 0) {
+                    rotated = 1;
+                    nrm[c0] = a - tn * ac;
+                    nrm[c1] = b + tn * ac;
+                }
                 for (int i = gl; i < p; i += G) {
                     float2 xi = x[i], yi = y[i];
                     kvj::rotate_pair(rot, xi.x, xi.y, yi.x, yi.y);
@@ -436,15 +456,18 @@ void svd_scatter(const std::vector<SvdScatter> &sc, const SvdPlan &p, const doub
 
 void svd_jacobi_f32(const SvdPlan &p, const double2 *T64, float2 *T, int *status, int max_sweeps, float tol) {
     if (p.secs.empty()) return;
-    static int smem_bytes = 0;  // dynamic shared memory the kernel may use (opt-in maximum less 4 KB)
+    static int smem_bytes = 0;  // dynamic shared memory: opt-in maximum less the static arrays and 4 KB
     if (!smem_bytes) {
         int optin = 0;
         KV_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx().device));
-        smem_bytes = std::max(0, optin - 4096);
+        smem_bytes = std::max(0, optin - 4096 - (int)sizeof(float) * kJacobiMaxQ);
         KV_CUDA(cudaFuncSetAttribute(k_svd_jacobi_w<1024, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
     }
     int64_t max_pq = 0;
-    for (auto &s : p.secs) max_pq = std::max<int64_t>(max_pq, (int64_t)s.p * s.q);
+    for (auto &s : p.secs) {
+        KV_REQUIRE(s.q <= kJacobiMaxQ, KV_EINVAL, "mixed-precision SVD: a sector has more than 2048 columns");
+        max_pq = std::max<int64_t>(max_pq, (int64_t)s.p * s.q);
+    }
     const int cap = smem_bytes / (int)sizeof(float2);
     const int elems = (int)std::min<int64_t>(max_pq, cap);
     k_to_f32<<<std::max(1, ctx().num_sms * 4), 256, 0, ctx().stream>>>(T64, T, p.t_elems);

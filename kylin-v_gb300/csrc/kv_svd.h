@@ -48,6 +48,8 @@ struct SvdDense {
 };
 
 void svd_gather(const SvdPlan &p, const double2 *A, double2 *T);
+// largest number of columns the mixed-mode Jacobi handles in one sector
+constexpr int kJacobiMaxQ = 2048;
 // mixed mode: FP32 one-sided Jacobi of T without accumulated rotations
 // (T oriented so the wanted singular vectors are its columns), sorted
 // normalised columns and singular values, and the first k columns in FP64
