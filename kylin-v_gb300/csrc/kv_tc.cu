@@ -39,7 +39,8 @@
 // Pipeline: warp 0 (one thread) issues the bulk copies of 3 stages
 // (cp.async.bulk completing on mbarriers), warp 1 allocates tensor memory and
 // one thread issues the MMAs (tcgen05.commit frees a stage and signals a
-// drain), warps 2-5 drain (each reads its 32-lane quarter of tensor memory).
+// drain), warps 2-9 drain (two per 32-lane quarter of tensor memory, each
+// taking half of the tile's columns).
 // Every mbarrier wait is bounded; on timeout the CTA records an error, waits
 // (bounded) for its copies and MMAs in flight, frees tensor memory and exits.
 #include <cuda_fp16.h>
@@ -70,9 +71,13 @@ constexpr int GKC = KDRAIN / BKC;              // K panels per drain group
 constexpr int FRAC = 29;
 constexpr int kZeroExp = -4000;                // exponent of an all-zero row
 constexpr long long WAIT_LIMIT = 1ll << 22;
-constexpr int SMEM_BYTES = STAGES * (A_BYTES + B_BYTES) + 1024 + 512;
+constexpr int EPI_WARPS = 8;                   // two per tensor-memory lane quarter, 16 columns each
+constexpr int EPI_COLS = BN / (EPI_WARPS / 4);
+constexpr int NTHREADS = 32 * (2 + EPI_WARPS);
+constexpr int SMEM_BYTES = STAGES * (A_BYTES + B_BYTES) + 1024 + 1024;
 
 static_assert(NACC * BN <= (int)TMEM_COLS, "accumulators exceed tensor memory");
+static_assert(EPI_COLS % 4 == 0, "the drain loads 4 columns per accumulator at once");
 static_assert(A_BYTES + B_BYTES < (1 << 20), "transaction count per stage");
 
 // ----------------------------------------------------------- slicing
@@ -251,7 +256,7 @@ __device__ __forceinline__ void tmem_ld4(uint32_t taddr, float *v) {
     v[3] = __uint_as_float(r3);
 }
 
-__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, %0;" ::"n"(32 * EPI_WARPS) : "memory"); }
 
 // v / 2^sh rounded to nearest, sh >= 0
 __device__ __forceinline__ long long sra_round(long long v, int sh) {
@@ -288,7 +293,7 @@ __device__ __forceinline__ long long combine(const float *p) {
     return (u << 8) + __float2int_rn(p[4]);
 }
 
-__global__ void __launch_bounds__(192, 1) k_gemm_tc(const GemmTile *__restrict__ tiles, const SegX *__restrict__ segs,
+__global__ void __launch_bounds__(NTHREADS, 1) k_gemm_tc(const GemmTile *__restrict__ tiles, const SegX *__restrict__ segs,
                                                     const __half *__restrict__ Apl, const __half *__restrict__ Bpl,
                                                     const int *__restrict__ Aexp, const int *__restrict__ Bexp,
                                                     double2 *__restrict__ C, const int *skip, int *err, int step,
@@ -308,6 +313,7 @@ __global__ void __launch_bounds__(192, 1) k_gemm_tc(const GemmTile *__restrict__
     uint64_t *full = bars, *empty = bars + STAGES, *accf = bars + 2 * STAGES, *acce = accf + 1, *mdone = acce + 1;
     uint32_t *tslot = (uint32_t *)(mdone + 1);
     int *s_ecol = (int *)(tslot + 4);  // [BN] largest column exponent over the tile's segments
+    int *s_fcol = s_ecol + BN;         // [EPI_WARPS][EPI_COLS] each epilogue warp's copy of a segment's
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const GemmTile t = tiles[blockIdx.x];
     const int nseg = t.seg_end - t.seg_begin;
@@ -325,7 +331,7 @@ __global__ void __launch_bounds__(192, 1) k_gemm_tc(const GemmTile *__restrict__
             mbar_init(smem_u32(empty + s), 1);
         }
         mbar_init(smem_u32(accf), 1);
-        mbar_init(smem_u32(acce), 128);
+        mbar_init(smem_u32(acce), 32 * EPI_WARPS);
         mbar_init(smem_u32(mdone), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -407,9 +413,13 @@ __global__ void __launch_bounds__(192, 1) k_gemm_tc(const GemmTile *__restrict__
         }
     } else {
         // ------------------------------------------------ drains and epilogue
-        const int q = warp & 3;  // tensor-memory lane quarter of this warp
+        // warp w reads lane quarter w % 4 (the rows it may access in tensor
+        // memory) and columns [c_lo, c_lo + EPI_COLS)
+        const int q = warp & 3;
+        const int c_lo = ((warp - 2) / 4) * EPI_COLS;
         const int m = q * 32 + lane;
         const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16);
+        int *fw = s_fcol + (warp - 2) * EPI_COLS;  // this warp's copy of the segment's column exponents
         int erow = kZeroExp;
         for (int s = t.seg_begin; s < t.seg_end; ++s)
             if (segs[s].entry <= step) erow = max(erow, Aexp[segs[s].a_exp + t.m0 + m]);
@@ -419,29 +429,32 @@ __global__ void __launch_bounds__(192, 1) k_gemm_tc(const GemmTile *__restrict__
                 if (segs[s].entry <= step) ec = max(ec, Bexp[segs[s].b_exp + t.n0 + lane]);
             s_ecol[lane] = ec;
         }
-        epi_bar();  // the only barrier of the epilogue warps: reached by all four unconditionally
-        long long cr[BN], ci[BN];
+        epi_bar();  // the only barrier of the epilogue warps: reached by all of them unconditionally
+        long long cr[EPI_COLS], ci[EPI_COLS];
 #pragma unroll
-        for (int c = 0; c < BN; ++c) cr[c] = ci[c] = 0;
+        for (int c = 0; c < EPI_COLS; ++c) cr[c] = ci[c] = 0;
         bool ok = true;
         int grp = 0;
         for (int sl = 0; sl < nseg && ok; ++sl) {
             const SegX g = segs[t.seg_begin + sl];
             if (g.entry > step) continue;
-            const int *fcol = Bexp + g.b_exp + t.n0;
+            // column shifts of this segment, into the warp's own shared-memory slots
+            if (lane < EPI_COLS) fw[lane] = s_ecol[c_lo + lane] - Bexp[g.b_exp + t.n0 + c_lo + lane];
+            __syncwarp();
             const int shr = erow - Aexp[g.a_exp + t.m0 + m];
             for (int kc0 = 0; kc0 < g.nkc; kc0 += GKC, ++grp) {
                 // warp-uniform decision: tcgen05.ld below is a warp-wide instruction
                 if (!__all_sync(0xFFFFFFFFu, mbar_wait(smem_u32(accf), (uint32_t)grp & 1u))) { ok = false; break; }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
-                for (int c0 = 0; c0 < BN; c0 += 4) {
+                for (int c0 = 0; c0 < EPI_COLS; c0 += 4) {
                     long long I[NCOMP][4];
 #pragma unroll
                     for (int c = 0; c < NCOMP; ++c) {
                         float a[NORD][4];
 #pragma unroll
-                        for (int o = 0; o < NORD; ++o) tmem_ld4(trow + (uint32_t)((c * NORD + o) * BN + c0), a[o]);
+                        for (int o = 0; o < NORD; ++o)
+                            tmem_ld4(trow + (uint32_t)((c * NORD + o) * BN + c_lo + c0), a[o]);
                         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
                         for (int jx = 0; jx < 4; ++jx) {
@@ -454,7 +467,7 @@ __global__ void __launch_bounds__(192, 1) k_gemm_tc(const GemmTile *__restrict__
 #pragma unroll
                     for (int jx = 0; jx < 4; ++jx) {
                         const int col = c0 + jx;
-                        const int sh = shr + s_ecol[col] - __ldg(fcol + col);
+                        const int sh = shr + fw[col];
                         cr[col] += sra_round(I[0][jx] - I[1][jx], sh);
                         ci[col] += sra_round(I[2][jx] - I[0][jx] - I[1][jx], sh);
                     }
@@ -462,16 +475,17 @@ __global__ void __launch_bounds__(192, 1) k_gemm_tc(const GemmTile *__restrict__
                 asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
                 mbar_arrive(smem_u32(acce));
             }
+            __syncwarp();  // fw is rewritten for the next segment
         }
         if (!ok && lane == 0) atomicExch(err, 1);
         const int gm = t.m0 + m;
         if (ok && gm < t.M) {
             double2 *crow = C + t.c_off + (int64_t)gm * t.ldc;
 #pragma unroll
-            for (int c = 0; c < BN; ++c) {
-                const int gn = t.n0 + c;
+            for (int c = 0; c < EPI_COLS; ++c) {
+                const int gn = t.n0 + c_lo + c;
                 if (gn < t.N) {
-                    const int sc = erow + s_ecol[c] - 2 * FRAC + 16;
+                    const int sc = erow + s_ecol[c_lo + c] - 2 * FRAC + 16;
                     crow[gn] = make_double2(i64_ldexp(cr[c], sc), i64_ldexp(ci[c], sc));
                 }
             }
@@ -597,7 +611,7 @@ void launch_gemm_mixed(const GemmPlan &p, const double2 *A, const double2 *B, do
         KV_CUDA(cudaGetLastError());
         ++n;
     }
-    k_gemm_tc<<<(unsigned)p.tiles.size(), 192, SMEM_BYTES, c.stream>>>(
+    k_gemm_tc<<<(unsigned)p.tiles.size(), NTHREADS, SMEM_BYTES, c.stream>>>(
         p.d_tiles.as<GemmTile>(), p.d_xsegs.as<SegX>(), ap.as<__half>(), bp.as<__half>(), ae.as<int>(), be.as<int>(),
         C, skip, g_err, step, p.write_inactive ? 1 : 0);
     KV_CUDA(cudaGetLastError());
