@@ -13,6 +13,8 @@
 #include <numeric>
 #include <string>
 
+#include <functional>
+
 #include "kv_engine.h"
 #include "kv_svd.h"
 
@@ -741,11 +743,13 @@ TensorP op_lanczos(int nsite, const DTensor &L, const DTensor &psi, const DTenso
 }
 
 // ---------------------------------------------------------------- SVD
-// mixed mode: singular values below this fraction of their sector's largest
-// are below the FP32 Jacobi's resolution (exact zeros come out at up to
-// ~1e-5 relative after many FP32 rotations) and are treated as zero; a state
-// dropped by this rule carries at most 1e-8 of the sector's weight
-constexpr double kMixedSvdFloor = 1e-4;
+// mixed mode: FP32 singular values below this fraction of their sector's
+// largest are treated as zero before ranking (a state dropped by this rule
+// carries at most 1e-12 of the sector's weight).  FP32 values above it are
+// only used to choose which columns get their value recomputed in FP64: an
+// FP32 value that is rounding noise on an exact zero (up to ~1e-5 relative)
+// comes back near zero from the FP64 rebuild and is dropped there.
+constexpr double kMixedSvdFloor = 1e-6;
 
 struct Micro {
     std::array<int, kMaxRank> shape{}, qn{};
@@ -861,36 +865,150 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
     for (int x : st) KV_REQUIRE(x >= 0, KV_ETIMEOUT, "Jacobi SVD did not converge within the sweep limit");
     for (double x : sv) KV_REQUIRE(std::isfinite(x), KV_ENONFINITE, "non-finite singular value");
     if (mixed) {
-        // FP32 Jacobi resolves singular values only down to ~1e-5 of the
-        // sector's largest: anything below kMixedSvdFloor of it is a zero
+        // below kMixedSvdFloor of the sector's largest: zero
         for (auto &sc : P.secs) {
             const double smax = sc.q > 0 ? sv[sc.s_off] : 0.0;
             for (int i = 0; i < sc.q; ++i)
                 if (sv[sc.s_off + i] <= kMixedSvdFloor * smax) sv[sc.s_off + i] = 0.0;
         }
     }
-    // global ordering and truncation, holstein/svd.h:350-388
-    std::vector<std::pair<int, double>> collect;
-    for (size_t s = 0; s < P.secs.size(); ++s) {
-        const int q = l2r ? rows[sec_rc[s].first].q : cols[sec_rc[s].second].q;
-        // min(m, n) singular values (a wide mixed-mode T has q - p surplus zero columns, sorted last)
-        const int ns = std::min(P.secs[s].m, P.secs[s].n);
-        for (int i = 0; i < ns; ++i) collect.push_back({q, sv[P.secs[s].s_off + i]});
-    }
-    std::sort(collect.begin(), collect.end(), [](const std::pair<int, double> &a, const std::pair<int, double> &b) {
-        return a.second > b.second;
-    });
+    const int nsec = (int)P.secs.size();
+    // global ordering and truncation, holstein/svd.h:350-388: all singular
+    // values sorted descending, dropped from the tail while i >= max_dim or
+    // s <= thres (never the first); returns the kept count per sector
+    auto truncate = [&](const std::vector<double> &vals, std::vector<double> *kept_vals, int *total) {
+        std::vector<std::pair<int, double>> collect;
+        std::vector<int> cnt(nsec, 0);
+        for (int s_ = 0; s_ < nsec; ++s_) {
+            // min(m, n) singular values (a wide mixed-mode T has q - p surplus zero columns, sorted last)
+            cnt[s_] = std::min(P.secs[s_].m, P.secs[s_].n);
+            for (int i = 0; i < cnt[s_]; ++i) collect.push_back({s_, vals[P.secs[s_].s_off + i]});
+        }
+        std::sort(collect.begin(), collect.end(),
+                  [](const std::pair<int, double> &a, const std::pair<int, double> &b) { return a.second > b.second; });
+        if (total) *total = (int)collect.size();
+        for (int i = (int)collect.size() - 1; i > 0; --i) {
+            if (!(i >= max_dim || collect[i].second <= thres)) break;
+            --cnt[collect[i].first];
+            collect.pop_back();
+        }
+        if (kept_vals)
+            for (auto &c : collect) kept_vals->push_back(c.second);
+        return cnt;
+    };
     SvdOut out;
-    out.n_total = (int)collect.size();
-    for (int i = (int)collect.size() - 1; i > 0; --i) {
-        if (!(i >= max_dim || collect[i].second <= thres)) break;
-        const int q = collect[i].first;
-        for (auto &rw : rows) if (rw.q == (l2r ? q : -q)) { rw.kept -= 1; break; }
-        for (auto &cl : cols) if (cl.q == (l2r ? -q : q)) { cl.kept -= 1; break; }
-        collect.pop_back();
+    std::vector<int> kfin = truncate(sv, &out.kept_s, &out.n_total);
+    // ---- mixed mode, part 1: FP64 rebuild of the candidate columns.  The
+    // kept factor is rebuilt in FP64 from the sector matrix and the FP32
+    // singular vectors of the other side,
+    //   L->R: X = A_s V S^-1   R->L: X = A_s^H U S^-1,
+    // over each sector's FP32-kept columns plus the candidates within 10%
+    // below the cutoff.  The first Cholesky-QR pass is a Gram-Schmidt in
+    // descending order: s_j R_jj is column j's singular value with the FP32
+    // error along the larger columns projected out, accurate to FP64 where
+    // the FP32 value is not (its error is ~1e-7 of the sector's largest).
+    // The truncation is redone with those values so the kept set is the one
+    // FP64 values select; the kept columns are a prefix of the pass-1 basis.
+    const int side = l2r ? 0 : 1;  // which factor is kept orthonormal
+    std::vector<int> kc(nsec, 0);  // columns rebuilt per sector
+    std::vector<SvdPolish> pol;
+    std::vector<int> pol_of_sector(nsec, -1);
+    DevBuf X, Gm, Wb, cst, cdiag;
+    const int tm = kTileM(KV_FP64), tn = kTileN(KV_FP64);
+    auto add_gemm = [&](GemmPlan &g, int64_t c_off, int M, int N, GemmSeg seg) {
+        const int sb = (int)g.segs.size();
+        g.segs.push_back(seg);
+        for (int m0 = 0; m0 < M; m0 += tm)
+            for (int n0 = 0; n0 < N; n0 += tn) g.tiles.push_back({c_off, N, M, N, m0, n0, sb, sb + 1});
+    };
+    auto polish_pass = [&](const std::vector<SvdPolish> &pl_list, const DevBuf &dp, double shift) {
+        GemmPlan gram;
+        int kmax = 1;
+        for (auto &pl : pl_list) {
+            add_gemm(gram, pl.g_off, pl.k, pl.k, GemmSeg{pl.x_off, pl.x_off, pl.rows, pl.ldx, pl.ldx, 1, 0});
+            kmax = std::max(kmax, pl.k);
+        }
+        gram.upload();
+        std::vector<int> item_pol, item_row0;
+        for (size_t i = 0; i < pl_list.size(); ++i)
+            for (int r0 = 0; r0 < pl_list[i].rows; r0 += kTrsmRows) {
+                item_pol.push_back((int)i);
+                item_row0.push_back(r0);
+            }
+        launch_gemm_fp64(gram, X.as<double2>(), X.as<double2>(), Gm.as<double2>(), 1.0, nullptr);
+        svd_chol(dp, (int)pl_list.size(), Gm.as<double2>(), cst.as<int>(), cdiag.as<double>(), shift);
+        svd_trsm(dp, item_pol, item_row0, Gm.as<double2>(), X.as<double2>(), kmax);
+    };
+    if (mixed) {
+        const double s_cut = out.kept_s.empty() ? 0.0 : out.kept_s.back();
+        int64_t x_elems = 0, g_elems = 0, w_elems = 0;
+        for (int s_ = 0; s_ < nsec; ++s_) {
+            const SvdSector &sc = P.secs[s_];
+            const int ns = std::min(sc.m, sc.n);
+            int k = kfin[s_];
+            while (k < ns && k < kfin[s_] + 64 && sv[sc.s_off + k] > 0.0 && sv[sc.s_off + k] >= 0.9 * s_cut) ++k;
+            kc[s_] = k;
+            if (k <= 0) continue;
+            const int xr = side == 0 ? sc.m : sc.n;  // rows of the kept factor
+            const int wr = side == 0 ? sc.n : sc.m;  // rows of the other side's vectors
+            pol_of_sector[s_] = (int)pol.size();
+            pol.push_back({x_elems, g_elems, w_elems, s_, xr, k, k});
+            x_elems += (int64_t)xr * k;
+            g_elems += (int64_t)k * k;
+            w_elems += (int64_t)wr * k;
+        }
+        DevBuf dpol = upload_vec(pol);
+        X = DevBuf(std::max<int64_t>(1, x_elems) * sizeof(double2));
+        Gm = DevBuf(std::max<int64_t>(1, g_elems) * sizeof(double2));
+        Wb = DevBuf(std::max<int64_t>(1, w_elems) * sizeof(double2));
+        cst = DevBuf(std::max<size_t>(1, pol.size()) * sizeof(int));
+        cdiag = DevBuf(std::max<size_t>(1, pol.size()) * sizeof(double));
+        KV_CUDA(cudaMemsetAsync(cst.p, 0, std::max<size_t>(1, pol.size()) * sizeof(int), ctx().stream));
+        svd_extract(dpol, (int)pol.size(), P, Us.as<float2>(), S.as<double>(), Wb.as<double2>());
+        // X = A_s W (L->R, K = n) or A_s^H W (R->L, K = m), A_s from T:
+        // A_s[i, j] = T[i + j p] (T = A_s) or conj(T[j + i p]) (T = A_s^H)
+        GemmPlan build;
+        for (auto &pl : pol) {
+            const SvdSector &sc = P.secs[pl.sector];
+            if (side == 0)
+                add_gemm(build, pl.x_off, sc.m, pl.k,
+                         GemmSeg{sc.t_off, pl.w_off, sc.n, sc.p, pl.k, sc.transposed ? 3 : 2, 0});
+            else
+                add_gemm(build, pl.x_off, sc.n, pl.k,
+                         GemmSeg{sc.t_off, pl.w_off, sc.m, sc.p, pl.k, sc.transposed ? 2 : 3, 0});
+        }
+        build.upload();
+        launch_gemm_fp64(build, T.as<double2>(), Wb.as<double2>(), X.as<double2>(), 1.0, nullptr);
+        // pass 1 (a 1e-14 relative shift keeps it defined; the span never changes)
+        polish_pass(pol, dpol, 1e-14);
+        // R's diagonals: refined singular values of the rebuilt columns
+        std::vector<std::vector<double2>> diag(pol.size());
+        for (size_t i = 0; i < pol.size(); ++i) {
+            diag[i].resize(pol[i].k);
+            KV_CUDA(cudaMemcpy2DAsync(diag[i].data(), sizeof(double2), Gm.as<double2>() + pol[i].g_off,
+                                      (size_t)(pol[i].k + 1) * sizeof(double2), sizeof(double2), pol[i].k,
+                                      cudaMemcpyDeviceToHost, ctx().stream));
+        }
+        KV_CUDA(cudaStreamSynchronize(ctx().stream));
+        std::vector<double> svr = sv;
+        for (size_t i = 0; i < pol.size(); ++i) {
+            const SvdSector &sc = P.secs[pol[i].sector];
+            for (int j = 0; j < pol[i].k; ++j) svr[sc.s_off + j] = sv[sc.s_off + j] * std::fabs(diag[i][j].x);
+        }
+        out.kept_s.clear();
+        kfin = truncate(svr, nullptr, nullptr);
+        for (int s_ = 0; s_ < nsec; ++s_) {
+            kfin[s_] = std::min(kfin[s_], kc[s_]);
+            for (int j = 0; j < kfin[s_]; ++j) out.kept_s.push_back(svr[P.secs[s_].s_off + j]);
+        }
+        std::sort(out.kept_s.begin(), out.kept_s.end(), std::greater<double>());
     }
-    out.n_kept = (int)collect.size();
-    for (auto &c : collect) out.kept_s.push_back(c.second);
+    out.n_kept = 0;
+    for (int s_ = 0; s_ < nsec; ++s_) {
+        rows[sec_rc[s_].first].kept = kfin[s_];
+        cols[sec_rc[s_].second].kept = kfin[s_];
+        out.n_kept += kfin[s_];
+    }
     // redistribution, holstein/svd.h:405-428 with LeftDir = -1
     Meta mu, mv;
     mu.rank = r1 + 1;
@@ -901,9 +1019,9 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
     for (int i = r1; i < M.rank; ++i) mv.dirs[i - r1 + 1] = M.dirs[i];
     struct Pending { int sector, side, pos, len, kept; };
     std::vector<Pending> pu, pv;
-    for (size_t s = 0; s < P.secs.size(); ++s) {
-        Macro &rw = rows[sec_rc[s].first];
-        Macro &cl = cols[sec_rc[s].second];
+    for (int s_ = 0; s_ < nsec; ++s_) {
+        Macro &rw = rows[sec_rc[s_].first];
+        Macro &cl = cols[sec_rc[s_].second];
         if (rw.kept <= 0 || cl.kept <= 0) continue;
         for (auto &ra : rw.subs) {
             BlockMeta b;
@@ -911,7 +1029,7 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
             b.shape[r1] = rw.kept;
             b.qn[r1] = rw.q;
             mu.blocks.push_back(b);
-            pu.push_back({(int)s, 0, ra.pos, ra.len, rw.kept});
+            pu.push_back({s_, 0, ra.pos, ra.len, rw.kept});
         }
         for (auto &ca : cl.subs) {
             BlockMeta b;
@@ -919,7 +1037,7 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
             b.qn[0] = -cl.q;
             for (int i = 0; i < M.rank - r1; ++i) { b.shape[i + 1] = ca.shape[i]; b.qn[i + 1] = ca.qn[i]; }
             mv.blocks.push_back(b);
-            pv.push_back({(int)s, 1, ca.pos, ca.len, cl.kept});
+            pv.push_back({s_, 1, ca.pos, ca.len, cl.kept});
         }
     }
     out.U = DTensor::make(mu, false);
@@ -934,85 +1052,40 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
         svd_scatter(svs, P, Us.as<double2>(), Vs.as<double2>(), S.as<double>(), out.V->data());
         return out;
     }
-    // ---- mixed mode: FP64 polish.  The kept factor is rebuilt in FP64 from the
-    // sector matrix and the FP32 singular vectors of the other side,
-    //   L->R: X = A_s V_k S_k^-1   R->L: X = A_s^H U_k S_k^-1,
-    // made orthonormal by Cholesky-QR2, and the other factor is the
-    // exact projection (Y = X^H A_s, or A_s X).  With no truncation the
-    // factorisation is exact to FP64 rounding; the FP32 error only enters the
-    // choice of the discarded directions.
-    const int side = l2r ? 0 : 1;  // which factor is kept orthonormal
-    std::vector<SvdPolish> pol;
-    std::vector<int> pol_of_sector(P.secs.size(), -1);
-    int64_t x_elems = 0, g_elems = 0, y_elems = 0, w_elems = 0;
-    std::vector<int64_t> y_off(P.secs.size(), 0);
-    for (size_t s_ = 0; s_ < P.secs.size(); ++s_) {
-        const int k = rows[sec_rc[s_].first].kept;
-        if (k <= 0 || cols[sec_rc[s_].second].kept <= 0) continue;
+    // ---- mixed mode, part 2: the kept prefix of each sector's pass-1 basis
+    // (X keeps its row stride kc), a second Cholesky-QR pass for FP64
+    // orthonormality, and the other factor as the exact projection
+    // (Y = X^H A_s, or A_s X).  With no truncation the factorisation is exact
+    // to FP64 rounding; the FP32 error only enters the choice of directions.
+    std::vector<SvdPolish> pol2;
+    std::vector<int> pol2_of_sector(nsec, -1);
+    std::vector<int64_t> y_off(nsec, 0);
+    int64_t y_elems = 0;
+    for (auto pl : pol) {
+        const int s_ = pl.sector;
+        if (kfin[s_] <= 0) continue;
         const SvdSector &sc = P.secs[s_];
-        const int xr = side == 0 ? sc.m : sc.n;  // rows of the kept factor
-        const int wr = side == 0 ? sc.n : sc.m;  // rows of the other side's vectors
-        pol_of_sector[s_] = (int)pol.size();
-        pol.push_back({x_elems, g_elems, w_elems, (int)s_, xr, k, 0});
-        x_elems += (int64_t)xr * k;
-        g_elems += (int64_t)k * k;
-        w_elems += (int64_t)wr * k;
+        pl.k = kfin[s_];
+        pol2_of_sector[s_] = (int)pol2.size();
+        pol2.push_back(pl);
         y_off[s_] = y_elems;
-        y_elems += (int64_t)k * (side == 0 ? sc.n : sc.m);
+        y_elems += (int64_t)pl.k * (side == 0 ? sc.n : sc.m);
     }
-    DevBuf dpol = upload_vec(pol);
-    DevBuf X(std::max<int64_t>(1, x_elems) * sizeof(double2)), Gm(std::max<int64_t>(1, g_elems) * sizeof(double2));
-    DevBuf Y(std::max<int64_t>(1, y_elems) * sizeof(double2)), Wb(std::max<int64_t>(1, w_elems) * sizeof(double2));
-    DevBuf cst(std::max<size_t>(1, pol.size()) * sizeof(int)), cdiag(std::max<size_t>(1, pol.size()) * sizeof(double));
-    KV_CUDA(cudaMemsetAsync(cst.p, 0, std::max<size_t>(1, pol.size()) * sizeof(int), ctx().stream));
-    svd_extract(dpol, (int)pol.size(), P, Us.as<float2>(), S.as<double>(), Wb.as<double2>());
-    const int tm = kTileM(KV_FP64), tn = kTileN(KV_FP64);
-    auto add_gemm = [&](GemmPlan &g, int64_t c_off, int M, int N, GemmSeg seg) {
-        const int sb = (int)g.segs.size();
-        g.segs.push_back(seg);
-        for (int m0 = 0; m0 < M; m0 += tm)
-            for (int n0 = 0; n0 < N; n0 += tn) g.tiles.push_back({c_off, N, M, N, m0, n0, sb, sb + 1});
-    };
-    // X = A_s W (L->R, K = n) or A_s^H W (R->L, K = m), A_s from T:
-    // A_s[i, j] = T[i + j p] (T = A_s) or conj(T[j + i p]) (T = A_s^H)
-    GemmPlan build;
-    for (auto &pl : pol) {
-        const SvdSector &sc = P.secs[pl.sector];
-        if (side == 0)
-            add_gemm(build, pl.x_off, sc.m, pl.k, GemmSeg{sc.t_off, pl.w_off, sc.n, sc.p, pl.k, sc.transposed ? 3 : 2, 0});
-        else
-            add_gemm(build, pl.x_off, sc.n, pl.k, GemmSeg{sc.t_off, pl.w_off, sc.m, sc.p, pl.k, sc.transposed ? 2 : 3, 0});
-    }
-    build.upload();
-    launch_gemm_fp64(build, T.as<double2>(), Wb.as<double2>(), X.as<double2>(), 1.0, nullptr);
-    GemmPlan gram;
-    for (auto &pl : pol) add_gemm(gram, pl.g_off, pl.k, pl.k, GemmSeg{pl.x_off, pl.x_off, pl.rows, pl.k, pl.k, 1, 0});
-    gram.upload();
-    std::vector<int> item_pol, item_row0;
-    int kmax = 1;
-    for (auto &pl : pol) kmax = std::max(kmax, pl.k);
-    for (size_t i = 0; i < pol.size(); ++i)
-        for (int r0 = 0; r0 < pol[i].rows; r0 += kTrsmRows) { item_pol.push_back((int)i); item_row0.push_back(r0); }
-    // Cholesky-QR2: X = A_s W Sigma^-1 is orthonormal up to the FP32 error of
-    // W, so two passes give FP64 orthonormality (the first with a 1e-14
-    // relative shift to keep it defined); the span never changes
-    for (int pass = 0; pass < 2; ++pass) {
-        launch_gemm_fp64(gram, X.as<double2>(), X.as<double2>(), Gm.as<double2>(), 1.0, nullptr);
-        svd_chol(dpol, (int)pol.size(), Gm.as<double2>(), cst.as<int>(), cdiag.as<double>(), pass == 0 ? 1e-14 : 0.0);
-        svd_trsm(dpol, item_pol, item_row0, Gm.as<double2>(), X.as<double2>(), kmax);
-    }
+    DevBuf dpol2 = upload_vec(pol2);
+    if (!pol2.empty()) polish_pass(pol2, dpol2, 0.0);
+    DevBuf Y(std::max<int64_t>(1, y_elems) * sizeof(double2));
     GemmPlan proj;
-    for (auto &pl : pol) {
+    for (auto &pl : pol2) {
         const SvdSector &sc = P.secs[pl.sector];
         const int64_t tof = sc.t_off;
         if (side == 0) {
             // Y = X^H A_s (k x n)
             add_gemm(proj, y_off[pl.sector], pl.k, sc.n,
-                     GemmSeg{pl.x_off, tof, sc.m, pl.k, sc.p, 1, sc.transposed ? 3 : 1});
+                     GemmSeg{pl.x_off, tof, sc.m, pl.ldx, sc.p, 1, sc.transposed ? 3 : 1});
         } else {
             // Lef = A_s X (m x k)
             add_gemm(proj, y_off[pl.sector], sc.m, pl.k,
-                     GemmSeg{tof, pl.x_off, sc.n, sc.p, pl.k, sc.transposed ? 3 : 2, 0});
+                     GemmSeg{tof, pl.x_off, sc.n, sc.p, pl.ldx, sc.transposed ? 3 : 2, 0});
         }
     }
     proj.upload();
@@ -1021,16 +1094,16 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
     std::vector<SvdDense> du, dv;
     for (size_t i = 0; i < pu.size(); ++i) {
         const int s_ = pu[i].sector;
-        const SvdPolish &pl = pol[pol_of_sector[s_]];
-        if (side == 0) du.push_back({out.U->meta.blocks[i].off, pl.x_off, 0, pu[i].pos, pu[i].len, pl.k, pl.k, 0});
+        const SvdPolish &pl = pol2[pol2_of_sector[s_]];
+        if (side == 0) du.push_back({out.U->meta.blocks[i].off, pl.x_off, 0, pu[i].pos, pu[i].len, pl.k, pl.ldx, 0});
         else du.push_back({out.U->meta.blocks[i].off, y_off[s_], 0, pu[i].pos, pu[i].len, pl.k, pl.k, 0});
     }
     for (size_t i = 0; i < pv.size(); ++i) {
         const int s_ = pv[i].sector;
-        const SvdPolish &pl = pol[pol_of_sector[s_]];
+        const SvdPolish &pl = pol2[pol2_of_sector[s_]];
         if (side == 0)
             dv.push_back({out.V->meta.blocks[i].off, y_off[s_], 1, pv[i].pos, pv[i].len, pl.k, P.secs[s_].n, 0});
-        else dv.push_back({out.V->meta.blocks[i].off, pl.x_off, 1, pv[i].pos, pv[i].len, pl.k, pl.k, 1});
+        else dv.push_back({out.V->meta.blocks[i].off, pl.x_off, 1, pv[i].pos, pv[i].len, pl.k, pl.ldx, 1});
     }
     svd_scatter_dense(du, side == 0 ? X.as<double2>() : Y.as<double2>(), out.U->data());
     svd_scatter_dense(dv, side == 0 ? Y.as<double2>() : X.as<double2>(), out.V->data());

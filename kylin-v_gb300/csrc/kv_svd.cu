@@ -344,7 +344,7 @@ __global__ void __launch_bounds__(32 * kTrsmRows) k_trsm_rows(const SvdPolish *_
     if (row >= d.rows) return;  // warp-uniform
     const int k = d.k;
     const double2 *r = G + d.g_off;
-    double2 *x = X + d.x_off + (int64_t)row * k;
+    double2 *x = X + d.x_off + (int64_t)row * d.ldx;
     double2 *y = ys + (int64_t)warp * k;
     for (int c = 0; c < k; ++c) {
         double sr = 0.0, si = 0.0;

@@ -34,11 +34,12 @@ struct SvdPlan {
 };
 
 // FP64 polish of the kept factor of one sector (mixed mode): W (the FP32
-// kept singular vectors of the other side) at w_off, the factor X
-// (rows x k, row-major) at x_off, its Gram / Cholesky factor (k x k) at g_off
+// singular vectors of the other side, divided by their singular values) at
+// w_off, the factor X (rows x k, row-major with row stride ldx >= k) at
+// x_off, its Gram / Cholesky factor (k x k) at g_off
 struct SvdPolish {
     int64_t x_off, g_off, w_off;
-    int sector, rows, k, pad;
+    int sector, rows, k, ldx;
 };
 // one output block copied from a dense row-major factor M (ld columns);
 // ctrans: the block is taken from M^H
