@@ -2,7 +2,7 @@
  * kvgpu.h -- C ABI of the GB300-native Holstein TDVP library (libkvgpu.so).
  *
  * The reference (Kylin-V) has no FFI: its operator surface is the C++
- * template API of holstein/*.h, called by src/kln-tdvp.cpp:73-78.  Each entry
+ * template API of the holstein/ headers, called by src/kln-tdvp.cpp:73-78.  Each entry
  * point below replaces one function of that surface; the citation on each
  * declaration names the reference function (file:line) whose arguments,
  * results and error behaviour it mirrors.
@@ -150,6 +150,12 @@ int kv_tdvp_free(kv_tdvp s);
 int kv_profile(int enable);
 int kv_profile_read(double *gemm_ms, double *gemm_ref_flops, long long *gemm_launches);
 int kv_counters(long long *launches);
+
+/* State::canonicalize (holstein/state.h:166-185): an L->R SVD sweep then an
+ * R->L one with truncation tol_svd / max_dim (the reference's defaults are 0
+ * and 1000), leaving the orthogonality centre on site 0.  out receives nsites
+ * new handles; the inputs are not modified. */
+int kv_canonicalize(int nsites, const kv_tensor *mps, double tol_svd, int max_dim, int precision, kv_tensor *out);
 
 /* <a|W|b> (Operator::join, holstein/operator.h:178-198) over nsites. */
 int kv_expectation(int nsites, const kv_tensor *bra, const kv_tensor *mpo, const kv_tensor *ket, double *re,

@@ -282,6 +282,18 @@ int kv_tdvp_free(kv_tdvp s) {
     return guard([&] { delete s; });
 }
 
+int kv_canonicalize(int nsites, const kv_tensor *mps, double tol_svd, int max_dim, int precision, kv_tensor *out) {
+    return guard([&] {
+        kv::require_init();
+        KV_REQUIRE(nsites >= 1 && mps && out, KV_EINVAL, "null argument");
+        std::vector<kv::TensorP> in;
+        for (int i = 0; i < nsites; ++i) in.push_back(kv::clone(*T(mps[i])));
+        std::vector<kv::TensorP> r = kv::op_canonicalize(in, tol_svd, max_dim, precision);
+        sync();
+        for (int i = 0; i < nsites; ++i) out[i] = wrap(r[i]);
+    });
+}
+
 int kv_expectation(int nsites, const kv_tensor *bra, const kv_tensor *mpo, const kv_tensor *ket, double *re,
                    double *im) {
     return guard([&] {

@@ -1408,6 +1408,27 @@ void Tdvp::two_site() {
     end_sweep();
 }
 
+// State::canonicalize (holstein/state.h:166-185): an L->R sweep of svd_impl<2,1>
+// carrying S.V^H into the next site, then an R->L sweep of svd_impl<1,2>
+// carrying U.S into the previous one; the orthogonality centre ends on site 0.
+std::vector<TensorP> op_canonicalize(const std::vector<TensorP> &in, double tol, int max_dim, int precision) {
+    check_precision(precision);
+    KV_REQUIRE(!in.empty(), KV_EINVAL, "empty MPS");
+    std::vector<TensorP> t(in.begin(), in.end());
+    const int ns = (int)t.size();
+    for (int i = 0; i < ns - 1; ++i) {
+        SvdOut r = op_svd(*t[i], 2, true, tol, max_dim, precision);
+        t[i] = r.U;
+        t[i + 1] = op_product(*r.V, *t[i + 1], 1, KV_OP_N, KV_OP_N, precision);
+    }
+    for (int i = ns - 1; i > 0; --i) {
+        SvdOut r = op_svd(*t[i], 1, false, tol, max_dim, precision);
+        t[i] = r.V;
+        t[i - 1] = op_product(*t[i - 1], *r.U, 1, KV_OP_N, KV_OP_N, precision);
+    }
+    return t;
+}
+
 // Operator::join (holstein/operator.h:178-198)
 cplx op_expectation(const std::vector<DTensor *> &a, const std::vector<DTensor *> &w, const std::vector<DTensor *> &b) {
     TensorP env = boundary_env(1, 0);

@@ -80,6 +80,7 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
 TensorP op_env(bool l2r, const DTensor &env, const DTensor &A, const DTensor &W, const DTensor *Wt, int precision,
                Flops *fl);
 TensorP op_permute(const DTensor &t, const std::vector<int> &ax);
+std::vector<TensorP> op_canonicalize(const std::vector<TensorP> &in, double tol, int max_dim, int precision);
 cplx op_expectation(const std::vector<DTensor *> &a, const std::vector<DTensor *> &w, const std::vector<DTensor *> &b);
 // the same value with all device scratch in a fixed static array (kv_noalloc.cu)
 cplx expectation_noalloc(const std::vector<DTensor *> &bra, const std::vector<DTensor *> &w,

@@ -28,7 +28,7 @@ EXPORTS = (
     "kv_tensor_download", "kv_tensor_free", "kv_product", "kv_heff_apply", "kv_env_update", "kv_lanczos_expm",
     "kv_svd_truncate", "kv_tdvp_create", "kv_tdvp_sweep", "kv_tdvp_site", "kv_tdvp_stats", "kv_tdvp_free",
     "kv_expectation", "kv_profile", "kv_profile_read", "kv_counters", "kv_expectation_noalloc",
-    "kv_tdvp_host_stats",
+    "kv_tdvp_host_stats", "kv_canonicalize",
 )
 
 
@@ -76,6 +76,7 @@ def lib():
         L.kv_counters.argtypes = [ctypes.POINTER(ctypes.c_longlong)]
         L.kv_tdvp_free.argtypes = [vp]
         L.kv_expectation.argtypes = [ctypes.c_int, pvp, pvp, pvp, dp, dp]
+        L.kv_canonicalize.argtypes = [ctypes.c_int, pvp, ctypes.c_double, ctypes.c_int, ctypes.c_int, pvp]
         L.kv_expectation_noalloc.argtypes = [ctypes.c_int, pvp, pvp, pvp, dp, dp]
         _lib = L
     return _lib
@@ -216,6 +217,16 @@ def expectation(bra, mpo, ket) -> complex:
     re, im = ctypes.c_double(), ctypes.c_double()
     check(lib().kv_expectation(ns, arr(hb), arr(hw), arr(hk), ctypes.byref(re), ctypes.byref(im)))
     return complex(re.value, im.value)
+
+
+def canonicalize(mps, tol_svd=0.0, max_dim=1000, precision=KV_FP64) -> list:
+    """State::canonicalize (holstein/state.h:166-185): L->R then R->L SVD
+    sweeps; returns new site tensors with the orthogonality centre on site 0."""
+    ns = len(mps)
+    hs = [_t(x) for x in mps]
+    outs = (ctypes.c_void_p * ns)()
+    check(lib().kv_canonicalize(ns, (ctypes.c_void_p * ns)(*[h.ptr for h in hs]), tol_svd, max_dim, precision, outs))
+    return [Tensor(outs[i]) for i in range(ns)]
 
 
 def profile(enable: bool):

@@ -150,3 +150,32 @@ def test_sweep_reference_flops(gpu, case):
         t.two_site() if mode == 2 else t.one_site()
         gf = t.stats()["ref_flops"]
         assert of > 0 and abs(gf - of) <= 1e-9 * of, (gf, of)
+
+
+@pytest.mark.parametrize("case", sorted(U.manifest()))
+def test_canonicalize(gpu, case):
+    """State::canonicalize on a non-canonical MPS: the state is unchanged,
+    sites 1..ns-1 are right-orthonormal, and the bond dimensions equal those
+    of the same SVD / product sequence run on the oracle."""
+    O = U.load_oracle()
+    ch, mps, _, _ = _traj_case(case, 0)
+    rng = np.random.default_rng(5)
+    bent = [kvio.BlockTensor(t.dirs, [(q, a * (1.0 + 0.3 * rng.standard_normal(a.shape))) for q, a in t.blocks])
+            for t in mps]
+    ident = [gpu.Tensor.from_host(x) for x in H.identity_mpo(ch)]
+    out = gpu.canonicalize(bent)
+    nin = gpu.expectation(bent, ident, bent).real
+    assert abs(gpu.expectation(out, ident, out).real - nin) < 1e-10 * nin
+    assert abs(gpu.expectation(out, ident, bent) - nin) < 1e-10 * nin
+    host = [t.to_host() for t in out]
+    for a in host[1:]:
+        for _, blk in O.product(a, a, 2, O.OP_N, O.OP_C).as_dict().items():
+            assert np.abs(blk - np.eye(blk.shape[0])).max() < 1e-12
+    ref = list(bent)
+    for i in range(len(ref) - 1):
+        u, v, _, _ = O.svd(ref[i], 2, True, 0.0, 1000)
+        ref[i], ref[i + 1] = u, O.product(v, ref[i + 1], 1)
+    for i in range(len(ref) - 1, 0, -1):
+        u, v, _, _ = O.svd(ref[i], 1, False, 0.0, 1000)
+        ref[i], ref[i - 1] = v, O.product(ref[i - 1], u, 1)
+    assert [t.legs()[2] for t in host[:-1]] == [t.legs()[2] for t in ref[:-1]]
