@@ -131,90 +131,65 @@ __global__ void __launch_bounds__(KT) k_normalize(KrylovState *st, const double2
         vnext[i] = make_double2(hv[i].x * inv, hv[i].y * inv);
 }
 
-// T = tridiag(Re alpha, beta upper); c = Z exp(img Lambda) Z^H e0 with
-// img = -i (forward) or +i (reverse): holstein/exponential.h:163-183.
-// The phases of the off-diagonal go into a diagonal unitary, T = P S P^H with
-// S real symmetric tridiagonal (off-diagonal |beta_k|, p_0 = 1,
-// p_{k+1} = p_k conj(beta_k)/|beta_k|), so c = P Z_S exp(img Lambda) Z_S^T e0.
-// S is diagonalised by implicit-shift QL (Wilkinson-type shift, Givens chase;
-// the textbook tridiagonal QL method).  One warp: every lane runs the same
-// scalar recurrence on its own copy of the diagonals, so no lane waits on
-// another, and lane k applies each rotation to row k of the eigenvector
-// matrix; the eigenvalues' phases and the sum over eigenvectors are
-// lane-parallel.  FP64 throughout.
+// T = tridiag(Re alpha, beta upper); c = exp(img T) e0 with img = -i (forward)
+// or +i (reverse).  The reference forms the same vector as
+// Z exp(img Lambda) Z^H e0 from a dense eigendecomposition
+// (holstein/exponential.h:163-183).  Here it is summed directly: m sub-steps
+// with ||T/m||_1 <= 1, each a Taylor series of exp(img T/m) applied to the
+// vector (terms t_k = img T t_{k-1} / (m k), stopping once a term falls below
+// 1e-18 of the sum), so no term is larger than the vector it is added to.
+// One warp; lane i holds component i and takes its neighbours' components
+// by shuffles, so a term costs a few FP64 instructions per lane.  FP64.
+__device__ __forceinline__ double2 shfl_down2(double2 v) {
+    return make_double2(__shfl_down_sync(0xFFFFFFFFu, v.x, 1), __shfl_down_sync(0xFFFFFFFFu, v.y, 1));
+}
+
+__device__ __forceinline__ double2 shfl_up2(double2 v) {
+    return make_double2(__shfl_up_sync(0xFFFFFFFFu, v.x, 1), __shfl_up_sync(0xFFFFFFFFu, v.y, 1));
+}
+
+__device__ __forceinline__ double warp_max(double v) {
+    for (int o = 16; o; o >>= 1) v = fmax(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+    return v;
+}
+
 __global__ void __launch_bounds__(32) k_tridiag_exp(KrylovState *st, int reverse) {
+    static_assert(kMaxKrylov <= 32, "one lane per Krylov vector");
     const int lane = threadIdx.x;
     const int n = st->iters;
     if (n <= 0) return;
-    double d[kMaxKrylov], e[kMaxKrylov], z[kMaxKrylov];
-    for (int i = 0; i < n; ++i) {
-        d[i] = st->alpha[i].x;
-        const double2 b = st->beta[i];
-        e[i] = (i + 1 < n) ? sqrt(b.x * b.x + b.y * b.y) : 0.0;
-        z[i] = (i == lane) ? 1.0 : 0.0;  // row `lane` of the eigenvector matrix
+    const bool on = lane < n;
+    const double a = on ? st->alpha[lane].x : 0.0;
+    const double2 zero = make_double2(0.0, 0.0);
+    const double2 bu = (lane + 1 < n) ? st->beta[lane] : zero;  // T[lane][lane + 1]
+    double2 bl = (on && lane >= 1) ? st->beta[lane - 1] : zero;  // T[lane][lane - 1] = conj(beta)
+    bl.y = -bl.y;
+    const double rs = warp_max(fabs(a) + sqrt(bu.x * bu.x + bu.y * bu.y) + sqrt(bl.x * bl.x + bl.y * bl.y));
+    if (!isfinite(rs)) {
+        if (on) st->coef[lane] = make_double2(nan(""), 0.0);
+        return;
     }
-    const double eps = 2.220446049250313e-16;
-    for (int l = 0; l < n; ++l) {
-        for (int iter = 0; iter < 64; ++iter) {
-            int m = l;
-            for (; m < n - 1; ++m)
-                if (fabs(e[m]) <= eps * (fabs(d[m]) + fabs(d[m + 1]))) break;
-            if (m == l) break;
-            // shift from the leading 2x2 block: the eigenvalue of it closer to d[l]
-            double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
-            double r = hypot(g, 1.0);
-            g = d[m] - d[l] + e[l] / (g + copysign(r, g));
-            double sn = 1.0, cs = 1.0, p = 0.0;
-            int i = m - 1;
-            for (; i >= l; --i) {
-                const double f = sn * e[i], b = cs * e[i];
-                r = hypot(f, g);
-                e[i + 1] = r;
-                if (r == 0.0) {  // split: the chase stops early
-                    d[i + 1] -= p;
-                    e[m] = 0.0;
-                    break;
-                }
-                sn = f / r;
-                cs = g / r;
-                g = d[i + 1] - p;
-                r = (d[i] - g) * sn + 2.0 * cs * b;
-                p = sn * r;
-                d[i + 1] = g + p;
-                g = cs * r - b;
-                const double zf = z[i + 1];
-                z[i + 1] = sn * z[i] + cs * zf;
-                z[i] = cs * z[i] - sn * zf;
-            }
-            if (r == 0.0 && i >= l) continue;
-            d[l] -= p;
-            e[l] = g;
-            e[m] = 0.0;
-        }
-    }
-    // p_lane: product of the off-diagonal phases above this row
-    double pr = 1.0, pi = 0.0;
-    for (int k = 0; k < lane && k + 1 < n; ++k) {
-        const double2 b = st->beta[k];
-        const double ab = sqrt(b.x * b.x + b.y * b.y);
-        if (ab > 0.0) {
-            const double cr = b.x / ab, ci = -b.y / ab;  // conj(beta_k)/|beta_k|
-            const double t = pr * cr - pi * ci;
-            pi = pr * ci + pi * cr;
-            pr = t;
-        }
-    }
+    const int m = max(1, (int)ceil(rs));
     const double sg = reverse ? 1.0 : -1.0;
-    double cr = 0.0, ci = 0.0;
-    for (int j = 0; j < n; ++j) {
-        const double z0 = __shfl_sync(0xFFFFFFFFu, z[j], 0);  // Z_S[0][j]
-        double sj, cj;
-        sincos(d[j], &sj, &cj);
-        const double w = z[j] * z0;
-        cr += w * cj;
-        ci += w * sg * sj;
+    double2 y = make_double2(lane == 0 ? 1.0 : 0.0, 0.0);
+    for (int step = 0; step < m; ++step) {
+        double2 term = y, acc = y;
+        for (int k = 1; k < 64; ++k) {
+            const double2 up = shfl_down2(term);  // component lane + 1 (bu = 0 past the end)
+            const double2 dn = shfl_up2(term);    // component lane - 1 (bl = 0 on lane 0)
+            const double tr = a * term.x + (bu.x * up.x - bu.y * up.y) + (bl.x * dn.x - bl.y * dn.y);
+            const double ti = a * term.y + (bu.x * up.y + bu.y * up.x) + (bl.x * dn.y + bl.y * dn.x);
+            const double f = sg / ((double)m * k);  // term <- i f T term
+            term = make_double2(-f * ti, f * tr);
+            acc.x += term.x;
+            acc.y += term.y;
+            const double tm = warp_max(fabs(term.x) + fabs(term.y));
+            const double am = warp_max(fabs(acc.x) + fabs(acc.y));
+            if (tm <= 1e-18 * am) break;
+        }
+        y = acc;
     }
-    if (lane < n) st->coef[lane] = make_double2(pr * cr - pi * ci, pr * ci + pi * cr);
+    if (on) st->coef[lane] = y;
 }
 
 __global__ void __launch_bounds__(KT) k_combine(const KrylovState *st, double2 *const *V, double2 *out,
