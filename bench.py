@@ -57,6 +57,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--compare-steps", type=int, default=20,
                     help="time steps of the mixed-vs-FP64 comparison leg (4-molecule chain)")
+    ap.add_argument("--chains", type=int, default=64,
+                    help=f"{BATCH_CONFIG}: members of the disordered ensemble advanced together")
+    ap.add_argument("--max-streams", type=int, default=0, help=f"{BATCH_CONFIG}: worker streams (0: library default)")
     ap.add_argument("--molecules", type=int, default=None,
                     help="shorter chain with the same local structure (profiling runs)")
     return ap.parse_args()
@@ -109,6 +112,9 @@ class Clocks:
         reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip() == "Active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(rows)}
+
+
+BATCH_CONFIG = "holstein-1site-batch64"
 
 
 def peaks():
@@ -357,10 +363,65 @@ def compare_fp64(args, G):
             "energy_fp64": float(obs[G.KV_FP64][1])}
 
 
+def run_batched(args):
+    """The batched ensemble: --chains members of the disordered ensemble
+    (holstein.disordered_chain: L in [8, 48], D in {32, 64, 128, 256},
+    eps ~ N(0, 0.5^2), omega = 1, g in [0.5, 1.5], cutoff 8), one-site TDVP at
+    dt = 0.05, advanced together by kv_sweep_batched.  The same chains advanced
+    one after another by kv_tdvp_sweep are timed beside it."""
+    import __graft_entry__ as ge
+
+    ge.load_package()
+    from kylin_v_gb300 import holstein as H
+    from kylin_v_gb300 import kvgpu as G
+
+    G.init(0)
+    prec = G.KV_MIXED_TF32 if args.precision == "mixed" else G.KV_FP64
+    members = [H.disordered_chain(i) for i in range(args.chains)]
+    host = [(H.random_mps(ch, D, seed=1234 + i), H.hamiltonian_mpo(ch), D) for i, (ch, D) in enumerate(members)]
+
+    def make():
+        return [G.TDVP([G.Tensor.from_host(x) for x in m], [G.Tensor.from_host(x) for x in w], 1e-8, 1e-8, D, 11,
+                       0.05, prec) for m, w, D in host]
+
+    bat, seq = make(), make()
+    G.sweep_batched(bat, 1, args.warmup, args.max_streams)
+    for t in seq:
+        for _ in range(args.warmup):
+            t.one_site()
+    n0 = G.launches()
+    bat_ms, flops = 0.0, 0.0
+    t0 = time.perf_counter()
+    with Clocks(0) as clk:
+        for _ in range(args.steps):
+            bat_ms += G.sweep_batched(bat, 1, 1, args.max_streams)
+            flops += sum(t.stats()["ref_flops"] for t in bat)
+    wall = time.perf_counter() - t0
+    launches = G.launches() - n0
+    seq_ms = 0.0
+    for _ in range(args.steps):
+        for t in seq:
+            t.one_site()
+            seq_ms += t.stats()["sweep_ms"]
+    line = {"metric": METRIC, "value": flops / (bat_ms / 1e3) / 1e12, "unit": "TFLOP/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": bat_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128" if not prec else "mixed (as the main workload)",
+            "data": "synthetic (seeded disordered ensemble, random right-canonical U(1) MPS)",
+            "config": {"workload": BATCH_CONFIG, "chains": args.chains, "mode": "1-site TDVP", "dt": 0.05,
+                       "max_iter": 11, "precision": args.precision, "max_streams": args.max_streams or 8,
+                       "sites": sum(ch.n_sites for ch, _ in members), "D": [D for _, D in members]},
+            "wall_ms_per_step": 1e3 * wall / args.steps,
+            "sequential_ms_per_step": seq_ms / args.steps, "batch_speedup": seq_ms / max(1e-9, bat_ms),
+            "gpu_launches": launches, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.config == BATCH_CONFIG:
+        run_batched(args)
     else:
         run_ours(args)
 

@@ -42,10 +42,16 @@ extern "C" {
 
 /* ------------------------------------------------------- arithmetic modes */
 /* KV_FP64: every contraction in complex128 on the CUDA cores.
- * KV_MIXED_TF32: block contractions as 3M (Gauss) real GEMMs on the tcgen05
- *   tensor cores with TF32 hi/lo split operands (hi*hi + hi*lo + lo*hi) and
- *   FP32 accumulation in tensor memory; Lanczos, norms, the tridiagonal
- *   exponential, MPO mixing and SVD stay FP64. */
+ * KV_MIXED_TF32 (the mixed-precision path; the name is kept from the API's
+ *   first form): block contractions as 3M (Gauss) real products on the
+ *   tcgen05 tensor cores.  Each operand is rounded to 30-bit fixed point
+ *   against a per-row (A) or per-column (B) power of two and split into four
+ *   balanced 8-bit digits, held exactly in FP16; the digit products of orders
+ *   0-4 accumulate exactly in FP32 tensor memory and are combined in int64,
+ *   so a product carries about 2^-29 relative error per operand, below a
+ *   TF32 or BF16x3 split.  Lanczos, norms, the tridiagonal exponential and
+ *   MPO mixing stay FP64; the SVD picks the kept subspace with FP32 Jacobi
+ *   and rebuilds the kept factors in FP64 (Cholesky-QR, exact projection). */
 #define KV_FP64        0
 #define KV_MIXED_TF32  1
 /* one part mixed, the other FP64 (to attribute mixed-precision error):
@@ -94,6 +100,22 @@ int kv_heff_apply(int nsite, kv_tensor L, kv_tensor psi, kv_tensor W1, kv_tensor
 
 /* Environment update env_sweep(env, A, W, l2r) (holstein/product.h:488-503). */
 int kv_env_update(int l2r, kv_tensor env, kv_tensor A, kv_tensor W, int precision, kv_tensor *out);
+/* Adjoints (vector-Jacobian products).  No reference counterpart: the
+ * reference has no derivative code.  For a real loss l, a cotangent is
+ * xbar = dl/dRe(x) + i dl/dIm(x) (so dl = Re<ybar, dy>, and for y linear in x,
+ * xbar = (dy/dx)^H ybar).  kv_adjoint_heff: given ybar for
+ * y = kv_heff_apply(nsite, L, psi, W1, W2, R, scale), returns the cotangents
+ * of psi, L, W1, W2 (two-site only) and R; pass NULL for any not wanted.
+ * kv_adjoint_env: given the cotangent of out = kv_env_update(l2r, env, A, W),
+ * returns those of env, A (through both its bra and ket use) and W.  Each
+ * cotangent tensor holds every charge block the contraction reaches, which
+ * can be more blocks than the primal tensor has; only the primal's blocks
+ * pair with a perturbation of it.  The contractions run in `precision`. */
+int kv_adjoint_heff(int nsite, kv_tensor L, kv_tensor psi, kv_tensor W1, kv_tensor W2, kv_tensor R, double scale,
+                    kv_tensor ybar, int precision, kv_tensor *psi_bar, kv_tensor *L_bar, kv_tensor *W1_bar,
+                    kv_tensor *W2_bar, kv_tensor *R_bar);
+int kv_adjoint_env(int l2r, kv_tensor env, kv_tensor A, kv_tensor W, kv_tensor out_bar, int precision,
+                   kv_tensor *env_bar, kv_tensor *A_bar, kv_tensor *W_bar);
 
 /* local_krylov<Rank> (holstein/exponential.h:92-190): psi <- exp(-+i H_eff dt/2) psi
  * (normalised first), Lanczos while k < max_iter-1 and the product of Lanczos
@@ -140,6 +162,22 @@ int kv_tdvp_stats(kv_tdvp s, double *module_ms, double *sweep_ms, double *ref_fl
 int kv_tdvp_host_stats(kv_tdvp s, double *module_host_ms, double *sweep_host_ms, long long *plans_built,
                        double *plan_ms);
 int kv_tdvp_free(kv_tdvp s);
+/* Advances n_chains independent chains (kv_tdvp handles, each created with
+ * kv_tdvp_create) by `steps` time steps of `mode` (1 = one_site, 2 =
+ * two_site).  No reference counterpart: the reference runs one chain per
+ * process (src/kln-tdvp.cpp:73-78).  It replaces a loop of kv_tdvp_sweep
+ * calls over the chains and leaves the same site tensors, bit for bit.  The
+ * chains are spread over up to max_streams worker threads (<= 0: 8), each
+ * with its own CUDA stream, staging ring and H_eff plan cache, so kernels of
+ * different chains run concurrently on the GPU; chains go to workers longest
+ * first by an estimate of their work, so the same set of chains is split the
+ * same way on every call and finds its plans cached.  Returns when all chains
+ * are done; device_ms (may be NULL) receives the device time from the first
+ * launch to the last.  A failing chain does not stop the others: the first
+ * failure's status is returned, kv_last_error names the chain, and that
+ * chain's state is undefined.  Call from the thread that called kv_init;
+ * the handles must not be used by another call meanwhile. */
+int kv_sweep_batched(int n_chains, const kv_tdvp *chains, int mode, int steps, int max_streams, double *device_ms);
 
 /* ------------------------------------------------------ instrumentation */
 /* No reference counterpart (the reference only has its Timer table).

@@ -1,8 +1,14 @@
 // C ABI of libkvgpu (include/kvgpu.h).  Every entry point converts C++
 // exceptions into status codes; nothing here exits the process.
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <set>
+#include <string>
+#include <thread>
+#include <vector>
 
 #include "kv_engine.h"
 
@@ -50,7 +56,45 @@ void sync() {
     const int st = kv::mixed_gemm_status();
     KV_REQUIRE(st == KV_OK, st, "a tensor-core GEMM wait timed out");
 }
+
+// Worker contexts of kv_sweep_batched, kept between calls so their plan
+// caches stay warm; closed by kv_shutdown.
+std::vector<std::unique_ptr<kv::Context>> g_workers;
+constexpr int kDefaultBatchStreams = 8;
+
+void close_workers() {
+    for (auto &w : g_workers) kv::context_close(*w);
+    g_workers.clear();
+}
 }  // namespace
+
+namespace kv {
+void context_open(Context &c, int device) {
+    KV_CUDA(cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, device));
+    KV_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+    KV_CUDA(cudaHostAlloc((void **)&c.ring, (size_t)Context::kRingChunks * Context::kRingChunk, cudaHostAllocDefault));
+    for (auto &e : c.ring_ev) KV_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    c.device = device;
+}
+
+void context_close(Context &c) {
+    if (c.device < 0) return;
+    KV_CUDA(cudaStreamSynchronize(c.stream));
+    Context *prev = &ctx();
+    bind_thread_context(&c);  // plans free their buffers on their own stream
+    clear_plan_cache();
+    bind_thread_context(prev == &main_ctx() ? nullptr : prev);
+    for (auto &e : c.ring_ev) cudaEventDestroy(e);
+    cudaFreeHost(c.ring);
+    c.ring = nullptr;
+    for (auto &e : c.ev_free) cudaEventDestroy(e);
+    c.ev_free.clear();
+    KV_CUDA(cudaStreamSynchronize(c.stream));
+    KV_CUDA(cudaStreamDestroy(c.stream));
+    c.stream = nullptr;
+    c.device = -1;
+}
+}  // namespace kv
 
 extern "C" {
 
@@ -60,40 +104,27 @@ const char *kv_last_error(void) { return g_err.c_str(); }
 
 int kv_init(int device) {
     return guard([&] {
-        auto &c = kv::ctx();
+        auto &c = kv::main_ctx();
         if (c.device == device && c.stream) return;
         KV_REQUIRE(c.device < 0, KV_EINVAL, "kv_init already called for another device");
         int n = 0;
         KV_CUDA(cudaGetDeviceCount(&n));
         KV_REQUIRE(device >= 0 && device < n, KV_EINVAL, "no such CUDA device");
         KV_CUDA(cudaSetDevice(device));
-        KV_CUDA(cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, device));
-        KV_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
         cudaMemPool_t pool;
         KV_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
         uint64_t thr = ~0ull;  // keep freed blocks cached in the pool
         KV_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
-        KV_CUDA(cudaHostAlloc((void **)&c.ring, (size_t)kv::Context::kRingChunks * kv::Context::kRingChunk,
-                              cudaHostAllocDefault));
-        for (auto &e : c.ring_ev) KV_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-        c.device = device;
+        kv::context_open(c, device);
     });
 }
 
 int kv_shutdown(void) {
     return guard([&] {
-        auto &c = kv::ctx();
+        auto &c = kv::main_ctx();
         if (c.device < 0) return;
-        KV_CUDA(cudaStreamSynchronize(c.stream));
-        kv::clear_plan_cache();
-        for (auto &e : c.ring_ev) cudaEventDestroy(e);
-        cudaFreeHost(c.ring);
-        c.ring = nullptr;
-        for (auto &e : c.ev_free) cudaEventDestroy(e);
-        c.ev_free.clear();
-        KV_CUDA(cudaStreamDestroy(c.stream));
-        c.stream = nullptr;
-        c.device = -1;
+        close_workers();
+        kv::context_close(c);
     });
 }
 
@@ -152,6 +183,48 @@ int kv_env_update(int l2r, kv_tensor env, kv_tensor A, kv_tensor W, int precisio
         kv::require_init();
         *out = wrap(kv::op_env(l2r != 0, *T(env), *T(A), *T(W), nullptr, precision, nullptr));
         sync();
+    });
+}
+
+int kv_adjoint_heff(int nsite, kv_tensor L, kv_tensor psi, kv_tensor W1, kv_tensor W2, kv_tensor R, double scale,
+                    kv_tensor ybar, int precision, kv_tensor *psi_bar, kv_tensor *L_bar, kv_tensor *W1_bar,
+                    kv_tensor *W2_bar, kv_tensor *R_bar) {
+    return guard([&] {
+        kv::require_init();
+        KV_REQUIRE(nsite >= 0 && nsite <= 2, KV_EINVAL, "nsite must be 0, 1 or 2");
+        KV_REQUIRE(nsite < 1 || Topt(W1), KV_EINVAL, "W1 required");
+        KV_REQUIRE(nsite < 2 || Topt(W2), KV_EINVAL, "W2 required");
+        KV_REQUIRE(nsite >= 1 || !W1_bar, KV_EINVAL, "no W1 in the zero-site H_eff");
+        KV_REQUIRE(nsite == 2 || !W2_bar, KV_EINVAL, "W2 is only in the two-site H_eff");
+        unsigned want = (psi_bar ? kv::kGradPsi : 0u) | (L_bar ? kv::kGradL : 0u) | (W1_bar ? kv::kGradW1 : 0u) |
+                        (W2_bar ? kv::kGradW2 : 0u) | (R_bar ? kv::kGradR : 0u);
+        T(L);
+        T(psi);
+        T(R);
+        kv::HeffGrads g = kv::op_adjoint_heff(nsite, L->t, psi->t, nsite >= 1 ? W1->t : nullptr,
+                                              nsite == 2 ? W2->t : nullptr, R->t, scale, *T(ybar), precision, want);
+        sync();
+        if (psi_bar) *psi_bar = wrap(g.psi);
+        if (L_bar) *L_bar = wrap(g.L);
+        if (W1_bar) *W1_bar = wrap(g.W1);
+        if (W2_bar) *W2_bar = wrap(g.W2);
+        if (R_bar) *R_bar = wrap(g.R);
+    });
+}
+
+int kv_adjoint_env(int l2r, kv_tensor env, kv_tensor A, kv_tensor W, kv_tensor env_out_bar, int precision,
+                   kv_tensor *env_bar, kv_tensor *A_bar, kv_tensor *W_bar) {
+    return guard([&] {
+        kv::require_init();
+        unsigned want = (env_bar ? kv::kGradEnv : 0u) | (A_bar ? kv::kGradA : 0u) | (W_bar ? kv::kGradW : 0u);
+        T(env);
+        T(A);
+        T(W);
+        kv::EnvGrads g = kv::op_adjoint_env(l2r != 0, env->t, A->t, W->t, *T(env_out_bar), precision, want);
+        sync();
+        if (env_bar) *env_bar = wrap(g.env);
+        if (A_bar) *A_bar = wrap(g.A);
+        if (W_bar) *W_bar = wrap(g.W);
     });
 }
 
@@ -218,6 +291,98 @@ int kv_tdvp_sweep(kv_tdvp s, int mode) {
         if (mode == 1) s->s->one_site();
         else if (mode == 2) s->s->two_site();
         else throw kv::Error(KV_EINVAL, "mode must be 1 or 2");
+    });
+}
+
+int kv_sweep_batched(int n_chains, const kv_tdvp *chains, int mode, int steps, int max_streams, double *device_ms) {
+    return guard([&] {
+        kv::require_init();
+        KV_REQUIRE(n_chains >= 0 && (n_chains == 0 || chains), KV_EINVAL, "null chain array");
+        KV_REQUIRE(mode == 1 || mode == 2, KV_EINVAL, "mode must be 1 or 2");
+        KV_REQUIRE(steps >= 0, KV_EINVAL, "steps must be >= 0");
+        std::set<const kv_tdvp_s *> seen;
+        for (int i = 0; i < n_chains; ++i) {
+            KV_REQUIRE(chains[i] && chains[i]->s, KV_EINVAL, "null TDVP handle");
+            KV_REQUIRE(seen.insert(chains[i]).second, KV_EINVAL, "a chain appears twice");
+        }
+        if (device_ms) *device_ms = 0.0;
+        if (n_chains == 0 || steps == 0) return;
+        auto &m = kv::main_ctx();
+        KV_REQUIRE(&kv::ctx() == &m, KV_EINVAL, "kv_sweep_batched called from a worker");
+        const int nw = std::min(n_chains, max_streams > 0 ? max_streams : kDefaultBatchStreams);
+        while ((int)g_workers.size() < nw) {
+            auto w = std::make_unique<kv::Context>();
+            kv::context_open(*w, m.device);
+            g_workers.push_back(std::move(w));
+        }
+        // Longest first, each chain to the least-loaded worker, by an estimate
+        // of its work (sum over sites of |A|^1.5); deterministic, so a chain
+        // returns to the same worker and finds its H_eff plans cached there.
+        std::vector<double> cost(n_chains, 0.0);
+        for (int i = 0; i < n_chains; ++i)
+            for (auto &a : chains[i]->s->mps) cost[i] += std::pow((double)a->meta.nelem, 1.5);
+        std::vector<int> order(n_chains);
+        for (int i = 0; i < n_chains; ++i) order[i] = i;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+        std::vector<std::vector<int>> assign(nw);
+        std::vector<double> load(nw, 0.0);
+        for (int i : order) {
+            const int w = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+            assign[w].push_back(i);
+            load[w] += cost[i];
+        }
+        // every worker stream starts after everything on the main stream
+        cudaEvent_t t0 = kv::prof_event(), t1 = kv::prof_event();
+        KV_CUDA(cudaEventRecord(t0, m.stream));
+        std::vector<cudaEvent_t> done(nw);
+        for (auto &e : done) KV_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        std::vector<int> code(n_chains, KV_OK), wcode(nw, KV_OK);
+        std::vector<std::string> msg(n_chains), wmsg(nw);
+        std::vector<std::thread> th;
+        for (int w = 0; w < nw; ++w)
+            th.emplace_back([&, w] {
+                kv::Context *c = g_workers[w].get();
+                wcode[w] = guard([&] {
+                    KV_CUDA(cudaSetDevice(c->device));
+                    KV_CUDA(cudaStreamWaitEvent(c->stream, t0, 0));
+                });
+                if (wcode[w] != KV_OK) {
+                    wmsg[w] = g_err;
+                    return;
+                }
+                kv::bind_thread_context(c);
+                for (int i : assign[w]) {
+                    kv::Tdvp &t = *chains[i]->s;
+                    code[i] = guard([&] {
+                        for (int s = 0; s < steps; ++s) mode == 1 ? t.one_site() : t.two_site();
+                    });
+                    if (code[i] != KV_OK) msg[i] = g_err;
+                }
+                wcode[w] = guard([&] {
+                    KV_CUDA(cudaEventRecord(done[w], c->stream));
+                    KV_CUDA(cudaStreamSynchronize(c->stream));
+                });
+                if (wcode[w] != KV_OK) wmsg[w] = g_err;
+                kv::bind_thread_context(nullptr);
+            });
+        for (auto &t : th) t.join();
+        for (int w = 0; w < nw; ++w) {
+            m.launches += g_workers[w]->launches;
+            g_workers[w]->launches = 0;
+            if (wcode[w] == KV_OK) KV_CUDA(cudaStreamWaitEvent(m.stream, done[w], 0));
+        }
+        KV_CUDA(cudaEventRecord(t1, m.stream));
+        sync();
+        float ms = 0.0f;
+        KV_CUDA(cudaEventElapsedTime(&ms, t0, t1));
+        if (device_ms) *device_ms = ms;
+        for (auto &e : done) cudaEventDestroy(e);
+        m.ev_free.push_back(t0);
+        m.ev_free.push_back(t1);
+        for (int w = 0; w < nw; ++w)
+            KV_REQUIRE(wcode[w] == KV_OK, wcode[w], "batched sweep, stream " + std::to_string(w) + ": " + wmsg[w]);
+        for (int i = 0; i < n_chains; ++i)
+            KV_REQUIRE(code[i] == KV_OK, code[i], "batched sweep, chain " + std::to_string(i) + ": " + msg[i]);
     });
 }
 

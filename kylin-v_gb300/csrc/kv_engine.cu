@@ -22,7 +22,10 @@ namespace kv {
 
 // ================================================================ runtime
 static Context g_ctx;
-Context &ctx() { return g_ctx; }
+thread_local Context *t_ctx = nullptr;
+Context &ctx() { return t_ctx ? *t_ctx : g_ctx; }
+Context &main_ctx() { return g_ctx; }
+void bind_thread_context(Context *c) { t_ctx = c; }
 void require_init() { KV_REQUIRE(g_ctx.device >= 0, KV_ENOTINIT, "kv_init has not been called"); }
 
 void DevBuf::alloc(size_t b) {
@@ -591,17 +594,23 @@ struct VecHash {
         return (size_t)h;
     }
 };
-std::unordered_map<std::vector<int>, std::shared_ptr<HeffPlan>, VecHash> g_plan_cache;
 constexpr size_t kPlanCacheMax = 16384;
-long long g_plans_built = 0;
-double g_plan_ms = 0.0;
 }  // namespace
 
-void clear_plan_cache() { g_plan_cache.clear(); }
+// Plans hold device buffers uploaded on their context's stream, so each
+// context keeps its own cache and no plan is read on another stream.
+struct PlanCache {
+    std::unordered_map<std::vector<int>, std::shared_ptr<HeffPlan>, VecHash> map;
+};
+
+void clear_plan_cache() {
+    delete ctx().plans;
+    ctx().plans = nullptr;
+}
 
 void plan_stats(long long *built, double *ms) {
-    *built = g_plans_built;
-    *ms = g_plan_ms;
+    *built = ctx().plans_built;
+    *ms = ctx().plan_ms;
 }
 
 std::shared_ptr<HeffPlan> get_heff_plan(int nsite, const Meta &L, const Meta &psi, const Meta *W1, const Meta *W2,
@@ -612,14 +621,17 @@ std::shared_ptr<HeffPlan> get_heff_plan(int nsite, const Meta &L, const Meta &ps
     key_meta(key, W1);
     key_meta(key, W2);
     key_meta(key, &R);
-    auto it = g_plan_cache.find(key);
-    if (it != g_plan_cache.end()) return it->second;
-    if (g_plan_cache.size() >= kPlanCacheMax) g_plan_cache.clear();
+    Context &c = ctx();
+    if (!c.plans) c.plans = new PlanCache;
+    auto &cache = c.plans->map;
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+    if (cache.size() >= kPlanCacheMax) cache.clear();
     const auto t0 = std::chrono::steady_clock::now();
     auto p = std::make_shared<HeffPlan>(plan_heff(nsite, L, psi, W1, W2, R, precision, max_iter));
-    ++g_plans_built;
-    g_plan_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    g_plan_cache.emplace(std::move(key), p);
+    ++c.plans_built;
+    c.plan_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    cache.emplace(std::move(key), p);
     return p;
 }
 

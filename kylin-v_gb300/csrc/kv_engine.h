@@ -86,6 +86,21 @@ cplx op_expectation(const std::vector<DTensor *> &a, const std::vector<DTensor *
 cplx expectation_noalloc(const std::vector<DTensor *> &bra, const std::vector<DTensor *> &w,
                          const std::vector<DTensor *> &ket);
 
+// Adjoints of the H_eff apply and the environment update (kv_adjoint.cu):
+// the cotangents selected by `want` (a mask of the kGrad* bits)
+enum : unsigned { kGradPsi = 1, kGradL = 2, kGradW1 = 4, kGradW2 = 8, kGradR = 16 };
+enum : unsigned { kGradEnv = 1, kGradA = 2, kGradW = 4 };
+struct HeffGrads {
+    TensorP psi, L, W1, W2, R;
+};
+struct EnvGrads {
+    TensorP env, A, W;
+};
+HeffGrads op_adjoint_heff(int nsite, const TensorP &L, const TensorP &psi, const TensorP &W1, const TensorP &W2,
+                          const TensorP &R, double scale, const DTensor &ybar, int precision, unsigned want);
+EnvGrads op_adjoint_env(bool l2r, const TensorP &env, const TensorP &A, const TensorP &W, const DTensor &ebar,
+                        int precision, unsigned want);
+
 enum Module { MOD_EVL0 = 0, MOD_EVL1, MOD_EVL2, MOD_SVD, MOD_UPDATE, MOD_SWEEP, MOD_COUNT };
 
 class Tdvp {

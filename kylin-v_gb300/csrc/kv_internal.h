@@ -51,6 +51,12 @@ struct ProfRec {
     int k;
 };
 
+struct PlanCache;  // H_eff plans keyed by block structure (kv_engine.cu)
+
+// Device, stream and host staging of one host thread's work.  The calling
+// thread uses the library's main context; kv_sweep_batched binds a worker
+// context (its own stream, staging ring and plan cache) to each of its
+// threads, so chains advance on concurrent streams.
 struct Context {
     int device = -1;
     int num_sms = 0;
@@ -69,8 +75,17 @@ struct Context {
     size_t ring_used = 0;
     cudaEvent_t ring_ev[kRingChunks] = {};
     bool ring_live[kRingChunks] = {};
+    PlanCache *plans = nullptr;
+    long long plans_built = 0;  // plan-cache misses
+    double plan_ms = 0.0;       // host ms spent building those plans
 };
+// the calling thread's context: its bound worker context, else the main one
 Context &ctx();
+Context &main_ctx();
+void bind_thread_context(Context *c);
+// create / destroy a context's stream, staging ring and plan cache
+void context_open(Context &c, int device);
+void context_close(Context &c);
 void require_init();
 inline void counted(int n = 1) { ctx().launches += n; }
 cudaEvent_t prof_event();

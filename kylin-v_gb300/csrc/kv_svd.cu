@@ -7,6 +7,7 @@
 // descending singular value.  The host applies the reference's global
 // truncation and the scatter kernel writes the kept columns into the U and
 // S.V^H block tensors.
+#include <mutex>
 #include "kv_internal.h"
 #include "kv_jacobi.cuh"
 #include "kv_svd.h"
@@ -456,13 +457,17 @@ void svd_scatter(const std::vector<SvdScatter> &sc, const SvdPlan &p, const doub
 
 void svd_jacobi_f32(const SvdPlan &p, const double2 *T64, float2 *T, int *status, int max_sweeps, float tol) {
     if (p.secs.empty()) return;
-    static int smem_bytes = 0;  // dynamic shared memory: opt-in maximum less the static arrays and 4 KB
-    if (!smem_bytes) {
+    // dynamic shared memory: opt-in maximum less the static arrays and 4 KB
+    // (set once; kv_sweep_batched runs this from several threads)
+    static int smem_bytes = 0;
+    static std::once_flag once;
+    std::call_once(once, [] {
         int optin = 0;
         KV_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx().device));
-        smem_bytes = std::max(0, optin - 4096 - (int)sizeof(float) * kJacobiMaxQ);
-        KV_CUDA(cudaFuncSetAttribute(k_svd_jacobi_w<1024, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
-    }
+        const int bytes = std::max(0, optin - 4096 - (int)sizeof(float) * kJacobiMaxQ);
+        KV_CUDA(cudaFuncSetAttribute(k_svd_jacobi_w<1024, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        smem_bytes = bytes;
+    });
     int64_t max_pq = 0;
     for (auto &s : p.secs) {
         KV_REQUIRE(s.q <= kJacobiMaxQ, KV_EINVAL, "mixed-precision SVD: a sector has more than 2048 columns");
@@ -504,12 +509,12 @@ void svd_trsm(const DevBuf &pol, const std::vector<int> &item_pol, const std::ve
               const double2 *G, double2 *X, int kmax) {
     if (item_pol.empty()) return;
     const size_t smem = (size_t)kTrsmRows * std::max(1, kmax) * sizeof(double2);
-    KV_REQUIRE(smem <= 200 * 1024, KV_EINVAL, "SVD polish: kept dimension of one sector too large");
-    static size_t attr = 0;
-    if (smem > 48 * 1024 && smem > attr) {
-        KV_CUDA(cudaFuncSetAttribute(k_trsm_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr = smem;
-    }
+    constexpr int kTrsmSmemMax = 200 * 1024;
+    KV_REQUIRE(smem <= kTrsmSmemMax, KV_EINVAL, "SVD polish: kept dimension of one sector too large");
+    static std::once_flag once;  // the limit is raised once, to the largest size allowed here
+    std::call_once(once, [] {
+        KV_CUDA(cudaFuncSetAttribute(k_trsm_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrsmSmemMax));
+    });
     DevBuf ip = upload_vec(item_pol), ir = upload_vec(item_row0);
     k_trsm_rows<<<(unsigned)item_pol.size(), 32 * kTrsmRows, smem, ctx().stream>>>(pol.as<SvdPolish>(), ip.as<int>(),
                                                                                   ir.as<int>(), G, X);

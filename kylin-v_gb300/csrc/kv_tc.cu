@@ -43,6 +43,7 @@
 // taking half of the tile's columns).
 // Every mbarrier wait is bounded; on timeout the CTA records an error, waits
 // (bounded) for its copies and MMAs in flight, frees tensor memory and exits.
+#include <mutex>
 #include <cuda_fp16.h>
 
 #include <cstdint>
@@ -501,7 +502,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_gemm_tc(const GemmTile *__restr
 }
 
 int *g_err = nullptr;
-bool g_attr = false;
+std::once_flag g_attr;
 
 }  // namespace
 
@@ -590,12 +591,13 @@ void launch_gemm_mixed(const GemmPlan &p, const double2 *A, const double2 *B, do
     KV_REQUIRE(p.tile_m == BM && p.tile_n == BN && p.xsegs.size() == p.segs.size(), KV_EINVAL,
                "internal: GEMM plan not prepared for the tensor-core path");
     auto &c = ctx();
-    if (!g_attr) {
+    std::call_once(g_attr, [] {  // once, also when several threads launch
         KV_CUDA(cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-        KV_CUDA(cudaMalloc(&g_err, sizeof(int)));
-        KV_CUDA(cudaMemset(g_err, 0, sizeof(int)));
-        g_attr = true;
-    }
+        int *e = nullptr;
+        KV_CUDA(cudaMalloc(&e, sizeof(int)));
+        KV_CUDA(cudaMemset(e, 0, sizeof(int)));
+        g_err = e;
+    });
     DevBuf ap(std::max<int64_t>(1, p.a_planes) * sizeof(__half)), bp(std::max<int64_t>(1, p.b_planes) * sizeof(__half));
     DevBuf ae(std::max<int64_t>(1, p.a_exps) * sizeof(int)), be(std::max<int64_t>(1, p.b_exps) * sizeof(int));
     int n = 0;

@@ -28,7 +28,7 @@ EXPORTS = (
     "kv_tensor_download", "kv_tensor_free", "kv_product", "kv_heff_apply", "kv_env_update", "kv_lanczos_expm",
     "kv_svd_truncate", "kv_tdvp_create", "kv_tdvp_sweep", "kv_tdvp_site", "kv_tdvp_stats", "kv_tdvp_free",
     "kv_expectation", "kv_profile", "kv_profile_read", "kv_counters", "kv_expectation_noalloc",
-    "kv_tdvp_host_stats", "kv_canonicalize",
+    "kv_tdvp_host_stats", "kv_canonicalize", "kv_sweep_batched", "kv_adjoint_heff", "kv_adjoint_env",
 )
 
 
@@ -78,6 +78,10 @@ def lib():
         L.kv_expectation.argtypes = [ctypes.c_int, pvp, pvp, pvp, dp, dp]
         L.kv_canonicalize.argtypes = [ctypes.c_int, pvp, ctypes.c_double, ctypes.c_int, ctypes.c_int, pvp]
         L.kv_expectation_noalloc.argtypes = [ctypes.c_int, pvp, pvp, pvp, dp, dp]
+        L.kv_sweep_batched.argtypes = [ctypes.c_int, pvp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
+        L.kv_adjoint_heff.argtypes = [ctypes.c_int, vp, vp, vp, vp, vp, ctypes.c_double, vp, ctypes.c_int,
+                                      pvp, pvp, pvp, pvp, pvp]
+        L.kv_adjoint_env.argtypes = [ctypes.c_int, vp, vp, vp, vp, ctypes.c_int, pvp, pvp, pvp]
         _lib = L
     return _lib
 
@@ -187,6 +191,29 @@ def env_sweep(env, A, W, left2right, precision=KV_FP64) -> Tensor:
     out = ctypes.c_void_p()
     check(lib().kv_env_update(int(left2right), env.ptr, A.ptr, W.ptr, precision, ctypes.byref(out)))
     return Tensor(out.value)
+
+
+HEFF_GRADS = ("psi", "L", "W1", "W2", "R")
+
+
+def adjoint_heff(nsite, L, psi, W1, W2, R, ybar, scale=1.0, precision=KV_FP64, want=HEFF_GRADS) -> dict:
+    """Cotangents of heff_apply's operands for the output cotangent ybar
+    (kv_adjoint_heff); `want` names the ones to compute."""
+    hs = [_t(x) for x in (L, psi, W1, W2, R, ybar)]
+    present = {"psi": True, "L": True, "W1": nsite >= 1, "W2": nsite == 2, "R": True}
+    outs = {k: ctypes.c_void_p() for k in HEFF_GRADS if k in want and present[k]}
+    refs = [ctypes.byref(outs[k]) if k in outs else None for k in HEFF_GRADS]
+    check(lib().kv_adjoint_heff(nsite, *[_p(h) for h in hs[:5]], scale, hs[5].ptr, precision, *refs))
+    return {k: Tensor(v.value) for k, v in outs.items()}
+
+
+def adjoint_env(env, A, W, left2right, out_bar, precision=KV_FP64, want=("env", "A", "W")) -> dict:
+    """Cotangents of env_sweep's operands for the output cotangent out_bar (kv_adjoint_env)."""
+    env, A, W, ob = _t(env), _t(A), _t(W), _t(out_bar)
+    outs = {k: ctypes.c_void_p() for k in ("env", "A", "W") if k in want}
+    refs = [ctypes.byref(outs[k]) if k in outs else None for k in ("env", "A", "W")]
+    check(lib().kv_adjoint_env(int(left2right), env.ptr, A.ptr, W.ptr, ob.ptr, precision, *refs))
+    return {k: Tensor(v.value) for k, v in outs.items()}
 
 
 def local_krylov(nsite, L, psi, W1, W2, R, dt, max_iter, tol, reverse=False, precision=KV_FP64):
@@ -310,3 +337,13 @@ class TDVP:
         if getattr(self, "ptr", None) and _lib is not None:
             _lib.kv_tdvp_free(self.ptr)
             self.ptr = None
+
+
+def sweep_batched(chains, mode: int, steps: int = 1, max_streams: int = 0) -> float:
+    """Advance independent chains (TDVP objects) by `steps` time steps of
+    `mode` concurrently (kv_sweep_batched); returns the device ms."""
+    n = len(chains)
+    arr = (ctypes.c_void_p * max(1, n))(*[c.ptr for c in chains])
+    ms = ctypes.c_double()
+    check(lib().kv_sweep_batched(n, arr, mode, steps, max_streams, ctypes.byref(ms)))
+    return ms.value
