@@ -645,7 +645,7 @@ int kvo_tensor_new(int rank, const int *dirs, int nblocks, const int *shapes, co
             blk.rank = rank;
             for (int i = 0; i < rank; ++i) { blk.shape[i] = shapes[b * rank + i]; blk.qn[i] = qns[b * rank + i]; }
             blk.data.resize(blk.size());
-            std::memcpy(blk.data.data(), data + 2 * off, blk.size() * sizeof(cplx));
+            for (size_t e = 0; e < blk.size(); ++e) blk.data[e] = cplx(data[2 * (off + e)], data[2 * (off + e) + 1]);
             off += blk.size();
             t->blocks.push_back(std::move(blk));
         }
