@@ -144,7 +144,13 @@ int kv_svd_truncate(kv_tensor A, int r1, int l2r, double tol, int max_dim, int p
 int kv_tdvp_create(int nsites, const kv_tensor *mps, const kv_tensor *mpo, double tol_svd, double tol_exp,
                    int max_dim, int max_iter, double dt, int precision, kv_tdvp *out);
 /* One time step: mode 1 = TDVP::one_site (holstein/tdvp.h:78-141),
- * mode 2 = TDVP::two_site (holstein/tdvp.h:144-227). */
+ * mode 2 = TDVP::two_site (holstein/tdvp.h:144-227), mode 0 = one step of
+ * total_start's global-Krylov stage (holstein/tdvp.h:318-327, global_main in
+ * holstein/krylov.h:199-283: a Krylov basis of whole MPSs, the MPO scaled by
+ * dt, tolExp / maxIter / tolSVD / maxDim as given); after it the sweep
+ * environments are rebuilt from the new state (the reference keeps the ones
+ * built before that stage, so its next sweep mixes two states).  The global
+ * step's contractions run in `precision`, its SVDs in FP64. */
 int kv_tdvp_sweep(kv_tdvp s, int mode);
 /* New handle with a copy of the current site tensor i. */
 int kv_tdvp_site(kv_tdvp s, int i, kv_tensor *out);
@@ -163,9 +169,9 @@ int kv_tdvp_host_stats(kv_tdvp s, double *module_host_ms, double *sweep_host_ms,
                        double *plan_ms);
 int kv_tdvp_free(kv_tdvp s);
 /* Advances n_chains independent chains (kv_tdvp handles, each created with
- * kv_tdvp_create) by `steps` time steps of `mode` (1 = one_site, 2 =
- * two_site).  No reference counterpart: the reference runs one chain per
- * process (src/kln-tdvp.cpp:73-78).  It replaces a loop of kv_tdvp_sweep
+ * kv_tdvp_create) by `steps` time steps of `mode` (as kv_tdvp_sweep).  No
+ * reference counterpart: the reference runs one chain per process
+ * (src/kln-tdvp.cpp:73-78).  It replaces a loop of kv_tdvp_sweep
  * calls over the chains and leaves the same site tensors, bit for bit.  The
  * chains are spread over up to max_streams worker threads (<= 0: 8), each
  * with its own CUDA stream, staging ring and H_eff plan cache, so kernels of

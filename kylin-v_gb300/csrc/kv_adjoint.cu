@@ -83,15 +83,7 @@ TensorP add(const DTensor &a, const DTensor &b) {
     return out;
 }
 
-// out[k, s', wr, rest] = sum_{wl, s} W[s', wl, s, wr] t[k, wl, s, rest], k = legs [0, lead)
-TensorP mix(const DTensor &t, const DTensor &W, int lead) {
-    KV_REQUIRE(lead >= 0 && lead + 2 <= t.meta.rank && W.meta.rank == 4, KV_EINVAL, "internal: bad MPO mix");
-    MixPlanFull M = plan_mix(t.meta, W.meta, lead);
-    M.mix.upload();
-    auto out = DTensor::make(M.out, false);
-    launch_mix(M.mix, t.data(), W.data(), out->data(), nullptr);
-    return out;
-}
+TensorP mix(const DTensor &t, const DTensor &W, int lead) { return op_mix(t, W, lead); }
 
 TensorP perm(const DTensor &t, std::vector<int> ax) { return op_permute(t, ax); }
 

@@ -290,7 +290,8 @@ int kv_tdvp_sweep(kv_tdvp s, int mode) {
         KV_REQUIRE(s && s->s, KV_EINVAL, "null TDVP handle");
         if (mode == 1) s->s->one_site();
         else if (mode == 2) s->s->two_site();
-        else throw kv::Error(KV_EINVAL, "mode must be 1 or 2");
+        else if (mode == 0) s->s->global_krylov();
+        else throw kv::Error(KV_EINVAL, "mode must be 0, 1 or 2");
     });
 }
 
@@ -298,7 +299,7 @@ int kv_sweep_batched(int n_chains, const kv_tdvp *chains, int mode, int steps, i
     return guard([&] {
         kv::require_init();
         KV_REQUIRE(n_chains >= 0 && (n_chains == 0 || chains), KV_EINVAL, "null chain array");
-        KV_REQUIRE(mode == 1 || mode == 2, KV_EINVAL, "mode must be 1 or 2");
+        KV_REQUIRE(mode >= 0 && mode <= 2, KV_EINVAL, "mode must be 0, 1 or 2");
         KV_REQUIRE(steps >= 0, KV_EINVAL, "steps must be >= 0");
         std::set<const kv_tdvp_s *> seen;
         for (int i = 0; i < n_chains; ++i) {
@@ -354,7 +355,11 @@ int kv_sweep_batched(int n_chains, const kv_tdvp *chains, int mode, int steps, i
                 for (int i : assign[w]) {
                     kv::Tdvp &t = *chains[i]->s;
                     code[i] = guard([&] {
-                        for (int s = 0; s < steps; ++s) mode == 1 ? t.one_site() : t.two_site();
+                        for (int s = 0; s < steps; ++s) {
+                            if (mode == 0) t.global_krylov();
+                            else if (mode == 1) t.one_site();
+                            else t.two_site();
+                        }
                     });
                     if (code[i] != KV_OK) msg[i] = g_err;
                 }

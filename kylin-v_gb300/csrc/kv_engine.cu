@@ -1229,13 +1229,30 @@ Tdvp::Tdvp(const std::vector<TensorP> &mps_in, const std::vector<TensorP> &mpo_i
     events.resize(2 * kMaxEvents);
     for (auto &e : events) KV_CUDA(cudaEventCreate(&e));
     for (auto &e : sweep_ev) KV_CUDA(cudaEventCreate(&e));
-    // holstein/tdvp.h:303-316
+    init_envs();
+}
+
+// holstein/tdvp.h:303-316
+void Tdvp::init_envs() {
     const int ns = (int)mps.size();
     envL = {boundary_env(1, 0)};
     envR = {boundary_env(-1, mps[ns - 1]->meta.blocks[0].qn[2])};
     for (int i = ns - 1; i > 0; --i)
         envR.push_back(op_env(false, *envR.back(), *mps[i], *mpo[i], mpo_t[i].get(), precision, nullptr));
     KV_CUDA(cudaStreamSynchronize(ctx().stream));
+}
+
+// holstein/tdvp.h:318-327: the MPO scaled by dt on its first site
+// (Operator::operator*=, holstein/operator.h:66-70), one global_main.  The
+// reference builds the sweep environments once, before this stage, so its
+// next sweep contracts the new state with environments of the old one (a
+// result that depends on the phases of singular vectors, i.e. on rounding);
+// here they are rebuilt from the new state.
+void Tdvp::global_krylov() {
+    std::vector<TensorP> Hc = mpo;
+    Hc[0] = op_scale(*mpo[0], dt);
+    global_main(Hc, mps, max_iter, tol_exp, tol_svd, max_dim, precision);
+    init_envs();
 }
 
 Tdvp::~Tdvp() {

@@ -80,6 +80,14 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
 TensorP op_env(bool l2r, const DTensor &env, const DTensor &A, const DTensor &W, const DTensor *Wt, int precision,
                Flops *fl);
 TensorP op_permute(const DTensor &t, const std::vector<int> &ax);
+// out[k, s', wr, rest] = sum_{wl, s} W[s', wl, s, wr] t[k, wl, s, rest] (k = legs [0, lead)),
+// equal output blocks merged
+TensorP op_mix(const DTensor &t, const DTensor &W, int lead);
+TensorP boundary_env(int dir0, int q);
+TensorP op_scale(const DTensor &t, cplx s);  // s * t
+// global_main (holstein/krylov.h:199-283) on the MPO Hc (already scaled by dt)
+void global_main(const std::vector<TensorP> &Hc, std::vector<TensorP> &mps, int max_iter, double tol_exp,
+                 double tol_svd, int maxd, int precision);
 std::vector<TensorP> op_canonicalize(const std::vector<TensorP> &in, double tol, int max_dim, int precision);
 cplx op_expectation(const std::vector<DTensor *> &a, const std::vector<DTensor *> &w, const std::vector<DTensor *> &b);
 // the same value with all device scratch in a fixed static array (kv_noalloc.cu)
@@ -110,6 +118,9 @@ class Tdvp {
     ~Tdvp();
     void one_site();
     void two_site();
+    // one step of total_start's global-Krylov stage, then the environments
+    // rebuilt from the new state
+    void global_krylov();
     std::vector<TensorP> mps, mpo, mpo_t;
     std::vector<TensorP> envL, envR;
     double tol_svd, tol_exp;
@@ -131,6 +142,7 @@ class Tdvp {
     TensorP krylov(int nsite, const DTensor &L, const DTensor &psi, const DTensor *W1, const DTensor *W2,
                    const DTensor &R, bool reverse, int module);
     void mark(int module, bool start);
+    void init_envs();
     KrylovState *next_state();
     void begin_sweep();
     void end_sweep();

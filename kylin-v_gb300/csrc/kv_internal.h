@@ -397,6 +397,8 @@ void krylov_step(KrylovState *st, int k, double2 *hv, const double2 *vprev, cons
 // coefficients from the tridiagonal exponential, then out = sum_i c_i v_i on
 // the support of v_{iters-1}
 void krylov_finish(KrylovState *st, double2 *const *dV, double2 *out, const KrylovLens &nl, int reverse);
+// st->coef = exp(-+i T) e0 for T = tridiag(Re alpha, beta upper) of dimension st->iters
+void tridiag_exp(KrylovState *st, int reverse);
 // sum |x|^2 into a device double (deterministic)
 void vec_norm2(const double2 *x, int64_t n, double2 *parts, double *result);
 

@@ -249,6 +249,12 @@ void krylov_step(KrylovState *st, int k, double2 *hv, const double2 *vprev, cons
     KV_CUDA(cudaGetLastError());
 }
 
+void tridiag_exp(KrylovState *st, int reverse) {
+    k_tridiag_exp<<<1, 32, 0, ctx().stream>>>(st, reverse);
+    counted();
+    KV_CUDA(cudaGetLastError());
+}
+
 void krylov_finish(KrylovState *st, double2 *const *dV, double2 *out, const KrylovLens &nl, int reverse) {
     k_tridiag_exp<<<1, 32, 0, ctx().stream>>>(st, reverse);
     counted();

@@ -300,6 +300,14 @@ class TDVP:
         self.ns = ns
         self._m = None  # the driver holds its own copies
 
+    def global_krylov(self):
+        """One step of total_start's global-Krylov stage (holstein/krylov.h:199-283)."""
+        check(lib().kv_tdvp_sweep(self.ptr, 0))
+
+    def sweep(self, mode: int):
+        """mode 0: global_krylov, 1: one_site, 2: two_site."""
+        check(lib().kv_tdvp_sweep(self.ptr, mode))
+
     def one_site(self):
         check(lib().kv_tdvp_sweep(self.ptr, 1))
 

@@ -15,7 +15,8 @@
  *   tensors: kvo_tensor_new / kvo_tensor_info / kvo_tensor_get / kvo_tensor_free
  *   ops:     kvo_product, kvo_apply_zero/single/double, kvo_env_sweep,
  *            kvo_local_krylov, kvo_svd
- *   sweep:   kvo_tdvp_new / kvo_tdvp_sweep / kvo_tdvp_site / kvo_tdvp_free
+ *   sweep:   kvo_tdvp_new / kvo_tdvp_sweep (mode 0: one global-Krylov step,
+ *            1: one_site, 2: two_site) / kvo_tdvp_site / kvo_tdvp_free
  *   observable: kvo_join
  */
 #include <algorithm>
@@ -605,6 +606,292 @@ cplx join(const std::vector<Tensor> &a, const std::vector<Tensor> &w, const std:
     return r;
 }
 
+// ------------------------------------------------------- global Krylov
+// The nK stage of TDVP::total_start (holstein/tdvp.h:318-327):
+// global_main (holstein/krylov.h:199-283) on the MPO scaled by dt.
+using State = std::vector<Tensor>;
+
+Tensor boundary2(int dir0, int q) {  // rank-2 boundary environment {dir0, -dir0}, (q, q) = 1
+    Tensor t;
+    t.rank = 2;
+    t.dirs = {dir0, -dir0};
+    Block b;
+    b.rank = 2;
+    b.shape = {1, 1};
+    b.qn = {q, q};
+    b.data = {cplx(1.0, 0.0)};
+    t.blocks.push_back(b);
+    return t;
+}
+
+// leg dimension per charge of axis `ax`, from the blocks (holstein/tensor.h:187-196)
+std::map<int, int> leg_dims(const Tensor &t, int ax) {
+    std::map<int, int> m;
+    for (auto &b : t.blocks) m[b.qn[ax]] = b.shape[ax];
+    return m;
+}
+
+// b placed at offset `pos` inside a zero block of shape `sh` (holstein/block.h:181-197)
+Block pad_block(const Block &b, const std::array<int, kMaxRank> &sh, const std::array<int, kMaxRank> &pos) {
+    Block r;
+    r.rank = b.rank;
+    r.shape = sh;
+    r.qn = b.qn;
+    r.data.assign(r.size(), cplx(0.0, 0.0));
+    std::array<size_t, kMaxRank> sd{}, rd{};
+    sd[b.rank - 1] = rd[b.rank - 1] = 1;
+    for (int i = b.rank - 2; i >= 0; --i) {
+        sd[i] = sd[i + 1] * b.shape[i + 1];
+        rd[i] = rd[i + 1] * sh[i + 1];
+    }
+    for (size_t e = 0; e < b.size(); ++e) {
+        size_t dst = 0;
+        for (int j = 0; j < b.rank; ++j) dst += ((e / sd[j]) % b.shape[j] + pos[j]) * rd[j];
+        r.data[dst] = b.data[e];
+    }
+    return r;
+}
+
+// stack (holstein/tensor.h:262-317): direct sum of om2 into om1 on the legs
+// in `ax`; om1's blocks keep offset 0, om2's go after om1's dimension of the
+// same charge, equal keys merge.
+void stack(Tensor &om1, const Tensor &om2, const std::vector<int> &ax) {
+    std::vector<std::map<int, int>> comb(kMaxRank);
+    for (int a : ax) {
+        comb[a] = leg_dims(om1, a);
+        for (auto &kv : leg_dims(om2, a)) comb[a][kv.first] += kv.second;
+    }
+    for (auto &b : om1.blocks) {
+        std::array<int, kMaxRank> sh = b.shape, pos{};
+        for (int a : ax) sh[a] = comb[a][b.qn[a]];
+        if (sh != b.shape) b = pad_block(b, sh, pos);
+    }
+    for (auto &b : om2.blocks) {
+        std::array<int, kMaxRank> sh = b.shape, pos{};
+        for (int a : ax) {
+            sh[a] = comb[a][b.qn[a]];
+            pos[a] = sh[a] - b.shape[a];
+        }
+        om1.push_merge(sh != b.shape ? pad_block(b, sh, pos) : b);
+    }
+}
+
+// State += (holstein/state.h:54-64)
+void state_add(State &a, const State &b) {
+    const int ns = (int)a.size();
+    stack(a[0], b[0], {2});
+    for (int i = 1; i < ns - 1; ++i) stack(a[i], b[i], {0, 2});
+    stack(a[ns - 1], b[ns - 1], {0});
+}
+
+// overlap(State, State) (holstein/state.h:206-227)
+cplx state_overlap(const State &s1, const State &s2) {
+    Tensor env = boundary2(1, 0);
+    for (size_t i = 0; i < s1.size(); ++i) env = product(s1[i], product(env, s2[i], 1, OP_N, OP_N), 2, OP_C, OP_N);
+    if (env.blocks.empty()) return 0.0;
+    const int q = env.blocks[0].qn[0];
+    cplx r = 0.0;
+    for (auto &b : env.blocks)
+        if (b.shape[0] == 1 && b.shape[1] == 1 && b.qn[0] == q && b.qn[1] == q) r += b.data[0];
+    return r;
+}
+
+// State::canonicalize (holstein/state.h:166-185)
+void canonicalize(State &s, double tol, int maxd) {
+    const int ns = (int)s.size();
+    for (int i = 0; i < ns - 1; ++i) {
+        SvdResult r = svd_impl(s[i], 2, true, tol, maxd);
+        s[i] = std::move(r.U);
+        s[i + 1] = product(r.V, s[i + 1], 1, OP_N, OP_N);
+    }
+    for (int i = ns - 1; i > 0; --i) {
+        SvdResult r = svd_impl(s[i], 1, false, tol, maxd);
+        s[i] = std::move(r.V);
+        s[i - 1] = product(s[i - 1], r.U, 1, OP_N, OP_N);
+    }
+}
+
+// env_mps_mpo(..., Chk = true) (holstein/product.h:278-319): equal blocks merged
+Tensor env_mps_mpo_merged(const Tensor &env, const Tensor &mps, const Tensor &mpo) {
+    Tensor raw = env_mps_mpo(env, mps, mpo), r;
+    r.rank = raw.rank;
+    r.dirs = raw.dirs;
+    for (auto &b : raw.blocks) r.push_merge(b);
+    return r;
+}
+
+// apply_operator (holstein/operator.h:232-269)
+State apply_operator(const State &op, const State &wf, double tol, int maxd) {
+    const int ns = (int)op.size();
+    Tensor envl = boundary(1, 0);
+    State res(ns);
+    const int lastB = wf[ns - 1].blocks.at(0).qn[2], lastw = op[ns - 1].blocks.at(0).qn[3];
+    for (int i = 0; i < ns; ++i) {
+        Tensor lmo = env_mps_mpo_merged(envl, wf[i], op[i]);
+        if (i == ns - 1) {
+            Tensor envr = boundary(-1, lastB);
+            envr.blocks[0].qn = {lastB, lastw, lastB};
+            res[i] = product(lmo, envr, 2, OP_N, OP_T);
+        } else {
+            SvdResult r = svd_impl(lmo, 2, true, tol, maxd);
+            res[i] = std::move(r.U);
+            envl = std::move(r.V);
+        }
+    }
+    for (int i = ns - 1; i > 0; --i) {
+        SvdResult r = svd_impl(res[i], 1, false, tol, maxd);
+        res[i] = std::move(r.V);
+        res[i - 1] = product(res[i - 1], r.U, 1, OP_N, OP_N);
+    }
+    return res;
+}
+
+// apply_ortho_site (holstein/krylov.h:13-45): Nh minus its projection on La, Lb
+Tensor apply_ortho_site(const Tensor &Nh, const Tensor &La, const Tensor &Lb) {
+    const cplx LNa = overlap(La, Nh), LNb = overlap(Lb, Nh);
+    const cplx aa = std::pow(tnorm(La), 2.0), bb = std::pow(tnorm(Lb), 2.0);
+    const cplx ab = overlap(La, Lb), ba = std::conj(ab);
+    const cplx cc = ab * ba - aa * bb;
+    Tensor res = Nh;
+    if (std::abs(cc) < 1e-17) {
+        if (std::abs(aa) < 1e-17) return res;
+        add_scaled(res, La, -1.0 * LNa / aa);
+    } else {
+        add_scaled(res, La, (bb * LNa - ab * LNb) / cc);
+        add_scaled(res, Lb, (aa * LNb - ba * LNa) / cc);
+    }
+    return res;
+}
+
+// 4-argument env_sweep (holstein/product.h:505-521), both directions
+Tensor env_sweep4(const Tensor &env, const Tensor &a1, const Tensor &W, const Tensor &a2, bool l2r) {
+    if (l2r) return env_sweep2(env, a1, W, a2);
+    return env_sweep2(env, transpose(a1, {2, 1, 0}), transpose(W, {0, 3, 2, 1}), transpose(a2, {2, 1, 0}));
+}
+
+// 2-leg env_sweep <a1|a2> (holstein/product.h:523-538), both directions
+Tensor env_state(const Tensor &env, const Tensor &a1, const Tensor &a2, bool l2r) {
+    if (l2r) return product(a1, product(env, a2, 1, OP_N, OP_N), 2, OP_C, OP_N);
+    return env_state(env, transpose(a1, {2, 1, 0}), transpose(a2, {2, 1, 0}), true);
+}
+
+// apply_double_state (holstein/krylov.h:125-131)
+Tensor apply_double_state(const Tensor &envl, const Tensor &M, const Tensor &envr) {
+    return product(product(envl, M, 1, OP_N, OP_N), envr, 1, OP_N, OP_T);
+}
+
+// apply_ortho(H, Va) (holstein/krylov.h:133-142)
+State apply_ortho1(const State &H, const State &Va, double tol, int maxd) {
+    State gss = apply_operator(H, Va, tol, maxd);
+    const cplx ovp = state_overlap(gss, Va);
+    State vac = Va;
+    scale(vac[0], -1.0 * ovp);
+    state_add(gss, vac);
+    canonicalize(gss, 0.0, 1000);
+    return gss;
+}
+
+// apply_ortho(H, Va, Vb) (holstein/krylov.h:145-197): H Va minus its
+// components on Va and Vb, fitted two sites at a time, both directions
+State apply_ortho2(const State &H, const State &Va, const State &Vb, double tol, int maxd) {
+    const int ns = (int)H.size();
+    State gss = apply_operator(H, Va, tol, maxd);
+    const int tot = gss[ns - 1].blocks.at(0).qn[2];
+    std::vector<Tensor> eLH = {boundary(1, 0)}, eRH = {boundary(-1, tot)};
+    std::vector<Tensor> eLa = {boundary2(1, 0)}, eRa = {boundary2(-1, tot)};
+    std::vector<Tensor> eLb = {boundary2(1, 0)}, eRb = {boundary2(-1, tot)};
+    for (int i = ns - 1; i > 1; --i) {  // init_env_op / init_env_state (holstein/krylov.h:48-94)
+        eRH.push_back(env_sweep4(eRH.back(), gss[i], H[i], Va[i], false));
+        eRa.push_back(env_state(eRa.back(), gss[i], Va[i], false));
+        eRb.push_back(env_state(eRb.back(), gss[i], Vb[i], false));
+    }
+    auto site = [&](int a, int b, bool l2r) {
+        Tensor Ta = product(Va[a], Va[b], 1, OP_N, OP_N), Tb = product(Vb[a], Vb[b], 1, OP_N, OP_N);
+        Tensor Nh = apply_double(eLH.back(), Ta, H[a], H[b], eRH.back());
+        Tensor La = apply_double_state(eLa.back(), Ta, eRa.back());
+        Tensor Lb = apply_double_state(eLb.back(), Tb, eRb.back());
+        SvdResult r = svd_impl(apply_ortho_site(Nh, La, Lb), 2, l2r, tol, maxd);
+        gss[a] = std::move(r.U);
+        gss[b] = std::move(r.V);
+    };
+    for (int i = 0; i < ns - 1; ++i) {
+        site(i, i + 1, true);
+        if (i < ns - 2) {  // update_env_op / update_env_state (holstein/krylov.h:97-124)
+            eLH.push_back(env_sweep4(eLH.back(), gss[i], H[i], Va[i], true));
+            eLa.push_back(env_state(eLa.back(), gss[i], Va[i], true));
+            eLb.push_back(env_state(eLb.back(), gss[i], Vb[i], true));
+            eRH.pop_back();
+            eRa.pop_back();
+            eRb.pop_back();
+        }
+    }
+    for (int i = ns - 1; i > 0; --i) {
+        site(i - 1, i, false);
+        if (i > 1) {
+            eRH.push_back(env_sweep4(eRH.back(), gss[i], H[i], Va[i], false));
+            eRa.push_back(env_state(eRa.back(), gss[i], Va[i], false));
+            eRb.push_back(env_state(eRb.back(), gss[i], Vb[i], false));
+            eLH.pop_back();
+            eLa.pop_back();
+            eLb.pop_back();
+        }
+    }
+    return gss;
+}
+
+// global_main (holstein/krylov.h:199-283): Krylov basis of MPSs with the MPO
+// (already scaled by dt), exp(-i Hm) e0 on the Hessenberg matrix of joins,
+// mps = sum_i c_i V_i with a canonicalisation after every addition
+void global_main(const State &Hc, State &mps, int max_iter, double tol_exp, double tol_svd, int maxd) {
+    scale(mps[0], 1.0 / tnorm(mps[0]));
+    std::vector<State> Vm = {mps};
+    int k = 0;
+    double err = 1.0;
+    while (k < max_iter - 1 && err > tol_exp) {
+        State hv = k > 0 ? apply_ortho2(Hc, Vm[k], Vm[k - 1], tol_svd, maxd) : apply_ortho1(Hc, Vm[k], tol_svd, maxd);
+        const double nmhv = tnorm(hv[0]);
+        err *= nmhv;
+        if (err < tol_exp || nmhv > 1.0) break;
+        scale(hv[0], 1.0 / nmhv);
+        Vm.push_back(std::move(hv));
+        ++k;
+    }
+    const int ld = (int)Vm.size();
+    std::vector<cplx> Hm((size_t)ld * ld, cplx(0.0, 0.0)), c(ld, cplx(0.0, 0.0));
+    std::vector<double> ev(ld);
+    for (int i = 0; i < ld; ++i) {
+        Hm[(size_t)i * ld + i] = join(Vm[i], Hc, Vm[i]);
+        if (i < ld - 1) Hm[(size_t)i * ld + i + 1] = join(Vm[i], Hc, Vm[i + 1]);
+    }
+    if (scipy_LAPACKE_zheevd(kRowMajor, 'V', 'U', ld, Hm.data(), ld, ev.data()) != 0)
+        throw std::runtime_error("zheevd failed");
+    const cplx img(0.0, -1.0);
+    for (int i = 0; i < ld; ++i)
+        for (int j = 0; j < ld; ++j) c[i] += Hm[(size_t)i * ld + j] * std::exp(img * ev[j]) * std::conj(Hm[j]);
+    mps = Vm[0];
+    scale(mps[0], c[0]);
+    for (int i = 1; i < ld; ++i) {
+        State t = Vm[i];
+        scale(t[0], c[i]);
+        state_add(mps, t);
+        canonicalize(mps, tol_svd, maxd);
+    }
+}
+
+// one step of the nK stage: the MPO scaled by dt on its first site
+// (Operator::operator*=, holstein/operator.h:66-70).  Deviation: the sweep
+// driver's environments are rebuilt from the new state afterwards.
+// total_start builds them once, before this stage (holstein/tdvp.h:303-316),
+// so its first sweep after a global step contracts the new MPS with
+// environments of the old one; that result depends on the phases of the
+// singular vectors the step leaves, which rounding decides.
+void global_step(Tdvp &s) {
+    State Hc = s.mpo;
+    scale(Hc[0], s.dt);
+    global_main(Hc, s.mps, s.max_iter, s.tol_exp, s.tol_svd, s.max_dim);
+    tdvp_init(s);
+}
+
 thread_local std::string g_err;
 
 template <class F>
@@ -750,7 +1037,8 @@ int kvo_tdvp_sweep(void *h, int mode) {
         auto *s = static_cast<Tdvp *>(h);
         if (mode == 1) one_site(*s);
         else if (mode == 2) two_site(*s);
-        else throw std::runtime_error("mode must be 1 or 2");
+        else if (mode == 0) global_step(*s);
+        else throw std::runtime_error("mode must be 0, 1 or 2");
     });
 }
 

@@ -1,7 +1,7 @@
 // Exercises the drop-in C++ layer (include/holstein/) the way a reference
 // driver does: load an MPS and an MPO in the reference's binary formats, build
 // Holstein::TDVP, run total_start on a stage string.  Usage:
-//   dropin_driver <mps file> <mpo file> <stage "[0,n2,0,n1]"> <maxD> <tolSVD>
+//   dropin_driver <mps file> <mpo file> <stage "[nK,n2,0,n1]"> <maxD> <tolSVD>
 #include "holstein/tdvp.h"
 
 using namespace KylinVib;

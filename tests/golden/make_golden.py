@@ -1,7 +1,8 @@
 """Generate the golden vectors in tests/golden/ from the compiled reference.
 
 Run here (where the reference sources are mounted) with
-``python tests/golden/make_golden.py``.  It builds the reference drivers and
+``python tests/golden/make_golden.py`` (everything) or ``... --add`` (only the
+trajectories the manifest lacks, from the committed inputs).  It builds the reference drivers and
 the golden tools (oracle/Makefile, target ``ref``) and, for each case:
 
 * writes the seeded inputs with this package's generators (Hamiltonian MPO,
@@ -51,16 +52,67 @@ def cases():
     return {
         # 3 molecules x 1 mode, cutoff 4: 9 sites
         "tiny1": dict(chain=HolsteinChain(3, [1.0], [[1.0], [0.8], [1.2]], cutoff=4, eps=[0.1, -0.2, 0.3]),
-                      D=8, seed=11, ops_sites=[1, 4], traj=[("[0,0,0,4]", 8, 1e-8), ("[0,3,0,0]", 8, 1e-8)],
+                      D=8, seed=11, ops_sites=[1, 4], traj=[("[0,0,0,4]", 8, 1e-8), ("[0,3,0,0]", 8, 1e-8), ("[3,0,0,0]", 8, 1e-8)],
                       keep_inputs=True),
         # 2 molecules x 2 modes, cutoff 3: 10 sites
         "tiny2m": dict(chain=HolsteinChain(2, [1.0, 0.4], [[1.0, 0.6], [0.9, 0.5]], cutoff=3),
-                       D=10, seed=12, ops_sites=[2, 6], traj=[("[0,0,0,3]", 10, 1e-8), ("[0,3,0,0]", 10, 1e-8)],
+                       D=10, seed=12, ops_sites=[2, 6], traj=[("[0,0,0,3]", 10, 1e-8), ("[0,3,0,0]", 10, 1e-8),
+                                                          ("[2,0,0,0]", 10, 1e-8)],
                        keep_inputs=True),
         # the 1-site benchmark shape: L=8, 1 mode, cutoff 8, D=32, 20 steps
         "l8c8d32": dict(chain=HolsteinChain(8, [1.0], [[1.0]] * 8, cutoff=8), D=32, seed=1234, ops_sites=[7],
                         traj=[("[0,0,0,20]", 32, 1e-8)], keep_inputs=False),
     }
+
+
+def trajectory(ch, work, out, stage, maxd, tol, dens):
+    """Run the reference TDVP driver on work/in.mps, work/H.mpo and write
+    out/traj_<stage>.txt; returns the manifest entry."""
+    for f in os.listdir(os.path.join(work, "State")):
+        os.remove(os.path.join(work, "State", f))
+    txt = run([os.path.join(REF_BIN, "kv_ref_tdvp"), "-w", "in.mps", "-o", "H.mpo", "-s", stage,
+               "-v", "0.05", "-D", str(maxd), "-t", str(tol), "-k", "11", "-e", "1e-8",
+               "-d", ",".join(os.path.basename(p) for p in dens)], work)
+    tag = stage.strip("[]").replace(",", "_")
+    with open(os.path.join(out, f"traj_{tag}.txt"), "w") as f:
+        f.write(f"# stage {stage} dt 0.05 maxD {maxd} tolSVD {tol} maxIter 11 tolExp 1e-8\n")
+        f.write(txt)
+    return {"stage": stage, "maxD": maxd, "tol_svd": tol, "file": f"traj_{tag}.txt"}
+
+
+def add_missing_trajectories():
+    """--add: the trajectories of cases() that the manifest lacks, from the
+    committed inputs (the seeded generator is not bit-reproducible across BLAS
+    thread counts, so existing vectors are left as they are)."""
+    _pkg()
+    from kylin_v_gb300 import holstein as H
+    from kylin_v_gb300 import kvio
+
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", "-j4"], check=True,
+                   stdout=subprocess.DEVNULL)
+    with open(os.path.join(HERE, "manifest.json")) as f:
+        manifest = json.load(f)
+    for name, c in cases().items():
+        have = {t["stage"] for t in manifest[name]["trajectories"]}
+        todo = [t for t in c["traj"] if t[0] not in have]
+        if not todo or not c["keep_inputs"]:
+            continue
+        ch = c["chain"]
+        out = os.path.join(HERE, name)
+        work = tempfile.mkdtemp(prefix="kvgold_")
+        os.makedirs(os.path.join(work, "State"))
+        for f in ("in.mps", "H.mpo"):
+            shutil.copy(os.path.join(out, f), os.path.join(work, f))
+        dens = []
+        for j in ch.exciton_sites():
+            p = os.path.join(work, f"D{j}.mpo")
+            kvio.write_mpo(p, H.density_mpo(ch, j))
+            dens.append(p)
+        for stage, maxd, tol in todo:
+            manifest[name]["trajectories"].append(trajectory(ch, work, out, stage, maxd, tol, dens))
+        shutil.rmtree(work)
+    with open(os.path.join(HERE, "manifest.json"), "w") as f:
+        json.dump(manifest, f, indent=1)
 
 
 def run(cmd, cwd):
@@ -113,19 +165,7 @@ def main():
                 os.makedirs(od, exist_ok=True)
                 run([os.path.join(REF_BIN, "kv_ref_ops"), "-w", "in.mps", "-o", "H.mpo", "-i", str(site),
                      "-v", "0.05", "-k", "11", "-e", "1e-8", "-t", "1e-8", "-D", str(c["D"]), "-O", od], work)
-        trajs = []
-        for stage, maxd, tol in c["traj"]:
-            for f in os.listdir(os.path.join(work, "State")):
-                os.remove(os.path.join(work, "State", f))
-            txt = run([os.path.join(REF_BIN, "kv_ref_tdvp"), "-w", "in.mps", "-o", "H.mpo", "-s", stage,
-                       "-v", "0.05", "-D", str(maxd), "-t", str(tol), "-k", "11", "-e", "1e-8",
-                       "-d", ",".join(os.path.basename(p) for p in dens)], work)
-            tag = stage.strip("[]").replace(",", "_")
-            with open(os.path.join(out, f"traj_{tag}.txt"), "w") as f:
-                f.write(f"# stage {stage} dt 0.05 maxD {maxd} tolSVD {tol} maxIter 11 tolExp 1e-8\n")
-                f.write(txt)
-            trajs.append({"stage": stage, "maxD": maxd, "tol_svd": tol, "file": f"traj_{tag}.txt"})
-        entry["trajectories"] = trajs
+        entry["trajectories"] = [trajectory(ch, work, out, stage, maxd, tol, dens) for stage, maxd, tol in c["traj"]]
         manifest[name] = entry
         shutil.rmtree(work)
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
@@ -133,4 +173,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    add_missing_trajectories() if "--add" in sys.argv[1:] else main()

@@ -65,3 +65,12 @@ def read_traj(path):
                 continue
             rows.append([float(x) for x in line.split()])
     return np.array(rows)
+
+
+def stage_modes(stage: str) -> list:
+    """Sweep modes of a total_start stage string [nK, n2TDVP, nSA, n1TDVP]
+    (holstein/tdvp.h:297-385) in the order the driver runs them: 0 = one
+    global-Krylov step, 2 = two_site, 1 = one_site (the SA stage is not built)."""
+    nk, n2, nsa, n1 = (int(x) for x in stage.strip("[]").split(","))
+    assert nsa == 0, "the SA-1TDVP stage is not built"
+    return [0] * nk + [2] * n2 + [1] * n1

@@ -48,7 +48,7 @@ def test_dropin_driver_matches_library(tmp_path):
     g = U.GOLDEN
     D = U.manifest()["tiny2m"]["D"]
     mps_file, mpo_file = os.path.join(g, "tiny2m", "in.mps"), os.path.join(g, "tiny2m", "H.mpo")
-    r = subprocess.run([str(exe), mps_file, mpo_file, "[0,1,0,1]", str(D), "1e-8"], cwd=tmp_path,
+    r = subprocess.run([str(exe), mps_file, mpo_file, "[1,1,0,1]", str(D), "1e-8"], cwd=tmp_path,
                        capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
     assert "Max bond dimension" in r.stdout
@@ -56,7 +56,7 @@ def test_dropin_driver_matches_library(tmp_path):
 
     kvgpu.init(0)
     t = kvgpu.TDVP(kvio.read_mps(mps_file), kvio.read_mpo(mpo_file), 1e-8, 1e-8, D, 11, 0.05)
-    for k, sweep in enumerate((t.two_site, t.one_site)):
+    for k, sweep in enumerate((t.global_krylov, t.two_site, t.one_site)):
         sweep()
         got = kvio.read_mps(str(tmp_path / "State" / f"T-{k}.mps"))
         want = [s.to_host() for s in t.sites()]

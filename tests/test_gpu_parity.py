@@ -113,16 +113,14 @@ TRAJ = [(c, i) for c, e in U.manifest().items() for i in range(len(e["trajectori
 def test_tdvp_trajectory(gpu, case, ti):
     ch, mps, mpo, tr = _traj_case(case, ti)
     ref = U.read_traj(f"{G}/{case}/{tr['file']}")
-    stg = [int(x) for x in tr["stage"].strip("[]").split(",")]
-    mode, n = (2, stg[1]) if stg[1] else (1, stg[3])
     dens = [H.density_mpo(ch, j) for j in ch.exciton_sites()]
     ident = H.identity_mpo(ch)
     t = gpu.TDVP(mps, mpo, tr["tol_svd"], 1e-8, tr["maxD"], 11, 0.05)
     dmpo = [[gpu.Tensor.from_host(x) for x in d] for d in dens]
     hmpo = [gpu.Tensor.from_host(x) for x in mpo]
     imp = [gpu.Tensor.from_host(x) for x in ident]
-    for k in range(n):
-        t.two_site() if mode == 2 else t.one_site()
+    for k, mode in enumerate(U.stage_modes(tr["stage"])):
+        t.sweep(mode)
         s = t.sites()
         assert abs(gpu.expectation(s, imp, s).real - ref[k][1]) < 1e-10
         assert abs(gpu.expectation(s, hmpo, s).real - ref[k][2]) < 1e-8
@@ -179,3 +177,24 @@ def test_canonicalize(gpu, case):
         u, v, _, _ = O.svd(ref[i], 1, False, 0.0, 1000)
         ref[i], ref[i - 1] = v, O.product(ref[i - 1], u, 1)
     assert [t.legs()[2] for t in host[:-1]] == [t.legs()[2] for t in ref[:-1]]
+
+
+@pytest.mark.parametrize("case", ["tiny1", "tiny2m"])
+def test_global_krylov_then_tdvp_matches_oracle(gpu, case):
+    """Global-Krylov steps followed by one- and two-site sweeps (the sweep
+    environments rebuilt after the Krylov stage, in both) against the oracle."""
+    ch, mps, mpo, tr = _traj_case(case, 0)
+    D = tr["maxD"]
+    dens = [H.density_mpo(ch, j) for j in ch.exciton_sites()]
+    t = gpu.TDVP(mps, mpo, 1e-8, 1e-8, D, 11, 0.05)
+    o = O.Tdvp(mps, mpo, 1e-8, 1e-8, D, 11, 0.05)
+    dmpo = [[gpu.Tensor.from_host(x) for x in d] for d in dens]
+    hmpo = [gpu.Tensor.from_host(x) for x in mpo]
+    for mode in (0, 0, 2, 1):
+        t.sweep(mode)
+        o.sweep(mode)
+        s, so = t.sites(), o.mps()
+        assert abs(gpu.expectation(s, hmpo, s).real - O.join(so, mpo, so).real) < 1e-9, mode
+        pops = np.array([gpu.expectation(s, d, s).real for d in dmpo])
+        pref = np.array([O.join(so, d, so).real for d in dens])
+        assert np.abs(pops - pref).max() < 1e-9, mode

@@ -87,10 +87,8 @@ def test_tdvp_trajectory_matches_reference(case, ti):
     dens = [H.density_mpo(ch, j) for j in ch.exciton_sites()]
     ident = H.identity_mpo(ch)
     ref = U.read_traj(f"{G}/{case}/{tr['file']}")
-    stg = [int(x) for x in tr["stage"].strip("[]").split(",")]
-    mode, n = (2, stg[1]) if stg[1] else (1, stg[3])
     t = O.Tdvp(mps, mpo, tr["tol_svd"], 1e-8, tr["maxD"], 11, 0.05)
-    for k in range(n):
+    for k, mode in enumerate(U.stage_modes(tr["stage"])):
         t.sweep(mode)
         s = t.mps()
         assert abs(O.join(s, ident, s).real - ref[k][1]) < 1e-12
