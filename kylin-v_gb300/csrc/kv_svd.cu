@@ -114,6 +114,8 @@ __global__ void __launch_bounds__(NT) k_svd_jacobi(const SvdSector *__restrict__
     if (threadIdx.x == 0) status[blockIdx.x] = converged ? sweep : -sweep;
 }
 
+constexpr int kJacEpl = 8;  // register-resident elements per lane: columns of <= 128 rows
+
 // Mixed mode: one-sided Jacobi in FP32 without accumulated rotations.  T is
 // oriented so that the singular vectors wanted afterwards are its own columns
 // (they converge to sigma_j w_j); T stays in shared memory when p*q <=
@@ -122,7 +124,12 @@ __global__ void __launch_bounds__(NT) k_svd_jacobi(const SvdSector *__restrict__
 // pass over the shared-memory banks).  Columns below 1e-7 of ||T||_F are
 // numerically zero in FP32 and are not rotated (this also lets wide T, q > p,
 // converge: its q - p surplus columns go to zero).
-template <int NT, int G>
+//
+// EPL > 0 (columns of at most G * EPL rows): each lane keeps its EPL elements
+// of the pair in registers between the dot product and the rotation, and the
+// complex arithmetic runs as packed FP32 pairs (fma.rn.f32x2: the real and
+// imaginary parts in one instruction).
+template <int NT, int G, int EPL>
 __global__ void __launch_bounds__(NT) k_svd_jacobi_w(const SvdSector *__restrict__ secs, float2 *__restrict__ T,
                                                      int *status, int max_sweeps, float tol, int smem_elems) {
     extern __shared__ float2 sT[];
@@ -177,10 +184,26 @@ __global__ void __launch_bounds__(NT) k_svd_jacobi_w(const SvdSector *__restrict
                 if (!(a > zt) || !(b > zt)) continue;
                 float2 *x = t + (int64_t)c0 * p, *y = t + (int64_t)c1 * p;
                 float cr = 0, ci = 0;
-                for (int i = gl; i < p; i += G) {
-                    const float2 xi = x[i], yi = y[i];
-                    cr += xi.x * yi.x + xi.y * yi.y;
-                    ci += xi.x * yi.y - xi.y * yi.x;
+                float2 xv[EPL > 0 ? EPL : 1], yv[EPL > 0 ? EPL : 1];
+                if constexpr (EPL > 0) {
+                    // (sum xr yr, sum xi yi) and (sum xr yi, sum xi yr)
+                    float2 a1 = make_float2(0.f, 0.f), a2 = make_float2(0.f, 0.f);
+#pragma unroll
+                    for (int k = 0; k < EPL; ++k) {
+                        const int i = gl + k * G;
+                        xv[k] = i < p ? x[i] : make_float2(0.f, 0.f);
+                        yv[k] = i < p ? y[i] : make_float2(0.f, 0.f);
+                        a1 = __ffma2_rn(xv[k], yv[k], a1);
+                        a2 = __ffma2_rn(xv[k], make_float2(yv[k].y, yv[k].x), a2);
+                    }
+                    cr = a1.x + a1.y;
+                    ci = a2.x - a2.y;
+                } else {
+                    for (int i = gl; i < p; i += G) {
+                        const float2 xi = x[i], yi = y[i];
+                        cr += xi.x * yi.x + xi.y * yi.y;
+                        ci += xi.x * yi.y - xi.y * yi.x;
+                    }
                 }
 #pragma unroll
                 for (int o = G / 2; o > 0; o >>= 1) {
@@ -203,11 +226,32 @@ __global__ void __launch_bounds__(NT) k_svd_jacobi_w(const SvdSector *__restrict
                     nrm[c0] = a - tn * ac;
                     nrm[c1] = b + tn * ac;
                 }
-                for (int i = gl; i < p; i += G) {
-                    float2 xi = x[i], yi = y[i];
-                    kvj::rotate_pair(rot, xi.x, xi.y, yi.x, yi.y);
-                    x[i] = xi;
-                    y[i] = yi;
+                if constexpr (EPL > 0) {
+                    // x' = cs x - s_re y - s_im (yi, -yr),  y' = cs y + s_re x + s_im (-xi, xr)
+                    const float2 cs2 = make_float2(rot.cs, rot.cs), sr2 = make_float2(rot.s_re, rot.s_re);
+                    const float2 msr2 = make_float2(-rot.s_re, -rot.s_re), pm = make_float2(-rot.s_im, rot.s_im);
+#pragma unroll
+                    for (int k = 0; k < EPL; ++k) {
+                        const int i = gl + k * G;
+                        const float2 xo = xv[k], yo = yv[k];
+                        float2 nx = __fmul2_rn(cs2, xo);
+                        nx = __ffma2_rn(msr2, yo, nx);
+                        nx = __ffma2_rn(pm, make_float2(yo.y, yo.x), nx);
+                        float2 ny = __fmul2_rn(cs2, yo);
+                        ny = __ffma2_rn(sr2, xo, ny);
+                        ny = __ffma2_rn(pm, make_float2(xo.y, xo.x), ny);
+                        if (i < p) {
+                            x[i] = nx;
+                            y[i] = ny;
+                        }
+                    }
+                } else {
+                    for (int i = gl; i < p; i += G) {
+                        float2 xi = x[i], yi = y[i];
+                        kvj::rotate_pair(rot, xi.x, xi.y, yi.x, yi.y);
+                        x[i] = xi;
+                        y[i] = yi;
+                    }
                 }
             }
             __syncthreads();
@@ -465,20 +509,29 @@ void svd_jacobi_f32(const SvdPlan &p, const double2 *T64, float2 *T, int *status
         int optin = 0;
         KV_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx().device));
         const int bytes = std::max(0, optin - 4096 - (int)sizeof(float) * kJacobiMaxQ);
-        KV_CUDA(cudaFuncSetAttribute(k_svd_jacobi_w<1024, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        KV_CUDA(cudaFuncSetAttribute(k_svd_jacobi_w<1024, 16, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        KV_CUDA(cudaFuncSetAttribute(k_svd_jacobi_w<1024, 16, kJacEpl>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     bytes));
         smem_bytes = bytes;
     });
     int64_t max_pq = 0;
+    int max_p = 0;
     for (auto &s : p.secs) {
         KV_REQUIRE(s.q <= kJacobiMaxQ, KV_EINVAL, "mixed-precision SVD: a sector has more than 2048 columns");
         max_pq = std::max<int64_t>(max_pq, (int64_t)s.p * s.q);
+        max_p = std::max(max_p, s.p);
     }
     const int cap = smem_bytes / (int)sizeof(float2);
     const int elems = (int)std::min<int64_t>(max_pq, cap);
     k_to_f32<<<std::max(1, ctx().num_sms * 4), 256, 0, ctx().stream>>>(T64, T, p.t_elems);
     counted();
-    k_svd_jacobi_w<1024, 16><<<(unsigned)p.secs.size(), 1024, (size_t)elems * sizeof(float2), ctx().stream>>>(
-        p.d_secs.as<SvdSector>(), T, status, max_sweeps, tol, elems);
+    if (max_p <= 16 * kJacEpl)
+        k_svd_jacobi_w<1024, 16, kJacEpl><<<(unsigned)p.secs.size(), 1024, (size_t)elems * sizeof(float2),
+                                            ctx().stream>>>(p.d_secs.as<SvdSector>(), T, status, max_sweeps, tol,
+                                                            elems);
+    else
+        k_svd_jacobi_w<1024, 16, 0><<<(unsigned)p.secs.size(), 1024, (size_t)elems * sizeof(float2), ctx().stream>>>(
+            p.d_secs.as<SvdSector>(), T, status, max_sweeps, tol, elems);
     counted();
     KV_CUDA(cudaGetLastError());
 }
