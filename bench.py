@@ -17,13 +17,19 @@ value      algorithmic TFLOP/s: 8*M*N*K summed over every complex GEMM the
 e2e        the same metric through the public C ABI with host buffers: every
            step uploads the MPS and MPO from pinned host memory, builds the
            environments, sweeps and downloads the MPS.
-roofline   grouped block-sparse GEMM (the dominant kernel): reference flops
-           of its block pairs / its event-timed duration, against the TF32
-           dense tensor peak (half the measured bf16 peak).
+roofline   the grouped block-sparse GEMM on the tensor cores: reference flops
+           of its block pairs / its event-timed duration, against the
+           measured dense FP16/BF16 tensor peak (the digit GEMM runs on the
+           FP16 pipe); traffic from the committed ncu summary.
+fp64_compare  the mixed path against the FP64 path on a 4-molecule chain of
+           the same structure over --compare-steps steps: time per step and
+           the largest site-population and energy differences.
 cpu_baseline  the CPU oracle (restatement of the reference on OpenBLAS, all
            host threads) on a 3-molecule chain of the same local structure.
 
 --impl reference  runs only the CPU oracle (rank 0) and prints its line.
+--config holstein-1site-batch64  the batched disordered ensemble instead
+           (run_batched); under torchrun its chains are split across ranks.
 N > 1 (torchrun): each rank evolves its own replica chain (a single chain's
 sweep is sequential), value = total flops / max time over ranks.
 """
