@@ -114,8 +114,6 @@ __global__ void __launch_bounds__(NT) k_svd_jacobi(const SvdSector *__restrict__
     if (threadIdx.x == 0) status[blockIdx.x] = converged ? sweep : -sweep;
 }
 
-constexpr int kJacEpl = 8;  // register-resident elements per lane: columns of <= 128 rows
-
 // Mixed mode: one-sided Jacobi in FP32 without accumulated rotations.  T is
 // oriented so that the singular vectors wanted afterwards are its own columns
 // (they converge to sigma_j w_j); T stays in shared memory when p*q <=
@@ -125,7 +123,8 @@ constexpr int kJacEpl = 8;  // register-resident elements per lane: columns of <
 // numerically zero in FP32 and are not rotated (this also lets wide T, q > p,
 // converge: its q - p surplus columns go to zero).
 //
-// EPL > 0 (columns of at most G * EPL rows): each lane keeps its EPL elements
+// EPL > 0 (columns of at most G * EPL rows; the launch picks 2, 4 or 8 from
+// its longest column): each lane keeps its EPL elements
 // of the pair in registers between the dot product and the rotation, and the
 // complex arithmetic runs as packed FP32 pairs (fma.rn.f32x2: the real and
 // imaginary parts in one instruction).
@@ -510,8 +509,9 @@ void svd_jacobi_f32(const SvdPlan &p, const double2 *T64, float2 *T, int *status
         KV_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx().device));
         const int bytes = std::max(0, optin - 4096 - (int)sizeof(float) * kJacobiMaxQ);
         KV_CUDA(cudaFuncSetAttribute(k_svd_jacobi_w<1024, 16, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-        KV_CUDA(cudaFuncSetAttribute(k_svd_jacobi_w<1024, 16, kJacEpl>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     bytes));
+        KV_CUDA(cudaFuncSetAttribute(k_svd_jacobi_w<1024, 16, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        KV_CUDA(cudaFuncSetAttribute(k_svd_jacobi_w<1024, 16, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        KV_CUDA(cudaFuncSetAttribute(k_svd_jacobi_w<1024, 16, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
         smem_bytes = bytes;
     });
     int64_t max_pq = 0;
@@ -525,13 +525,15 @@ void svd_jacobi_f32(const SvdPlan &p, const double2 *T64, float2 *T, int *status
     const int elems = (int)std::min<int64_t>(max_pq, cap);
     k_to_f32<<<std::max(1, ctx().num_sms * 4), 256, 0, ctx().stream>>>(T64, T, p.t_elems);
     counted();
-    if (max_p <= 16 * kJacEpl)
-        k_svd_jacobi_w<1024, 16, kJacEpl><<<(unsigned)p.secs.size(), 1024, (size_t)elems * sizeof(float2),
-                                            ctx().stream>>>(p.d_secs.as<SvdSector>(), T, status, max_sweeps, tol,
-                                                            elems);
-    else
-        k_svd_jacobi_w<1024, 16, 0><<<(unsigned)p.secs.size(), 1024, (size_t)elems * sizeof(float2), ctx().stream>>>(
+    // elements per lane from the longest column of the launch (16 lanes a pair)
+    auto launch = [&](auto kernel) {
+        kernel<<<(unsigned)p.secs.size(), 1024, (size_t)elems * sizeof(float2), ctx().stream>>>(
             p.d_secs.as<SvdSector>(), T, status, max_sweeps, tol, elems);
+    };
+    if (max_p <= 32) launch(k_svd_jacobi_w<1024, 16, 2>);
+    else if (max_p <= 64) launch(k_svd_jacobi_w<1024, 16, 4>);
+    else if (max_p <= 128) launch(k_svd_jacobi_w<1024, 16, 8>);
+    else launch(k_svd_jacobi_w<1024, 16, 0>);
     counted();
     KV_CUDA(cudaGetLastError());
 }
