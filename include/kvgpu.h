@@ -154,7 +154,8 @@ int kv_tdvp_create(int nsites, const kv_tensor *mps, const kv_tensor *mpo, doubl
 int kv_tdvp_sweep(kv_tdvp s, int mode);
 /* New handle with a copy of the current site tensor i. */
 int kv_tdvp_site(kv_tdvp s, int i, kv_tensor *out);
-/* Timings of the last sweep: per-module device time in ms in the order
+/* Timings of the last one- or two-site sweep (a global-Krylov step leaves
+ * them as they were): per-module device time in ms in the order
  * Evl-0, Evl-1, Evl-2, SVD, Update, Sweep (the reference's Timer modules,
  * util/timer.h:19-66, holstein/tdvp.h:85-106), the whole sweep's device
  * time, the algorithmic flop count (8*M*N*K summed over every zgemm the

@@ -57,6 +57,20 @@ void sync() {
     KV_REQUIRE(st == KV_OK, st, "a tensor-core GEMM wait timed out");
 }
 
+// CUDA events owned by one call, destroyed on every exit path.
+struct Events {
+    std::vector<cudaEvent_t> ev;
+    cudaEvent_t make(unsigned flags) {
+        cudaEvent_t e;
+        KV_CUDA(cudaEventCreateWithFlags(&e, flags));
+        ev.push_back(e);
+        return e;
+    }
+    ~Events() {
+        for (auto e : ev) cudaEventDestroy(e);
+    }
+};
+
 // Worker contexts of kv_sweep_batched, kept between calls so their plan
 // caches stay warm; closed by kv_shutdown.
 std::vector<std::unique_ptr<kv::Context>> g_workers;
@@ -333,44 +347,54 @@ int kv_sweep_batched(int n_chains, const kv_tdvp *chains, int mode, int steps, i
             load[w] += cost[i];
         }
         // every worker stream starts after everything on the main stream
-        cudaEvent_t t0 = kv::prof_event(), t1 = kv::prof_event();
+        Events ev;
+        cudaEvent_t t0 = ev.make(cudaEventDefault), t1 = ev.make(cudaEventDefault);
         KV_CUDA(cudaEventRecord(t0, m.stream));
         std::vector<cudaEvent_t> done(nw);
-        for (auto &e : done) KV_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        for (auto &e : done) e = ev.make(cudaEventDisableTiming);
         std::vector<int> code(n_chains, KV_OK), wcode(nw, KV_OK);
         std::vector<std::string> msg(n_chains), wmsg(nw);
         std::vector<std::thread> th;
-        for (int w = 0; w < nw; ++w)
-            th.emplace_back([&, w] {
-                kv::Context *c = g_workers[w].get();
-                wcode[w] = guard([&] {
-                    KV_CUDA(cudaSetDevice(c->device));
-                    KV_CUDA(cudaStreamWaitEvent(c->stream, t0, 0));
-                });
-                if (wcode[w] != KV_OK) {
-                    wmsg[w] = g_err;
-                    return;
-                }
-                kv::bind_thread_context(c);
-                for (int i : assign[w]) {
-                    kv::Tdvp &t = *chains[i]->s;
-                    code[i] = guard([&] {
-                        for (int s = 0; s < steps; ++s) {
-                            if (mode == 0) t.global_krylov();
-                            else if (mode == 1) t.one_site();
-                            else t.two_site();
-                        }
-                    });
-                    if (code[i] != KV_OK) msg[i] = g_err;
-                }
-                wcode[w] = guard([&] {
-                    KV_CUDA(cudaEventRecord(done[w], c->stream));
-                    KV_CUDA(cudaStreamSynchronize(c->stream));
-                });
-                if (wcode[w] != KV_OK) wmsg[w] = g_err;
-                kv::bind_thread_context(nullptr);
+        auto join_all = [&] {
+            for (auto &x : th)
+                if (x.joinable()) x.join();
+        };
+        auto body = [&](int w) {
+            kv::Context *c = g_workers[w].get();
+            wcode[w] = guard([&] {
+                KV_CUDA(cudaSetDevice(c->device));
+                KV_CUDA(cudaStreamWaitEvent(c->stream, t0, 0));
             });
-        for (auto &t : th) t.join();
+            if (wcode[w] != KV_OK) {
+                wmsg[w] = g_err;
+                return;
+            }
+            kv::bind_thread_context(c);
+            for (int i : assign[w]) {
+                kv::Tdvp &t = *chains[i]->s;
+                code[i] = guard([&] {
+                    for (int s = 0; s < steps; ++s) {
+                        if (mode == 0) t.global_krylov();
+                        else if (mode == 1) t.one_site();
+                        else t.two_site();
+                    }
+                });
+                if (code[i] != KV_OK) msg[i] = g_err;
+            }
+            wcode[w] = guard([&] {
+                KV_CUDA(cudaEventRecord(done[w], c->stream));
+                KV_CUDA(cudaStreamSynchronize(c->stream));
+            });
+            if (wcode[w] != KV_OK) wmsg[w] = g_err;
+            kv::bind_thread_context(nullptr);
+        };
+        try {
+            for (int w = 0; w < nw; ++w) th.emplace_back(body, w);
+        } catch (...) {  // a thread could not be started: wait for the others, then report
+            join_all();
+            throw;
+        }
+        join_all();
         for (int w = 0; w < nw; ++w) {
             m.launches += g_workers[w]->launches;
             g_workers[w]->launches = 0;
@@ -381,9 +405,6 @@ int kv_sweep_batched(int n_chains, const kv_tdvp *chains, int mode, int steps, i
         float ms = 0.0f;
         KV_CUDA(cudaEventElapsedTime(&ms, t0, t1));
         if (device_ms) *device_ms = ms;
-        for (auto &e : done) cudaEventDestroy(e);
-        m.ev_free.push_back(t0);
-        m.ev_free.push_back(t1);
         for (int w = 0; w < nw; ++w)
             KV_REQUIRE(wcode[w] == KV_OK, wcode[w], "batched sweep, stream " + std::to_string(w) + ": " + wmsg[w]);
         for (int i = 0; i < n_chains; ++i)

@@ -294,18 +294,22 @@ __device__ __forceinline__ long long combine(const float *p) {
     return (u << 8) + __float2int_rn(p[4]);
 }
 
-__global__ void __launch_bounds__(NTHREADS, 1) k_gemm_tc(const GemmTile *__restrict__ tiles, const SegX *__restrict__ segs,
+// Persistent: CTA b takes tiles b, b + gridDim.x, ...; each role walks the
+// same tile sequence and keeps its mbarrier phase counters across tiles, so
+// the producer streams the next tile's panels while the current tile drains.
+__device__ __forceinline__ bool tile_active(const GemmTile &t, const SegX *segs, int step) {
+    for (int s = t.seg_begin; s < t.seg_end; ++s)
+        if (segs[s].entry <= step) return true;
+    return false;
+}
+
+__global__ void __launch_bounds__(NTHREADS, 1) k_gemm_tc(const GemmTile *__restrict__ tiles, int ntiles,
+                                                    const SegX *__restrict__ segs,
                                                     const __half *__restrict__ Apl, const __half *__restrict__ Bpl,
                                                     const int *__restrict__ Aexp, const int *__restrict__ Bexp,
                                                     double2 *__restrict__ C, const int *skip, int *err, int step,
                                                     int write_inactive) {
     if (skip && *skip) return;
-    {  // tiles without an active segment at this step: zeros, or nothing for intermediates
-        const GemmTile t0 = tiles[blockIdx.x];
-        bool any = false;
-        for (int s = t0.seg_begin; s < t0.seg_end && !any; ++s) any = segs[s].entry <= step;
-        if (!any && !write_inactive) return;
-    }
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t *sA = smem;
@@ -316,9 +320,6 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_gemm_tc(const GemmTile *__restr
     int *s_ecol = (int *)(tslot + 4);  // [BN] largest column exponent over the tile's segments
     int *s_fcol = s_ecol + BN;         // [EPI_WARPS][EPI_COLS] each epilogue warp's copy of a segment's
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const GemmTile t = tiles[blockIdx.x];
-    const int nseg = t.seg_end - t.seg_begin;
-    const int rt = t.m0 / BM, nt = t.n0 / BN;
 
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
@@ -347,19 +348,25 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_gemm_tc(const GemmTile *__restr
             int it = 0;
             int uses[STAGES] = {0, 0, 0};
             bool ok = true;
-            for (int s = t.seg_begin; s < t.seg_end && ok; ++s) {
-                const SegX g = segs[s];
-                if (g.entry > step) continue;
-                const __half *ap = Apl + g.a_pan + (int64_t)rt * g.nkc * A_PANEL;
-                const __half *bp = Bpl + g.b_pan + (int64_t)nt * g.nkc * B_PANEL;
-                for (int kc = 0; kc < g.nkc; ++kc, ++it) {
-                    const int st = it % STAGES;
-                    const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
-                    if (!mbar_wait(smem_u32(empty + st), ph ^ 1u)) { ok = false; break; }
-                    mbar_expect_tx(smem_u32(full + st), (uint32_t)(A_BYTES + B_BYTES));
-                    bulk_g2s(smem_u32(sA + st * A_BYTES), ap + (int64_t)kc * A_PANEL, A_BYTES, smem_u32(full + st));
-                    bulk_g2s(smem_u32(sB + st * B_BYTES), bp + (int64_t)kc * B_PANEL, B_BYTES, smem_u32(full + st));
-                    ++uses[st];
+            for (int ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
+                const GemmTile t = tiles[ti];
+                const int rt = t.m0 / BM, nt = t.n0 / BN;
+                for (int s = t.seg_begin; s < t.seg_end && ok; ++s) {
+                    const SegX g = segs[s];
+                    if (g.entry > step) continue;
+                    const __half *ap = Apl + g.a_pan + (int64_t)rt * g.nkc * A_PANEL;
+                    const __half *bp = Bpl + g.b_pan + (int64_t)nt * g.nkc * B_PANEL;
+                    for (int kc = 0; kc < g.nkc; ++kc, ++it) {
+                        const int st = it % STAGES;
+                        const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+                        if (!mbar_wait(smem_u32(empty + st), ph ^ 1u)) { ok = false; break; }
+                        mbar_expect_tx(smem_u32(full + st), (uint32_t)(A_BYTES + B_BYTES));
+                        bulk_g2s(smem_u32(sA + st * A_BYTES), ap + (int64_t)kc * A_PANEL, A_BYTES,
+                                 smem_u32(full + st));
+                        bulk_g2s(smem_u32(sB + st * B_BYTES), bp + (int64_t)kc * B_PANEL, B_BYTES,
+                                 smem_u32(full + st));
+                        ++uses[st];
+                    }
                 }
             }
             if (!ok) atomicExch(err, 1);
@@ -372,39 +379,42 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_gemm_tc(const GemmTile *__restr
         if (lane == 0) {
             int it = 0, grp = 0;
             bool ok = true;
-            for (int s = t.seg_begin; s < t.seg_end && ok; ++s) {
-                if (segs[s].entry > step) continue;
-                const int nkc = segs[s].nkc;
-                for (int kc0 = 0; kc0 < nkc && ok; kc0 += GKC, ++grp) {
-                    // the epilogue has read the previous group's accumulators
-                    if (!mbar_wait(smem_u32(acce), ((uint32_t)grp & 1u) ^ 1u)) { ok = false; break; }
-                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                    const int kc1 = min(nkc, kc0 + GKC);
-                    for (int kc = kc0; kc < kc1; ++kc, ++it) {
-                        const int st = it % STAGES;
-                        const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
-                        if (!mbar_wait(smem_u32(full + st), ph)) { ok = false; break; }
+            for (int ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
+                const GemmTile t = tiles[ti];
+                for (int s = t.seg_begin; s < t.seg_end && ok; ++s) {
+                    if (segs[s].entry > step) continue;
+                    const int nkc = segs[s].nkc;
+                    for (int kc0 = 0; kc0 < nkc && ok; kc0 += GKC, ++grp) {
+                        // the epilogue has read the previous group's accumulators
+                        if (!mbar_wait(smem_u32(acce), ((uint32_t)grp & 1u) ^ 1u)) { ok = false; break; }
                         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                        const uint32_t a0 = smem_u32(sA + st * A_BYTES), b0 = smem_u32(sB + st * B_BYTES);
+                        const int kc1 = min(nkc, kc0 + GKC);
+                        for (int kc = kc0; kc < kc1; ++kc, ++it) {
+                            const int st = it % STAGES;
+                            const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+                            if (!mbar_wait(smem_u32(full + st), ph)) { ok = false; break; }
+                            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                            const uint32_t a0 = smem_u32(sA + st * A_BYTES), b0 = smem_u32(sB + st * B_BYTES);
 #pragma unroll
-                        for (int c = 0; c < NCOMP; ++c)
+                            for (int c = 0; c < NCOMP; ++c)
 #pragma unroll
-                            for (int o = 0; o < NORD; ++o) {
-                                const uint32_t d = tmem + (uint32_t)((c * NORD + o) * BN);
+                                for (int o = 0; o < NORD; ++o) {
+                                    const uint32_t d = tmem + (uint32_t)((c * NORD + o) * BN);
 #pragma unroll
-                                for (int i = (o > NDIG - 1 ? o - (NDIG - 1) : 0); i <= (o < NDIG - 1 ? o : NDIG - 1);
-                                     ++i) {
-                                    const int jj = o - i;
-                                    const bool first = (i == (o > NDIG - 1 ? o - (NDIG - 1) : 0));
-                                    const uint64_t ad = make_desc(a0 + (c * NDIG + i) * PLANE_A, 128, 256);
-                                    const uint64_t bd = make_desc(b0 + (c * NDIG + jj) * PLANE_B, 128, 256);
-                                    mma_f16(d, ad, bd, (first && kc == kc0) ? 0u : 1u);
+                                    for (int i = (o > NDIG - 1 ? o - (NDIG - 1) : 0);
+                                         i <= (o < NDIG - 1 ? o : NDIG - 1); ++i) {
+                                        const int jj = o - i;
+                                        const bool first = (i == (o > NDIG - 1 ? o - (NDIG - 1) : 0));
+                                        const uint64_t ad = make_desc(a0 + (c * NDIG + i) * PLANE_A, 128, 256);
+                                        const uint64_t bd = make_desc(b0 + (c * NDIG + jj) * PLANE_B, 128, 256);
+                                        mma_f16(d, ad, bd, (first && kc == kc0) ? 0u : 1u);
+                                    }
                                 }
-                            }
-                        mma_commit(smem_u32(empty + st));  // stage free once these MMAs are done
+                            mma_commit(smem_u32(empty + st));  // stage free once these MMAs are done
+                        }
+                        if (!ok) break;
+                        mma_commit(smem_u32(accf));  // accumulators ready for the drain
                     }
-                    if (!ok) break;
-                    mma_commit(smem_u32(accf));  // accumulators ready for the drain
                 }
             }
             if (!ok) atomicExch(err, 1);
@@ -421,76 +431,84 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_gemm_tc(const GemmTile *__restr
         const int m = q * 32 + lane;
         const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16);
         int *fw = s_fcol + (warp - 2) * EPI_COLS;  // this warp's copy of the segment's column exponents
-        int erow = kZeroExp;
-        for (int s = t.seg_begin; s < t.seg_end; ++s)
-            if (segs[s].entry <= step) erow = max(erow, Aexp[segs[s].a_exp + t.m0 + m]);
-        if (warp == 2) {
-            int ec = kZeroExp;
-            for (int s = t.seg_begin; s < t.seg_end; ++s)
-                if (segs[s].entry <= step) ec = max(ec, Bexp[segs[s].b_exp + t.n0 + lane]);
-            s_ecol[lane] = ec;
-        }
-        epi_bar();  // the only barrier of the epilogue warps: reached by all of them unconditionally
-        long long cr[EPI_COLS], ci[EPI_COLS];
-#pragma unroll
-        for (int c = 0; c < EPI_COLS; ++c) cr[c] = ci[c] = 0;
-        bool ok = true;
+        bool ok = true;  // warp-uniform; after a timed-out wait the warp stops waiting but keeps the barriers
         int grp = 0;
-        for (int sl = 0; sl < nseg && ok; ++sl) {
-            const SegX g = segs[t.seg_begin + sl];
-            if (g.entry > step) continue;
-            // column shifts of this segment, into the warp's own shared-memory slots
-            if (lane < EPI_COLS) fw[lane] = s_ecol[c_lo + lane] - Bexp[g.b_exp + t.n0 + c_lo + lane];
-            __syncwarp();
-            const int shr = erow - Aexp[g.a_exp + t.m0 + m];
-            for (int kc0 = 0; kc0 < g.nkc; kc0 += GKC, ++grp) {
-                // warp-uniform decision: tcgen05.ld below is a warp-wide instruction
-                if (!__all_sync(0xFFFFFFFFu, mbar_wait(smem_u32(accf), (uint32_t)grp & 1u))) { ok = false; break; }
-                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x) {
+            const GemmTile t = tiles[ti];
+            const bool act = tile_active(t, segs, step);
+            if (!act && !write_inactive) continue;  // the same for every epilogue warp
+            const int nseg = t.seg_end - t.seg_begin;
+            int erow = kZeroExp;
+            for (int s = t.seg_begin; s < t.seg_end; ++s)
+                if (segs[s].entry <= step) erow = max(erow, Aexp[segs[s].a_exp + t.m0 + m]);
+            if (warp == 2) {
+                int ec = kZeroExp;
+                for (int s = t.seg_begin; s < t.seg_end; ++s)
+                    if (segs[s].entry <= step) ec = max(ec, Bexp[segs[s].b_exp + t.n0 + lane]);
+                s_ecol[lane] = ec;
+            }
+            epi_bar();  // s_ecol written; reached by every epilogue warp for every tile
+            long long cr[EPI_COLS], ci[EPI_COLS];
 #pragma unroll
-                for (int c0 = 0; c0 < EPI_COLS; c0 += 4) {
-                    long long I[NCOMP][4];
+            for (int c = 0; c < EPI_COLS; ++c) cr[c] = ci[c] = 0;
+            for (int sl = 0; sl < nseg; ++sl) {
+                const SegX g = segs[t.seg_begin + sl];
+                if (g.entry > step) continue;
+                // column shifts of this segment, into the warp's own shared-memory slots
+                if (lane < EPI_COLS) fw[lane] = s_ecol[c_lo + lane] - Bexp[g.b_exp + t.n0 + c_lo + lane];
+                __syncwarp();
+                const int shr = erow - Aexp[g.a_exp + t.m0 + m];
+                for (int kc0 = 0; kc0 < g.nkc; kc0 += GKC, ++grp) {
+                    // warp-uniform decision: tcgen05.ld below is a warp-wide instruction
+                    if (ok && !__all_sync(0xFFFFFFFFu, mbar_wait(smem_u32(accf), (uint32_t)grp & 1u))) ok = false;
+                    if (!ok) continue;
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
-                    for (int c = 0; c < NCOMP; ++c) {
-                        float a[NORD][4];
+                    for (int c0 = 0; c0 < EPI_COLS; c0 += 4) {
+                        long long I[NCOMP][4];
 #pragma unroll
-                        for (int o = 0; o < NORD; ++o)
-                            tmem_ld4(trow + (uint32_t)((c * NORD + o) * BN + c_lo + c0), a[o]);
-                        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                        for (int c = 0; c < NCOMP; ++c) {
+                            float a[NORD][4];
+#pragma unroll
+                            for (int o = 0; o < NORD; ++o)
+                                tmem_ld4(trow + (uint32_t)((c * NORD + o) * BN + c_lo + c0), a[o]);
+                            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                            for (int jx = 0; jx < 4; ++jx) {
+                                float p[NORD];
+#pragma unroll
+                                for (int o = 0; o < NORD; ++o) p[o] = a[o][jx];
+                                I[c][jx] = combine(p);
+                            }
+                        }
 #pragma unroll
                         for (int jx = 0; jx < 4; ++jx) {
-                            float p[NORD];
-#pragma unroll
-                            for (int o = 0; o < NORD; ++o) p[o] = a[o][jx];
-                            I[c][jx] = combine(p);
+                            const int col = c0 + jx;
+                            const int sh = shr + fw[col];
+                            cr[col] += sra_round(I[0][jx] - I[1][jx], sh);
+                            ci[col] += sra_round(I[2][jx] - I[0][jx] - I[1][jx], sh);
                         }
                     }
+                    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                    mbar_arrive(smem_u32(acce));
+                }
+                __syncwarp();  // fw is rewritten for the next segment
+            }
+            const int gm = t.m0 + m;
+            if (ok && gm < t.M) {
+                double2 *crow = C + t.c_off + (int64_t)gm * t.ldc;
 #pragma unroll
-                    for (int jx = 0; jx < 4; ++jx) {
-                        const int col = c0 + jx;
-                        const int sh = shr + fw[col];
-                        cr[col] += sra_round(I[0][jx] - I[1][jx], sh);
-                        ci[col] += sra_round(I[2][jx] - I[0][jx] - I[1][jx], sh);
+                for (int c = 0; c < EPI_COLS; ++c) {
+                    const int gn = t.n0 + c_lo + c;
+                    if (gn < t.N) {
+                        const int sc = erow + s_ecol[c_lo + c] - 2 * FRAC + 16;
+                        crow[gn] = make_double2(i64_ldexp(cr[c], sc), i64_ldexp(ci[c], sc));
                     }
                 }
-                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-                mbar_arrive(smem_u32(acce));
             }
-            __syncwarp();  // fw is rewritten for the next segment
+            epi_bar();  // every warp has used s_ecol before the next tile rewrites it
         }
         if (!ok && lane == 0) atomicExch(err, 1);
-        const int gm = t.m0 + m;
-        if (ok && gm < t.M) {
-            double2 *crow = C + t.c_off + (int64_t)gm * t.ldc;
-#pragma unroll
-            for (int c = 0; c < EPI_COLS; ++c) {
-                const int gn = t.n0 + c_lo + c;
-                if (gn < t.N) {
-                    const int sc = erow + s_ecol[c_lo + c] - 2 * FRAC + 16;
-                    crow[gn] = make_double2(i64_ldexp(cr[c], sc), i64_ldexp(ci[c], sc));
-                }
-            }
-        }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -613,9 +631,11 @@ void launch_gemm_mixed(const GemmPlan &p, const double2 *A, const double2 *B, do
         KV_CUDA(cudaGetLastError());
         ++n;
     }
-    k_gemm_tc<<<(unsigned)p.tiles.size(), NTHREADS, SMEM_BYTES, c.stream>>>(
-        p.d_tiles.as<GemmTile>(), p.d_xsegs.as<SegX>(), ap.as<__half>(), bp.as<__half>(), ae.as<int>(), be.as<int>(),
-        C, skip, g_err, step, p.write_inactive ? 1 : 0);
+    // persistent: one CTA per SM at most (the kernel holds all of an SM's tensor memory)
+    const int ntiles = (int)p.tiles.size();
+    k_gemm_tc<<<(unsigned)std::min(ntiles, c.num_sms), NTHREADS, SMEM_BYTES, c.stream>>>(
+        p.d_tiles.as<GemmTile>(), ntiles, p.d_xsegs.as<SegX>(), ap.as<__half>(), bp.as<__half>(), ae.as<int>(),
+        be.as<int>(), C, skip, g_err, step, p.write_inactive ? 1 : 0);
     KV_CUDA(cudaGetLastError());
     counted(n + 1);
     // the slices are freed stream-ordered after the GEMM
