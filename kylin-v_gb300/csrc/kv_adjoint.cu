@@ -29,18 +29,6 @@ __global__ void k_conj_scale(const double2 *__restrict__ in, double2 *__restrict
     }
 }
 
-// out[dst + i] += in[src + i] for each (src, dst, size) triple; one CTA per block
-__global__ void k_block_acc(const int64_t *__restrict__ desc, const double2 *__restrict__ in,
-                            double2 *__restrict__ out) {
-    const int64_t src = desc[3 * blockIdx.x], dst = desc[3 * blockIdx.x + 1], n = desc[3 * blockIdx.x + 2];
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
-        const double2 a = in[src + i];
-        double2 &o = out[dst + i];
-        o.x += a.x;
-        o.y += a.y;
-    }
-}
-
 int grid(int64_t n) {
     const int64_t g = (n + 255) / 256;
     return (int)std::max<int64_t>(1, std::min<int64_t>(g, (int64_t)ctx().num_sms * 8));
@@ -64,24 +52,7 @@ TensorP conj_scale(const DTensor &t, double s, bool conj) {
 TensorP cj(const DTensor &t) { return conj_scale(t, 1.0, true); }
 
 // a + b over the union of their blocks
-TensorP add(const DTensor &a, const DTensor &b) {
-    Meta m = a.meta;
-    for (auto &blk : b.meta.blocks) m.add(blk);
-    auto out = DTensor::make(m, true);
-    for (const DTensor *x : {&a, &b}) {
-        std::vector<int64_t> desc;
-        for (auto &blk : x->meta.blocks) {
-            const int j = out->meta.find(blk);
-            desc.insert(desc.end(), {blk.off, out->meta.blocks[j].off, blk.size});
-        }
-        if (desc.empty()) continue;
-        DevBuf d = upload_vec(desc);
-        k_block_acc<<<(unsigned)(desc.size() / 3), 256, 0, ctx().stream>>>(d.as<int64_t>(), x->data(), out->data());
-        counted();
-        KV_CUDA(cudaGetLastError());
-    }
-    return out;
-}
+TensorP add(const DTensor &a, const DTensor &b) { return op_add_scaled(a, b, cplx(1.0, 0.0)); }
 
 TensorP mix(const DTensor &t, const DTensor &W, int lead) { return op_mix(t, W, lead); }
 

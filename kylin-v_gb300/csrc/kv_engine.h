@@ -85,6 +85,8 @@ TensorP op_permute(const DTensor &t, const std::vector<int> &ax);
 TensorP op_mix(const DTensor &t, const DTensor &W, int lead);
 TensorP boundary_env(int dir0, int q);
 TensorP op_scale(const DTensor &t, cplx s);  // s * t
+// t + v s over the union of the blocks (equal keys merged, t's blocks first)
+TensorP op_add_scaled(const DTensor &t, const DTensor &s, cplx v);
 // global_main (holstein/krylov.h:199-283) on the MPO Hc (already scaled by dt)
 void global_main(const std::vector<TensorP> &Hc, std::vector<TensorP> &mps, int max_iter, double tol_exp,
                  double tol_svd, int maxd, int precision);

@@ -128,9 +128,13 @@ cplx toverlap(const DTensor &ori, const DTensor &oth) {
 
 double tnorm(const DTensor &t) { return std::sqrt(std::max(0.0, toverlap(t, t).real())); }
 
+TensorP add_scaled(const DTensor &t, const DTensor &s, cplx v) { return op_add_scaled(t, s, v); }
+
+}  // namespace
+
 // t + v s with the merge rule of push_back_ch (holstein/tensor.h:172-185):
 // blocks of t in order, then the new keys of s appended
-TensorP add_scaled(const DTensor &t, const DTensor &s, cplx v) {
+TensorP op_add_scaled(const DTensor &t, const DTensor &s, cplx v) {
     Meta m = t.meta;
     for (auto &b : s.meta.blocks) m.add(b);
     auto out = DTensor::make(m, true);
@@ -147,6 +151,8 @@ TensorP add_scaled(const DTensor &t, const DTensor &s, cplx v) {
     }
     return out;
 }
+
+namespace {
 
 std::map<int, int> leg_dims(const Meta &m, int ax) {
     std::map<int, int> r;
