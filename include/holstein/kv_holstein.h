@@ -294,7 +294,7 @@ class TDVP {
 
     void total_start(const array<INT, 4> &r) {
         if (r[2] != 0) {
-            cout << "The SA-1TDVP stage is not available in this build." << endl;
+            cout << "The SA-1TDVP stage is not available in libkvgpu." << endl;
             exit(1);
         }
         INT swp = 0;
