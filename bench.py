@@ -231,6 +231,7 @@ def run_ours(args):
     host_sweep_ms, plans_built, plan_ms = 0.0, 0, 0.0
     barrier()
     n0 = G.launches()
+    G.svd_stats(reset=True)
     G.profile(True)
     with Clocks(local) as clk:
         for _ in range(args.steps):
@@ -253,6 +254,7 @@ def run_ours(args):
     prof = G.profile_read()
     G.profile(False)
     launches = G.launches() - n0
+    svd = G.svd_stats(reset=True)
     clocks = clk.summary()
     tot_flops, max_ms = flops, dev_ms
     if ws > 1:
@@ -323,6 +325,9 @@ def run_ours(args):
                      "peak_source": f"dense FP16/BF16 tensor rate, {src} ({bf16:.1f} TFLOP/s bf16); "
                                     "achieved counts the reference's 8MNK flops of the block pairs"},
         "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
+        "svd_sectors": {"per_step": svd["sectors"] / args.steps, "mean_columns": svd["mean_columns"],
+                        "mean_rank": svd["mean_rank"], "mean_jacobi_sweeps": svd["mean_sweeps"],
+                        "max_jacobi_sweeps": svd["max_sweeps"]},
     }
     if not args.no_compare:
         line["fp64_compare"] = compare_fp64(args, G)

@@ -35,25 +35,33 @@ extern "C" {
 #define KV_EINVAL     -1  /* bad argument (rank, shapes, directions, mode)   */
 #define KV_ECUDA      -2  /* CUDA runtime error                             */
 #define KV_ENOMEM     -3  /* device allocation failed                       */
-#define KV_ENONFINITE -4  /* NaN/Inf in a Lanczos norm or singular value    */
+#define KV_ENONFINITE -4  /* NaN/Inf in an operand, a norm or a singular value */
 #define KV_ETIMEOUT   -5  /* a bounded device wait gave up                  */
 #define KV_ENOTINIT   -6  /* kv_init not called                            */
 #define KV_EMISMATCH  -7  /* contracted legs' directions mismatch           */
 
 /* ------------------------------------------------------- arithmetic modes */
 /* KV_FP64: every contraction in complex128 on the CUDA cores.
- * KV_MIXED_TF32 (the mixed-precision path; the name is kept from the API's
- *   first form): block contractions as 3M (Gauss) real products on the
- *   tcgen05 tensor cores.  Each operand is rounded to 30-bit fixed point
- *   against a per-row (A) or per-column (B) power of two and split into four
- *   balanced 8-bit digits, held exactly in FP16; the digit products of orders
- *   0-4 accumulate exactly in FP32 tensor memory and are combined in int64,
- *   so a product carries about 2^-29 relative error per operand, below a
- *   TF32 or BF16x3 split.  Lanczos, norms, the tridiagonal exponential and
- *   MPO mixing stay FP64; the SVD picks the kept subspace with FP32 Jacobi
- *   and rebuilds the kept factors in FP64 (Cholesky-QR, exact projection). */
-#define KV_FP64        0
-#define KV_MIXED_TF32  1
+ * KV_MIXED_3M_DIGITS (the mixed-precision path): block contractions as 3M
+ *   (Gauss) real products on the tcgen05 tensor cores.  Each operand is
+ *   rounded to 30-bit fixed point against a per-row (A) or per-column (B)
+ *   power of two and split into four balanced 8-bit digits, held exactly in
+ *   FP16; the digit products of orders 0-4 accumulate exactly in FP32 tensor
+ *   memory and are combined in int64, so a product carries about 2^-29
+ *   relative error per operand, below a TF32 or BF16x3 split.  Lanczos,
+ *   norms, the tridiagonal exponential and MPO mixing stay FP64; the SVD
+ *   picks the kept subspace in FP32 and rebuilds the kept factors in FP64
+ *   (Cholesky-QR, exact projection).
+ * KV_MIXED_TF32, KV_MIXED_3M_TF32 and KV_MIXED_3M_BF16X3 are other names of
+ *   the same mode, kept so code written against the mixed-precision names
+ *   of the survey compiles: no TF32 or BF16 split is implemented, because
+ *   the digit products are more accurate than either at the same tensor
+ *   pipe cost per exact product. */
+#define KV_FP64             0
+#define KV_MIXED_3M_DIGITS  1
+#define KV_MIXED_TF32       KV_MIXED_3M_DIGITS
+#define KV_MIXED_3M_TF32    KV_MIXED_3M_DIGITS
+#define KV_MIXED_3M_BF16X3  KV_MIXED_3M_DIGITS
 /* one part mixed, the other FP64 (to attribute mixed-precision error):
  * KV_MIXED_GEMM = tensor-core contractions + FP64 SVD,
  * KV_MIXED_SVD  = FP64 contractions + mixed SVD */
@@ -195,6 +203,26 @@ int kv_sweep_batched(int n_chains, const kv_tdvp *chains, int mode, int steps, i
 int kv_profile(int enable);
 int kv_profile_read(double *gemm_ms, double *gemm_ref_flops, long long *gemm_launches);
 int kv_counters(long long *launches);
+/* Charge sectors factorised by the block SVD on the calling thread's stream
+ * since kv_init (or the last reset): their count, summed column counts, summed
+ * ranks the mixed path's QR reduction kept (min(rows, columns) where none
+ * ran), summed Jacobi sweeps and the largest sweep count of one sector.
+ * reset != 0 clears the counters after reading them.  No reference
+ * counterpart. */
+int kv_svd_stats(int reset, long long *sectors, long long *columns, long long *rank, long long *sweeps,
+                 int *max_sweeps);
+/* Test hook for the failure path of the tensor-core GEMM; no reference
+ * counterpart.  kv_debug_gemm_stall(1): until called with 0, every
+ * tensor-core GEMM issues no operand copies and gives up each wait after a
+ * short limit, so its first wait runs out with nothing in flight; the kernel
+ * then frees its tensor memory and returns, and the call reports KV_ETIMEOUT.
+ * Calls after kv_debug_gemm_stall(0) run normally. */
+int kv_debug_gemm_stall(int on);
+/* Test hook; no reference counterpart.  Bytes of the device's default memory
+ * pool (where the library's stream-ordered allocations live) in use now and
+ * at the high-water mark; reset_high != 0 first resets the mark to the
+ * current use.  A call that allocates nothing leaves the mark unchanged. */
+int kv_debug_pool_usage(int reset_high, long long *used_current, long long *used_high);
 
 /* State::canonicalize (holstein/state.h:166-185): an L->R SVD sweep then an
  * R->L one with truncation tol_svd / max_dim (the reference's defaults are 0
@@ -213,10 +241,15 @@ int kv_expectation(int nsites, const kv_tensor *bra, const kv_tensor *mpo, const
  * allocation.  Every intermediate (environments, MPO-mixing buffers, GEMM
  * task lists) lives in one static 64 MiB device array that each GPU loading
  * this library reserves until the process exits; a call whose scratch would
- * exceed 64 MiB (about a 30-site MPS at bond dimension 64) fails with
- * KV_ENOMEM.  The first call on a device looks up the array's address
- * (cudaGetSymbolAddress) and must come before any stream capture.  All calls
- * share the array: calls that overlap on the GPU race.  The inputs are device
+ * exceed 64 MiB fails with KV_ENOMEM.  The scratch is set by the largest
+ * site, not by the number of sites (after each site only the new environment
+ * is kept): at most about 16*D^2*w*(2d+2) bytes for bond dimension D, MPO
+ * bond dimension w and local dimension d (charge blocks make it smaller),
+ * plus the task lists -- a D = 128, w = 7, d = 16 chain fits.  The first call
+ * on a device looks up the array's address (cudaGetSymbolAddress, under a
+ * lock, so first calls from several threads are safe) and must come before
+ * any stream capture.  All calls share the array: calls that overlap on the
+ * GPU race.  The inputs are device
  * tensors the caller already holds; re/im are host doubles.  kv_init must
  * have been called. */
 int kv_expectation_noalloc(int nsites, const kv_tensor *bra, const kv_tensor *mpo, const kv_tensor *ket,

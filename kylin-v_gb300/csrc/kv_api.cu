@@ -22,6 +22,17 @@ struct kv_tdvp_s {
 namespace {
 thread_local std::string g_err;
 
+// A call that fails part-way can leave the device error word of the
+// tensor-core GEMM set (an Inf/NaN operand seen before the failure was
+// raised); it belongs to the failed call, so it is cleared, not reported by
+// the next one.
+void drop_pending_status() noexcept {
+    try {
+        if (kv::ctx().device >= 0) kv::mixed_gemm_status();
+    } catch (...) {
+    }
+}
+
 template <class F>
 int guard(F &&f) {
     try {
@@ -29,6 +40,7 @@ int guard(F &&f) {
         return KV_OK;
     } catch (const kv::Error &e) {
         g_err = e.what();
+        if (e.code != KV_ECUDA) drop_pending_status();
         return e.code;
     } catch (const std::bad_alloc &) {
         g_err = "host allocation failed";
@@ -54,7 +66,8 @@ kv_tensor wrap(kv::TensorP t) {
 void sync() {
     KV_CUDA(cudaStreamSynchronize(kv::ctx().stream));
     const int st = kv::mixed_gemm_status();
-    KV_REQUIRE(st == KV_OK, st, "a tensor-core GEMM wait timed out");
+    KV_REQUIRE(st == KV_OK, st, st == KV_ETIMEOUT ? "a tensor-core GEMM wait timed out"
+                                                  : "a tensor-core GEMM operand holds Inf or NaN");
 }
 
 // CUDA events owned by one call, destroyed on every exit path.
@@ -460,6 +473,46 @@ int kv_profile_read(double *gemm_ms, double *gemm_ref_flops, long long *gemm_lau
         if (gemm_launches) *gemm_launches = c.prof_launches;
         c.prof_ms = c.prof_flops = 0.0;
         c.prof_launches = 0;
+    });
+}
+
+int kv_debug_gemm_stall(int on) {
+    return guard([&] {
+        kv::require_init();
+        KV_CUDA(cudaStreamSynchronize(kv::ctx().stream));
+        kv::set_gemm_stall_test(on);
+    });
+}
+
+int kv_svd_stats(int reset, long long *sectors, long long *columns, long long *rank, long long *sweeps,
+                 int *max_sweeps) {
+    return guard([&] {
+        kv::require_init();
+        auto &v = kv::ctx().svd;
+        if (sectors) *sectors = v.sectors;
+        if (columns) *columns = v.columns;
+        if (rank) *rank = v.rank;
+        if (sweeps) *sweeps = v.sweeps;
+        if (max_sweeps) *max_sweeps = v.max_sweeps;
+        if (reset) v = kv::Context::SvdStats{};
+    });
+}
+
+int kv_debug_pool_usage(int reset_high, long long *used_current, long long *used_high) {
+    return guard([&] {
+        kv::require_init();
+        KV_CUDA(cudaStreamSynchronize(kv::ctx().stream));
+        cudaMemPool_t pool;
+        KV_CUDA(cudaDeviceGetDefaultMemPool(&pool, kv::ctx().device));
+        unsigned long long cur = 0, high = 0;
+        if (reset_high) {
+            unsigned long long zero = 0;  // resets the high-water mark to the current use
+            KV_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &zero));
+        }
+        KV_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &cur));
+        KV_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &high));
+        if (used_current) *used_current = (long long)cur;
+        if (used_high) *used_high = (long long)high;
     });
 }
 

@@ -762,6 +762,10 @@ TensorP op_lanczos(int nsite, const DTensor &L, const DTensor &psi, const DTenso
 // FP32 value that is rounding noise on an exact zero (up to ~1e-5 relative)
 // comes back near zero from the FP64 rebuild and is dropped there.
 constexpr double kMixedSvdFloor = 1e-6;
+// mixed mode: the QR reduction stops once every remaining row of a sector is
+// below this fraction of the sector's Frobenius norm (FP32 rounding level;
+// the dropped part is below ~1e-7 sqrt(rows) of the sector's norm)
+constexpr float kQrFloor = 1e-7f;
 
 struct Micro {
     std::array<int, kMaxRank> shape{}, qn{};
@@ -853,28 +857,46 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
     const size_t cb = mixed ? sizeof(float2) : sizeof(double2);
     DevBuf T(std::max<int64_t>(1, P.t_elems) * sizeof(double2));
     DevBuf Us(std::max<int64_t>(1, P.t_elems) * cb), V(std::max<int64_t>(1, P.v_elems) * cb);
-    DevBuf Vs(std::max<int64_t>(1, P.v_elems) * cb), T32(mixed ? std::max<int64_t>(1, P.t_elems) * cb : 16);
+    DevBuf Vs(std::max<int64_t>(1, P.v_elems) * cb);
     DevBuf S(std::max<int64_t>(1, P.s_elems) * sizeof(double));
-    DevBuf status(std::max<size_t>(1, P.secs.size()) * sizeof(int));
+    DevBuf status(std::max<size_t>(1, 2 * P.secs.size()) * sizeof(int));  // sweeps, then QR ranks
     svd_gather(P, A.data(), T.as<double2>());
+    bool qr_ranks = false;
     if (mixed) {
         // tolerance 1e-5 on the columns' cosines: a residual c_ij <= 1e-5 s_i s_j
         // tilts the kept subspace by ~1e-5 s_j / s_i, and the FP64 polish
-        // rebuilds the kept factor exactly from that subspace
-        svd_jacobi_f32(P, T.as<double2>(), T32.as<float2>(), status.as<int>(), 60, 1e-5f);
-        svd_finalize_f32(P, T32.as<float2>(), Us.as<float2>(), S.as<double>());
+        // rebuilds the kept factor exactly from that subspace.  Sectors that
+        // fit shared memory are first reduced to their numerical rank (rows
+        // below 1e-7 ||T||_F dropped by a pivoted Householder QR).
+        qr_ranks = svd_qrjacobi_f32(P, T.as<double2>(), Us.as<float2>(), S.as<double>(), status.as<int>(),
+                                    status.as<int>() + P.secs.size(), 60, 1e-5f, kQrFloor);
+        if (!qr_ranks) {
+            DevBuf T32(std::max<int64_t>(1, P.t_elems) * cb);
+            svd_jacobi_f32(P, T.as<double2>(), T32.as<float2>(), status.as<int>(), 60, 1e-5f);
+            svd_finalize_f32(P, T32.as<float2>(), Us.as<float2>(), S.as<double>());
+        }
     } else {
         svd_jacobi(P, T.as<double2>(), V.as<double2>(), status.as<int>(), 60, 1e-15);
         svd_finalize(P, T.as<double2>(), V.as<double2>(), Us.as<double2>(), Vs.as<double2>(), S.as<double>());
     }
     std::vector<double> sv(P.s_elems);
-    std::vector<int> st(P.secs.size());
+    std::vector<int> st(2 * P.secs.size());
     if (P.s_elems)
         KV_CUDA(cudaMemcpyAsync(sv.data(), S.p, P.s_elems * sizeof(double), cudaMemcpyDeviceToHost, ctx().stream));
     if (!st.empty())
         KV_CUDA(cudaMemcpyAsync(st.data(), status.p, st.size() * sizeof(int), cudaMemcpyDeviceToHost, ctx().stream));
     KV_CUDA(cudaStreamSynchronize(ctx().stream));
-    for (int x : st) KV_REQUIRE(x >= 0, KV_ETIMEOUT, "Jacobi SVD did not converge within the sweep limit");
+    {
+        auto &c = ctx();
+        for (size_t i = 0; i < P.secs.size(); ++i) {
+            KV_REQUIRE(st[i] >= 0, KV_ETIMEOUT, "Jacobi SVD did not converge within the sweep limit");
+            c.svd.sectors += 1;
+            c.svd.columns += P.secs[i].q;
+            c.svd.rank += qr_ranks ? st[P.secs.size() + i] : std::min(P.secs[i].p, P.secs[i].q);
+            c.svd.sweeps += st[i];
+            c.svd.max_sweeps = std::max(c.svd.max_sweeps, st[i]);
+        }
+    }
     for (double x : sv) KV_REQUIRE(std::isfinite(x), KV_ENONFINITE, "non-finite singular value");
     if (mixed) {
         // below kMixedSvdFloor of the sector's largest: zero
@@ -1319,7 +1341,8 @@ void Tdvp::end_sweep() {
     sweep_ms = sms;
     {
         const int st = mixed_gemm_status();
-        KV_REQUIRE(st == KV_OK, st, "a tensor-core GEMM wait timed out");
+        KV_REQUIRE(st == KV_OK, st, st == KV_ETIMEOUT ? "a tensor-core GEMM wait timed out"
+                                                      : "a tensor-core GEMM operand holds Inf or NaN");
     }
     for (auto &m : module_ms) m = 0.0;
     for (int i = 0; i < n_marks; ++i) {

@@ -76,6 +76,12 @@ struct Context {
     cudaEvent_t ring_ev[kRingChunks] = {};
     bool ring_live[kRingChunks] = {};
     PlanCache *plans = nullptr;
+    // charge sectors through the mixed/FP64 SVD: count, columns, rank
+    // reached by the QR reduction (else min(rows, columns)), Jacobi sweeps
+    struct SvdStats {
+        long long sectors = 0, columns = 0, rank = 0, sweeps = 0;
+        int max_sweeps = 0;
+    } svd;
     long long plans_built = 0;  // plan-cache misses
     double plan_ms = 0.0;       // host ms spent building those plans
 };
@@ -358,8 +364,12 @@ void run_gemm(const GemmPlan &g, const double2 *A, const double2 *B, double2 *C,
               const int *skip, const KrylovState *st = nullptr, int k = -1, double credit_flops = -1.0);
 void launch_gemm_mixed(const GemmPlan &p, const double2 *A, const double2 *B, double2 *C, double alpha,
                        const int *skip, int step = kAllSteps);
-// KV_ETIMEOUT if a tensor-core kernel's bounded wait gave up since the last call
+// KV_ETIMEOUT if a tensor-core kernel's bounded wait gave up, KV_ENONFINITE if
+// a sliced operand held an Inf or NaN, since the last call (then cleared)
 int mixed_gemm_status();
+// test hook: tensor-core GEMMs issue no copies and wait briefly, so their first
+// wait runs out with nothing in flight (kv_debug_gemm_stall)
+void set_gemm_stall_test(int on);
 void launch_mix(const MixPlan &p, const double2 *in, const double2 *W, double2 *out, const int *skip,
                 int step = kAllSteps);
 void launch_permute(const double2 *in, double2 *out, const std::vector<int64_t> &desc, int nblocks);

@@ -14,6 +14,7 @@ namespace kv {
 namespace {
 
 constexpr int KT = 256;
+constexpr double kMaxTridiagNorm = 1e5;  // largest ||T||_1 the Taylor sub-stepping accepts
 
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 
@@ -158,6 +159,10 @@ __global__ void __launch_bounds__(32) k_tridiag_exp(KrylovState *st, int reverse
     const int lane = threadIdx.x;
     const int n = st->iters;
     if (n <= 0) return;
+    if (st->status != KV_OK) {  // a non-finite Lanczos norm: no coefficients
+        if (lane < n) st->coef[lane] = make_double2(nan(""), 0.0);
+        return;
+    }
     const bool on = lane < n;
     const double a = on ? st->alpha[lane].x : 0.0;
     const double2 zero = make_double2(0.0, 0.0);
@@ -165,8 +170,12 @@ __global__ void __launch_bounds__(32) k_tridiag_exp(KrylovState *st, int reverse
     double2 bl = (on && lane >= 1) ? st->beta[lane - 1] : zero;  // T[lane][lane - 1] = conj(beta)
     bl.y = -bl.y;
     const double rs = warp_max(fabs(a) + sqrt(bu.x * bu.x + bu.y * bu.y) + sqrt(bl.x * bl.x + bl.y * bl.y));
-    if (!isfinite(rs)) {
+    // the sub-step count is ceil(||T||_1): a norm beyond kMaxTridiagNorm (far
+    // above any dt * H_eff of a physical chain) is reported as non-finite
+    // instead of looping over that many steps
+    if (!(rs <= kMaxTridiagNorm)) {
         if (on) st->coef[lane] = make_double2(nan(""), 0.0);
+        if (lane == 0) st->status = KV_ENONFINITE;
         return;
     }
     const int m = max(1, (int)ceil(rs));

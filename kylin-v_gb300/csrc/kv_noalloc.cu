@@ -11,12 +11,18 @@
 // already holds; the result is written to caller-provided host doubles.
 //
 // Set-up: the first call on a device resolves the array's device address with
-// cudaGetSymbolAddress (with that device current); make that first call
-// before any stream capture.  Every call reuses the same array, so calls that
-// overlap on the GPU (different threads or streams) race; buffers are written
-// before they are read, nothing relies on the array's previous contents.
+// cudaGetSymbolAddress (with that device current, under a mutex, so first
+// calls from several threads are safe); make that first call before any
+// stream capture.  Every call reuses the same array, so calls that overlap on
+// the GPU (different threads or streams) race; buffers are written before
+// they are read, nothing relies on the array's previous contents.
+//
+// Limit: the scratch needed is set by one site, not by the number of sites
+// (after each site only the new environment is kept): about
+// 16 * D^2 * w * (2 d + 2) bytes for bond dimension D, MPO bond dimension w
+// and local dimension d, plus the GEMM and mixing task lists.
 #include <cstring>
-#include <map>
+#include <mutex>
 #include <string>
 
 #include "kv_engine.h"
@@ -28,17 +34,20 @@ namespace {
 constexpr size_t kNoAllocBytes = size_t(64) << 20;  // 64 MiB
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
-std::map<int, char *> g_scratch_addr;  // device -> address of g_noalloc_scratch
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+char *g_scratch_addr[kMaxDevices] = {};  // device -> address of g_noalloc_scratch
 
 char *scratch_base() {
     const int dev = ctx().device;
-    auto it = g_scratch_addr.find(dev);
-    if (it != g_scratch_addr.end()) return it->second;
+    KV_REQUIRE(dev >= 0 && dev < kMaxDevices, KV_EINVAL, "device index out of range");
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    if (g_scratch_addr[dev]) return g_scratch_addr[dev];
     void *p = nullptr;
     KV_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
     KV_REQUIRE(p != nullptr, KV_ECUDA, "cudaGetSymbolAddress returned null for the no-alloc scratch");
     g_scratch_addr[dev] = static_cast<char *>(p);
-    return static_cast<char *>(p);
+    return g_scratch_addr[dev];
 }
 
 // Bump allocator over the static array.
@@ -54,23 +63,33 @@ struct Arena {
     }
 };
 
-// A DevBuf pointing into the arena; the pointer is cleared before the owner
-// is destroyed so nothing is ever freed.
-void view(DevBuf &d, void *p, size_t n) {
-    d.p = p;
-    d.bytes = n;
-}
-void unview(DevBuf &d) {
-    d.p = nullptr;
-    d.bytes = 0;
-}
+// DevBufs pointing into the arena.  Every view is cleared when the set goes
+// out of scope -- on return and when an exception leaves the scope -- so a
+// plan's destructor never hands an arena address to cudaFreeAsync.
+struct Views {
+    std::vector<DevBuf *> held;
+    Views() = default;
+    Views(const Views &) = delete;
+    Views &operator=(const Views &) = delete;
+    void view(DevBuf &d, void *p, size_t n) {
+        held.push_back(&d);
+        d.p = p;
+        d.bytes = n;
+    }
+    ~Views() {
+        for (DevBuf *d : held) {
+            d->p = nullptr;
+            d->bytes = 0;
+        }
+    }
+};
 
 template <class T>
-void put(Arena &ar, DevBuf &d, const std::vector<T> &v) {
+void put(Arena &ar, Views &vw, DevBuf &d, const std::vector<T> &v) {
     const size_t n = std::max<size_t>(1, v.size()) * sizeof(T);
     void *p = ar.take(n);
+    vw.view(d, p, n);
     if (!v.empty()) upload_bytes(p, v.data(), v.size() * sizeof(T));
-    view(d, p, n);
 }
 
 // product<> of two arena-resident operands into an arena-resident output
@@ -82,11 +101,10 @@ void arena_product(Arena &ar, const Meta &A, const double2 *a, const Meta &B, co
     std::vector<int64_t> offs;
     for (auto &blk : out.blocks) offs.push_back(blk.off);
     build_tiles(P, offs, kTileM(KV_FP64), kTileN(KV_FP64));
-    put(ar, P.gemm.d_tiles, P.gemm.tiles);
-    put(ar, P.gemm.d_segs, P.gemm.segs);
+    Views vw;
+    put(ar, vw, P.gemm.d_tiles, P.gemm.tiles);
+    put(ar, vw, P.gemm.d_segs, P.gemm.segs);
     launch_gemm_fp64(P.gemm, a, b, c, 1.0, nullptr);
-    unview(P.gemm.d_tiles);
-    unview(P.gemm.d_segs);
 }
 
 }  // namespace
@@ -115,13 +133,13 @@ cplx expectation_noalloc(const std::vector<DTensor *> &bra, const std::vector<DT
         arena_product(ar, env, env_d, ket[i]->meta, ket[i]->data(), 1, KV_OP_N, KV_OP_N, t1, t1_d);
         MixPlanFull M = plan_mix(t1, w[i]->meta, 1);
         double2 *t2_d = static_cast<double2 *>(ar.take(std::max<int64_t>(1, M.out.nelem) * sizeof(double2)));
-        put(ar, M.mix.d_terms, M.mix.terms);
-        put(ar, M.mix.d_jobs, M.mix.jobs);
-        put(ar, M.mix.d_items, M.mix.items);
-        launch_mix(M.mix, t1_d, w[i]->data(), t2_d, nullptr);
-        unview(M.mix.d_terms);
-        unview(M.mix.d_jobs);
-        unview(M.mix.d_items);
+        {
+            Views vw;
+            put(ar, vw, M.mix.d_terms, M.mix.terms);
+            put(ar, vw, M.mix.d_jobs, M.mix.jobs);
+            put(ar, vw, M.mix.d_items, M.mix.items);
+            launch_mix(M.mix, t1_d, w[i]->data(), t2_d, nullptr);
+        }
         Meta next;
         double2 *next_d;
         arena_product(ar, bra[i]->meta, bra[i]->data(), M.out, t2_d, 2, KV_OP_C, KV_OP_N, next, next_d);

@@ -263,6 +263,333 @@ __global__ void __launch_bounds__(NT) k_svd_jacobi_w(const SvdSector *__restrict
     if (threadIdx.x == 0) status[blockIdx.x] = converged ? sweep : -sweep;
 }
 
+// QR-preconditioned one-sided Jacobi (mixed mode).  One CTA per charge
+// sector; the sector is held in shared memory in FP32 as p rows of length q
+// (row stride q + 1, so column reads by consecutive rows fall in distinct
+// banks), scaled by a power of two so that its largest element lies in
+// [0.5, 1).  The wanted singular vectors are T's left ones (its column space).
+//
+//  1. Pivoted Householder from the right on T's rows: at step k the row with
+//     the largest trailing norm (positions k..q-1) is the pivot; the unitary
+//     reflector H_k with x H_k = (beta, 0, ..., 0) for that row's trailing part
+//     x is applied to every row not yet pivoted.  After r steps
+//     T H_1 ... H_r = [M | E]: M = T Q (p x r, Q the first r columns of the
+//     product) and E has rows of norm below qr_floor * ||T||_F, where the loop
+//     stops.  T = M Q^H + E Q'^H, so T's left singular vectors above the FP32
+//     noise level are M's.  One barrier per step: every warp finds the next
+//     pivot itself from the per-warp maxima of the previous step (double
+//     buffered), and each row's exact trailing norm is accumulated while the
+//     row is updated.
+//  2. One-sided Jacobi on M's r columns (round-robin pairs, 16 lanes a pair,
+//     tolerance `tol` on the cosine); M is row-pivoted triangular, so it
+//     converges in fewer sweeps than T, and only r columns are rotated.
+//  3. Columns sorted by norm: S = norms (descending), Us = normalised columns
+//     (column-major p x r at the sector's t_off), S = 0 in the sector's
+//     remaining slots up to q.
+// status[sector] = Jacobi sweeps used (negative: no convergence), ranks[sector] = r.
+template <int EPL>
+__global__ void __launch_bounds__(1024, 1) k_svd_qrj(const SvdSector *__restrict__ secs,
+                                                     const double2 *__restrict__ T64, float2 *__restrict__ Us,
+                                                     double *__restrict__ S, int *status, int *ranks, int max_sweeps,
+                                                     float tol, float qr_floor) {
+    constexpr int NT = 1024, NW = NT / 32;
+    constexpr int GQ = 8;                      // lanes per row in the QR phase
+    constexpr int GJ = 16;                     // lanes per column pair in the Jacobi phase
+    extern __shared__ float2 sw[];
+    __shared__ float wbest[2][NW];
+    __shared__ int wbesti[2][NW];
+    __shared__ float red[NW];
+    __shared__ double dred[NW];
+    __shared__ int rotated;
+    const SvdSector s = secs[blockIdx.x];
+    const int p = s.p, q = s.q, ldw = q + 1, kmax = min(p, q);
+    float2 *alph = sw + (int64_t)p * ldw;       // [kmax] reflector values conj(alpha_k)
+    float *rn = reinterpret_cast<float *>(alph + kmax);  // [p] trailing row norms^2
+    float *cn = rn + p;                         // [kmax] column norms^2 (Jacobi), then norms
+    int *piv = reinterpret_cast<int *>(cn + kmax);       // [kmax] pivot rows
+    int *done = piv + kmax;                     // [p] row already pivoted
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+    // ---- load (FP64 column-major p x q -> FP32 rows) scaled by a power of two
+    // that brings the largest element to [0.5, 1): sectors whose entries are
+    // far below 1 would otherwise underflow FP32 in the squared norms
+    const double2 *src = T64 + s.t_off;
+    double amax = 0.0;  // largest |re|, |im|; +inf if any element is Inf or NaN
+    for (int64_t e = tid; e < (int64_t)p * q; e += NT) {
+        const double2 v = src[e];
+        const double m = fmax(fabs(v.x), fabs(v.y));
+        amax = (isfinite(v.x) && isfinite(v.y)) ? fmax(amax, m) : INFINITY;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xFFFFFFFFu, amax, o));
+    if (lane == 0) dred[warp] = amax;
+    __syncthreads();
+    amax = 0.0;
+    for (int w = 0; w < NW; ++w) amax = fmax(amax, dred[w]);
+    if (!isfinite(amax)) {  // a non-finite sector: its singular values are NaN (reported by the host)
+        for (int j = tid; j < q; j += NT) S[s.s_off + j] = nan("");
+        if (tid == 0) {
+            status[blockIdx.x] = 0;
+            ranks[blockIdx.x] = 0;
+        }
+        return;
+    }
+    int ex = 0;
+    if (amax > 0.0 && isfinite(amax)) frexp(amax, &ex);
+    const double down = ldexp(1.0, -ex), up = ldexp(1.0, ex);  // exact powers of two
+    for (int64_t e = tid; e < (int64_t)p * q; e += NT) {
+        const int i = (int)(e % p), c = (int)(e / p);
+        const double2 v = src[e];
+        sw[(int64_t)i * ldw + c] = make_float2((float)(v.x * down), (float)(v.y * down));
+    }
+    __syncthreads();
+    const int gq = tid / GQ, gql = tid % GQ, ngq = NT / GQ;
+    const unsigned qmask = 0xFFu << (lane & ~(GQ - 1));
+    float bv = -1.f;
+    int bi = 0x7FFFFFFF;
+    float fro = 0.f;
+    for (int i0 = 0; i0 < p; i0 += ngq) {
+        const int i = i0 + gq;
+        float a = 0.f;
+        if (i < p)
+            for (int c = gql; c < q; c += GQ) {
+                const float2 w = sw[(int64_t)i * ldw + c];
+                a += w.x * w.x + w.y * w.y;
+            }
+#pragma unroll
+        for (int o = GQ / 2; o > 0; o >>= 1) a += __shfl_xor_sync(qmask, a, o, GQ);
+        if (i < p) {
+            if (gql == 0) { rn[i] = a; done[i] = 0; fro += a; }
+            if (a > bv || (a == bv && i < bi)) { bv = a; bi = i; }
+        }
+    }
+    // per-warp maximum (value, lowest index) and the Frobenius norm
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float ov = __shfl_xor_sync(0xFFFFFFFFu, bv, o);
+        const int oi = __shfl_xor_sync(0xFFFFFFFFu, bi, o);
+        if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+        fro += __shfl_xor_sync(0xFFFFFFFFu, fro, o);
+    }
+    if (lane == 0) { wbest[0][warp] = bv; wbesti[0][warp] = bi; red[warp] = fro; }
+    __syncthreads();
+    float fro2 = 0.f;
+    for (int w = 0; w < NW; ++w) fro2 += red[w];
+    const float thr2 = qr_floor * qr_floor * fro2;
+
+    // ---- pivoted Householder on the rows
+    int r = 0;
+    for (int k = 0; k < kmax; ++k) {
+        const int cur = k & 1;
+        float mv = wbest[cur][lane];
+        int mi = wbesti[cur][lane];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float ov = __shfl_xor_sync(0xFFFFFFFFu, mv, o);
+            const int oi = __shfl_xor_sync(0xFFFFFFFFu, mi, o);
+            if (ov > mv || (ov == mv && oi < mi)) { mv = ov; mi = oi; }
+        }
+        if (!(mv > thr2) || mi >= p) break;  // uniform: every warp computed the same maximum
+        r = k + 1;
+        const int ip = mi;
+        const float2 *xr = sw + (int64_t)ip * ldw;
+        // u = conj(x), alpha = -e^{i phi} |u| (phi = arg u_0), v = u - alpha e_0,
+        // beta = 2 / |v|^2 = 1 / (|u| (|u| + |u_0|));  x H = conj(alpha) e_0^T
+        const float nu = sqrtf(mv);
+        const float2 x0 = xr[k];
+        const float a0 = sqrtf(x0.x * x0.x + x0.y * x0.y);
+        const float ph_r = a0 > 0.f ? x0.x / a0 : 1.f, ph_i = a0 > 0.f ? -x0.y / a0 : 0.f;  // e^{i phi}
+        const float2 v0 = make_float2(ph_r * (a0 + nu), ph_i * (a0 + nu));              // u_0 - alpha
+        const float beta = 1.f / (nu * (nu + a0));
+        if (tid == 0) {
+            alph[k] = make_float2(-ph_r * nu, ph_i * nu);  // conj(alpha)
+            piv[k] = ip;
+            done[ip] = 1;
+        }
+        float gbv = -1.f;
+        int gbi = 0x7FFFFFFF;
+        for (int i0 = 0; i0 < p; i0 += ngq) {
+            const int i = i0 + gq;
+            const bool live = i < p && i != ip && !done[i];
+            // group-uniform: every lane of the group has the same i
+            if (live) {
+                float2 *wr = sw + (int64_t)i * ldw;
+                float sr = 0.f, si = 0.f;  // s = sum_c w_c v_c, v_c = conj(x_c) (c > k)
+                for (int c = k + gql; c < q; c += GQ) {
+                    const float2 w = wr[c];
+                    const float2 vc = c == k ? v0 : make_float2(xr[c].x, -xr[c].y);
+                    sr += w.x * vc.x - w.y * vc.y;
+                    si += w.x * vc.y + w.y * vc.x;
+                }
+#pragma unroll
+                for (int o = GQ / 2; o > 0; o >>= 1) {
+                    sr += __shfl_xor_sync(qmask, sr, o, GQ);
+                    si += __shfl_xor_sync(qmask, si, o, GQ);
+                }
+                const float fr = beta * sr, fi = beta * si;
+                float tn = 0.f;
+                for (int c = k + gql; c < q; c += GQ) {
+                    float2 w = wr[c];
+                    const float2 cv = c == k ? make_float2(v0.x, -v0.y) : xr[c];  // conj(v_c)
+                    w.x -= fr * cv.x - fi * cv.y;
+                    w.y -= fr * cv.y + fi * cv.x;
+                    wr[c] = w;
+                    if (c > k) tn += w.x * w.x + w.y * w.y;
+                }
+#pragma unroll
+                for (int o = GQ / 2; o > 0; o >>= 1) tn += __shfl_xor_sync(qmask, tn, o, GQ);
+                if (gql == 0) rn[i] = tn;
+                if (tn > gbv || (tn == gbv && i < gbi)) { gbv = tn; gbi = i; }
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float ov = __shfl_xor_sync(0xFFFFFFFFu, gbv, o);
+            const int oi = __shfl_xor_sync(0xFFFFFFFFu, gbi, o);
+            if (ov > gbv || (ov == gbv && oi < gbi)) { gbv = ov; gbi = oi; }
+        }
+        if (lane == 0) { wbest[cur ^ 1][warp] = gbv; wbesti[cur ^ 1][warp] = gbi; }
+        __syncthreads();
+    }
+    // pivot rows: conj(alpha_k) at position k, zeros after it (within the r columns kept)
+    for (int e = tid; e < r * r; e += NT) {
+        const int kk = e / r, c = e % r;
+        if (c >= kk) sw[(int64_t)piv[kk] * ldw + c] = c == kk ? alph[kk] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+
+    // ---- one-sided Jacobi on the r columns of M
+    const int gj = tid / GJ, gjl = tid % GJ, ngj = NT / GJ;
+    const unsigned jmask = 0xFFFFu << (lane & ~(GJ - 1));
+    const float zt = 1e-14f * fro2;  // (1e-7 ||T||_F)^2: numerically zero columns
+    const int qe = r + (r & 1), m1 = qe - 1;
+    int sweep = 0;
+    bool converged = r < 2;
+    for (; sweep < max_sweeps && !converged; ++sweep) {
+        for (int j = warp; j < r; j += NW) {
+            float a = 0.f;
+            for (int i = lane; i < p; i += 32) {
+                const float2 x = sw[(int64_t)i * ldw + j];
+                a += x.x * x.x + x.y * x.y;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xFFFFFFFFu, a, o);
+            if (lane == 0) cn[j] = a;
+        }
+        if (tid == 0) rotated = 0;
+        __syncthreads();
+        for (int rr = 0; rr < m1; ++rr) {
+            for (int pi = gj; pi < qe / 2; pi += ngj) {
+                int c0 = 0, c1;
+                if (pi > 0) { c0 = pi - 1 + rr; if (c0 >= m1) c0 -= m1; ++c0; }
+                c1 = qe - 2 - pi + rr; if (c1 >= m1) c1 -= m1; ++c1;
+                if (c0 > c1) { const int x = c0; c0 = c1; c1 = x; }
+                if (c1 >= r) continue;
+                const float a = cn[c0], b = cn[c1];
+                if (!(a > zt) || !(b > zt)) continue;
+                float cr = 0.f, ci = 0.f;
+                float2 xv[EPL > 0 ? EPL : 1], yv[EPL > 0 ? EPL : 1];
+                if constexpr (EPL > 0) {
+                    float2 a1 = make_float2(0.f, 0.f), a2 = make_float2(0.f, 0.f);
+#pragma unroll
+                    for (int kk = 0; kk < EPL; ++kk) {
+                        const int i = gjl + kk * GJ;
+                        xv[kk] = i < p ? sw[(int64_t)i * ldw + c0] : make_float2(0.f, 0.f);
+                        yv[kk] = i < p ? sw[(int64_t)i * ldw + c1] : make_float2(0.f, 0.f);
+                        a1 = __ffma2_rn(xv[kk], yv[kk], a1);
+                        a2 = __ffma2_rn(xv[kk], make_float2(yv[kk].y, yv[kk].x), a2);
+                    }
+                    cr = a1.x + a1.y;
+                    ci = a2.x - a2.y;
+                } else {
+                    for (int i = gjl; i < p; i += GJ) {
+                        const float2 xi = sw[(int64_t)i * ldw + c0], yi = sw[(int64_t)i * ldw + c1];
+                        cr += xi.x * yi.x + xi.y * yi.y;
+                        ci += xi.x * yi.y - xi.y * yi.x;
+                    }
+                }
+#pragma unroll
+                for (int o = GJ / 2; o > 0; o >>= 1) {
+                    cr += __shfl_xor_sync(jmask, cr, o, GJ);
+                    ci += __shfl_xor_sync(jmask, ci, o, GJ);
+                }
+                const float ac = sqrtf(cr * cr + ci * ci);
+                if (!(ac > tol * sqrtf(a * b))) continue;
+                const float z = (b - a) / (2.f * ac);
+                const float tn = copysignf(1.f, z) / (fabsf(z) + sqrtf(1.f + z * z));
+                kvj::Rot<float> rot;
+                rot.cs = 1.f / sqrtf(1.f + tn * tn);
+                const float sn = tn * rot.cs;
+                rot.s_re = sn * cr / ac;
+                rot.s_im = sn * ci / ac;
+                if (gjl == 0) {
+                    rotated = 1;
+                    cn[c0] = a - tn * ac;
+                    cn[c1] = b + tn * ac;
+                }
+                if constexpr (EPL > 0) {
+                    const float2 cs2 = make_float2(rot.cs, rot.cs), sr2 = make_float2(rot.s_re, rot.s_re);
+                    const float2 msr2 = make_float2(-rot.s_re, -rot.s_re), pm = make_float2(-rot.s_im, rot.s_im);
+#pragma unroll
+                    for (int kk = 0; kk < EPL; ++kk) {
+                        const int i = gjl + kk * GJ;
+                        const float2 xo = xv[kk], yo = yv[kk];
+                        float2 nx = __fmul2_rn(cs2, xo);
+                        nx = __ffma2_rn(msr2, yo, nx);
+                        nx = __ffma2_rn(pm, make_float2(yo.y, yo.x), nx);
+                        float2 ny = __fmul2_rn(cs2, yo);
+                        ny = __ffma2_rn(sr2, xo, ny);
+                        ny = __ffma2_rn(pm, make_float2(xo.y, xo.x), ny);
+                        if (i < p) {
+                            sw[(int64_t)i * ldw + c0] = nx;
+                            sw[(int64_t)i * ldw + c1] = ny;
+                        }
+                    }
+                } else {
+                    for (int i = gjl; i < p; i += GJ) {
+                        float2 xi = sw[(int64_t)i * ldw + c0], yi = sw[(int64_t)i * ldw + c1];
+                        kvj::rotate_pair(rot, xi.x, xi.y, yi.x, yi.y);
+                        sw[(int64_t)i * ldw + c0] = xi;
+                        sw[(int64_t)i * ldw + c1] = yi;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        converged = (rotated == 0);
+        __syncthreads();
+    }
+
+    // ---- sorted singular values and normalised columns
+    for (int j = warp; j < r; j += NW) {
+        float a = 0.f;
+        for (int i = lane; i < p; i += 32) {
+            const float2 x = sw[(int64_t)i * ldw + j];
+            a += x.x * x.x + x.y * x.y;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xFFFFFFFFu, a, o);
+        if (lane == 0) cn[j] = sqrtf(a);
+    }
+    __syncthreads();
+    for (int j = warp; j < r; j += NW) {
+        const float sj = cn[j];
+        int rank = 0;
+        for (int i = 0; i < r; ++i) rank += (cn[i] > sj) || (cn[i] == sj && i < j);
+        const float inv = sj > 0.f ? 1.f / sj : 0.f;
+        for (int i = lane; i < p; i += 32) {
+            const float2 x = sw[(int64_t)i * ldw + j];
+            Us[s.t_off + (int64_t)rank * p + i] = make_float2(x.x * inv, x.y * inv);
+        }
+        if (lane == 0) S[s.s_off + rank] = (double)sj * up;
+    }
+    for (int j = r + tid; j < q; j += NT) S[s.s_off + j] = 0.0;  // every one of the sector's q slots
+    if (tid == 0) {
+        status[blockIdx.x] = converged ? sweep : -sweep;
+        ranks[blockIdx.x] = r;
+    }
+}
+
 // singular values (as double), descending order, normalised U columns
 template <class R>
 __global__ void __launch_bounds__(256) k_svd_finalize(const SvdSector *__restrict__ secs,
@@ -460,6 +787,60 @@ __global__ void __launch_bounds__(256) k_svd_scatter(const SvdScatter *__restric
     }
 }
 
+constexpr int kMaxDevices = 64;
+std::mutex g_attr_mu;
+int g_jacobi_smem[kMaxDevices];
+bool g_jacobi_set[kMaxDevices], g_trsm_set[kMaxDevices];
+
+// per device: raise the Jacobi kernels' dynamic shared-memory limit once and
+// return it (function attributes belong to the device they were set on)
+int jacobi_smem_limit(int dev) {
+    KV_REQUIRE(dev >= 0 && dev < kMaxDevices, KV_EINVAL, "device index out of range");
+    std::lock_guard<std::mutex> lk(g_attr_mu);
+    if (!g_jacobi_set[dev]) {
+        int optin = 0;
+        KV_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        const int bytes = std::max(0, optin - 4096 - (int)sizeof(float) * kJacobiMaxQ);
+        KV_CUDA(cudaFuncSetAttribute(k_svd_jacobi_w<1024, 16, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        KV_CUDA(cudaFuncSetAttribute(k_svd_jacobi_w<1024, 16, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        KV_CUDA(cudaFuncSetAttribute(k_svd_jacobi_w<1024, 16, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        KV_CUDA(cudaFuncSetAttribute(k_svd_jacobi_w<1024, 16, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        g_jacobi_smem[dev] = bytes;
+        g_jacobi_set[dev] = true;
+    }
+    return g_jacobi_smem[dev];
+}
+
+bool g_qrj_set[kMaxDevices];
+int g_qrj_smem[kMaxDevices];
+
+// per device: the QR-Jacobi kernels may use the whole opt-in shared memory
+int qrj_smem_limit(int dev) {
+    KV_REQUIRE(dev >= 0 && dev < kMaxDevices, KV_EINVAL, "device index out of range");
+    std::lock_guard<std::mutex> lk(g_attr_mu);
+    if (!g_qrj_set[dev]) {
+        int optin = 0;
+        KV_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        const int bytes = std::max(0, optin - 1024);  // less the kernel's static arrays
+        KV_CUDA(cudaFuncSetAttribute(k_svd_qrj<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        KV_CUDA(cudaFuncSetAttribute(k_svd_qrj<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        KV_CUDA(cudaFuncSetAttribute(k_svd_qrj<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        KV_CUDA(cudaFuncSetAttribute(k_svd_qrj<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        g_qrj_smem[dev] = bytes;
+        g_qrj_set[dev] = true;
+    }
+    return g_qrj_smem[dev];
+}
+
+void trsm_smem_raise(int dev, int bytes) {
+    KV_REQUIRE(dev >= 0 && dev < kMaxDevices, KV_EINVAL, "device index out of range");
+    std::lock_guard<std::mutex> lk(g_attr_mu);
+    if (!g_trsm_set[dev]) {
+        KV_CUDA(cudaFuncSetAttribute(k_trsm_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        g_trsm_set[dev] = true;
+    }
+}
+
 }  // namespace
 
 void svd_gather(const SvdPlan &p, const double2 *A, double2 *T) {
@@ -500,20 +881,9 @@ void svd_scatter(const std::vector<SvdScatter> &sc, const SvdPlan &p, const doub
 
 void svd_jacobi_f32(const SvdPlan &p, const double2 *T64, float2 *T, int *status, int max_sweeps, float tol) {
     if (p.secs.empty()) return;
-    // dynamic shared memory: opt-in maximum less the static arrays and 4 KB
-    // (set once; kv_sweep_batched runs this from several threads)
-    static int smem_bytes = 0;
-    static std::once_flag once;
-    std::call_once(once, [] {
-        int optin = 0;
-        KV_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx().device));
-        const int bytes = std::max(0, optin - 4096 - (int)sizeof(float) * kJacobiMaxQ);
-        KV_CUDA(cudaFuncSetAttribute(k_svd_jacobi_w<1024, 16, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-        KV_CUDA(cudaFuncSetAttribute(k_svd_jacobi_w<1024, 16, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-        KV_CUDA(cudaFuncSetAttribute(k_svd_jacobi_w<1024, 16, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-        KV_CUDA(cudaFuncSetAttribute(k_svd_jacobi_w<1024, 16, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-        smem_bytes = bytes;
-    });
+    // dynamic shared memory: opt-in maximum less the static arrays and 4 KB,
+    // raised once per device (kv_sweep_batched runs this from several threads)
+    const int smem_bytes = jacobi_smem_limit(ctx().device);
     int64_t max_pq = 0;
     int max_p = 0;
     for (auto &s : p.secs) {
@@ -536,6 +906,36 @@ void svd_jacobi_f32(const SvdPlan &p, const double2 *T64, float2 *T, int *status
     else launch(k_svd_jacobi_w<1024, 16, 0>);
     counted();
     KV_CUDA(cudaGetLastError());
+}
+
+// shared-memory bytes of k_svd_qrj for a p x q sector
+static size_t qrj_smem(int p, int q) {
+    const size_t kmax = (size_t)std::min(p, q);
+    return sizeof(float2) * ((size_t)p * (q + 1) + kmax) + sizeof(float) * (2 * (size_t)p + 2 * kmax);
+}
+
+bool svd_qrjacobi_f32(const SvdPlan &p, const double2 *T64, float2 *Us, double *S, int *status, int *ranks,
+                      int max_sweeps, float tol, float qr_floor) {
+    if (p.secs.empty()) return true;
+    const int limit = qrj_smem_limit(ctx().device);
+    size_t smem = 0;
+    int max_p = 0;
+    for (auto &sc : p.secs) {
+        smem = std::max(smem, qrj_smem(sc.p, sc.q));
+        max_p = std::max(max_p, sc.p);
+    }
+    if (smem > (size_t)limit) return false;
+    auto launch = [&](auto kernel) {
+        kernel<<<(unsigned)p.secs.size(), 1024, smem, ctx().stream>>>(p.d_secs.as<SvdSector>(), T64, Us, S, status,
+                                                                      ranks, max_sweeps, tol, qr_floor);
+    };
+    if (max_p <= 32) launch(k_svd_qrj<2>);
+    else if (max_p <= 64) launch(k_svd_qrj<4>);
+    else if (max_p <= 128) launch(k_svd_qrj<8>);
+    else launch(k_svd_qrj<0>);
+    counted();
+    KV_CUDA(cudaGetLastError());
+    return true;
 }
 
 void svd_finalize_f32(const SvdPlan &p, const float2 *T, float2 *Us, double *S) {
@@ -566,10 +966,7 @@ void svd_trsm(const DevBuf &pol, const std::vector<int> &item_pol, const std::ve
     const size_t smem = (size_t)kTrsmRows * std::max(1, kmax) * sizeof(double2);
     constexpr int kTrsmSmemMax = 200 * 1024;
     KV_REQUIRE(smem <= kTrsmSmemMax, KV_EINVAL, "SVD polish: kept dimension of one sector too large");
-    static std::once_flag once;  // the limit is raised once, to the largest size allowed here
-    std::call_once(once, [] {
-        KV_CUDA(cudaFuncSetAttribute(k_trsm_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrsmSmemMax));
-    });
+    trsm_smem_raise(ctx().device, kTrsmSmemMax);  // once per device, to the largest size allowed here
     DevBuf ip = upload_vec(item_pol), ir = upload_vec(item_row0);
     k_trsm_rows<<<(unsigned)item_pol.size(), 32 * kTrsmRows, smem, ctx().stream>>>(pol.as<SvdPolish>(), ip.as<int>(),
                                                                                   ir.as<int>(), G, X);

@@ -56,6 +56,13 @@ constexpr int kJacobiMaxQ = 2048;
 // normalised columns and singular values, and the first k columns in FP64
 void svd_jacobi_f32(const SvdPlan &p, const double2 *T64, float2 *T, int *status, int max_sweeps, float tol);
 void svd_finalize_f32(const SvdPlan &p, const float2 *T, float2 *Us, double *S);
+// mixed mode, every sector in shared memory: pivoted Householder on T's rows
+// truncated where the remaining rows fall below qr_floor ||T||_F, one-sided
+// Jacobi on the rank-r factor, sorted normalised columns and singular values
+// (zero beyond r; ranks[sector] = r).  Returns false, launching nothing, when
+// a sector does not fit shared memory.
+bool svd_qrjacobi_f32(const SvdPlan &p, const double2 *T64, float2 *Us, double *S, int *status, int *ranks,
+                      int max_sweeps, float tol, float qr_floor);
 void svd_extract(const DevBuf &pol, int npol, const SvdPlan &p, const float2 *Us, const double *S, double2 *W);
 // rows of X per triangular-solve CTA (one warp per row)
 constexpr int kTrsmRows = 8;

@@ -71,7 +71,9 @@ constexpr int KDRAIN = 336;                    // K-steps accumulated exactly be
 constexpr int GKC = KDRAIN / BKC;              // K panels per drain group
 constexpr int FRAC = 29;
 constexpr int kZeroExp = -4000;                // exponent of an all-zero row
-constexpr long long WAIT_LIMIT = 1ll << 22;
+constexpr int kErrTimeout = 1, kErrNonFinite = 2;  // bits of the per-device error word
+constexpr int kMaxFiniteExp = 1024;            // row / column exponents of finite operands are <= 1024
+constexpr long long WAIT_LIMIT = 1ll << 22;   // try_wait polls before a wait gives up
 constexpr int EPI_WARPS = 8;                   // two per tensor-memory lane quarter, 16 columns each
 constexpr int EPI_COLS = BN / (EPI_WARPS / 4);
 constexpr int NTHREADS = 32 * (2 + EPI_WARPS);
@@ -120,10 +122,13 @@ __device__ __forceinline__ __half2 digits2(int d0, int d1) {
 
 // One CTA per (job, 8 consecutive rows); one warp per row: pass 1 finds the
 // row exponent, pass 2 writes the digits of two adjacent K positions per lane.
+// A row holding an Inf or NaN sets bit kErrNonFinite of *err: fixed point has
+// no code for it, and the digits written for that row are meaningless.
 template <int TR>
 __global__ void __launch_bounds__(256) k_slice(const SliceJob *__restrict__ jobs, const int2 *__restrict__ items,
                                                const double2 *__restrict__ src, __half *__restrict__ dst,
-                                               int *__restrict__ exps, double alpha, const int *skip, int step) {
+                                               int *__restrict__ exps, double alpha, const int *skip, int step,
+                                               int *err) {
     if (skip && *skip) return;
     const int2 it = items[blockIdx.x];
     const SliceJob j = jobs[it.x];
@@ -152,7 +157,10 @@ __global__ void __launch_bounds__(256) k_slice(const SliceJob *__restrict__ jobs
 #pragma unroll
     for (int o = 16; o; o >>= 1) mx = max(mx, (unsigned long long)__shfl_xor_sync(0xFFFFFFFFu, mx, o));
     const int e = mx ? (int)(mx >> 52) - 1022 : kZeroExp;
-    if (lane == 0) exps[j.exp_off + r] = e;
+    if (lane == 0) {
+        exps[j.exp_off + r] = e;
+        if (mx >= 0x7FF0000000000000ull) atomicOr(err, kErrNonFinite);
+    }
     __half *pan = dst + j.dst_off + (int64_t)(r / TR) * j.nkc * (NPL * TR * BKC);
     const int rr = r % TR;
     for (int k = 2 * lane; k < kpad; k += 64) {  // k even: k and k + 1 are adjacent in the panel
@@ -225,8 +233,8 @@ __device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
 }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
-    for (long long i = 0; i < WAIT_LIMIT; ++i) {
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, long long limit = WAIT_LIMIT) {
+    for (long long i = 0; i < limit; ++i) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
@@ -308,7 +316,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_gemm_tc(const GemmTile *__restr
                                                     const __half *__restrict__ Apl, const __half *__restrict__ Bpl,
                                                     const int *__restrict__ Aexp, const int *__restrict__ Bexp,
                                                     double2 *__restrict__ C, const int *skip, int *err, int step,
-                                                    int write_inactive) {
+                                                    int write_inactive, long long wait_limit, int no_copies) {
     if (skip && *skip) return;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -356,10 +364,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_gemm_tc(const GemmTile *__restr
                     if (g.entry > step) continue;
                     const __half *ap = Apl + g.a_pan + (int64_t)rt * g.nkc * A_PANEL;
                     const __half *bp = Bpl + g.b_pan + (int64_t)nt * g.nkc * B_PANEL;
-                    for (int kc = 0; kc < g.nkc; ++kc, ++it) {
+                    for (int kc = 0; kc < g.nkc && !no_copies; ++kc, ++it) {
                         const int st = it % STAGES;
                         const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
-                        if (!mbar_wait(smem_u32(empty + st), ph ^ 1u)) { ok = false; break; }
+                        if (!mbar_wait(smem_u32(empty + st), ph ^ 1u, wait_limit)) { ok = false; break; }
                         mbar_expect_tx(smem_u32(full + st), (uint32_t)(A_BYTES + B_BYTES));
                         bulk_g2s(smem_u32(sA + st * A_BYTES), ap + (int64_t)kc * A_PANEL, A_BYTES,
                                  smem_u32(full + st));
@@ -369,10 +377,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_gemm_tc(const GemmTile *__restr
                     }
                 }
             }
-            if (!ok) atomicExch(err, 1);
+            if (!ok) atomicOr(err, kErrTimeout);
             // no copy may land after the CTA exits: wait (bounded) for the last one into each stage
             for (int st = 0; st < STAGES; ++st)
-                if (uses[st]) mbar_wait(smem_u32(full + st), (uint32_t)(uses[st] - 1) & 1u);
+                if (uses[st]) mbar_wait(smem_u32(full + st), (uint32_t)(uses[st] - 1) & 1u, wait_limit);
         }
     } else if (warp == 1) {
         // ------------------------------------------------ MMA issue
@@ -386,13 +394,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_gemm_tc(const GemmTile *__restr
                     const int nkc = segs[s].nkc;
                     for (int kc0 = 0; kc0 < nkc && ok; kc0 += GKC, ++grp) {
                         // the epilogue has read the previous group's accumulators
-                        if (!mbar_wait(smem_u32(acce), ((uint32_t)grp & 1u) ^ 1u)) { ok = false; break; }
+                        if (!mbar_wait(smem_u32(acce), ((uint32_t)grp & 1u) ^ 1u, wait_limit)) { ok = false; break; }
                         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                         const int kc1 = min(nkc, kc0 + GKC);
                         for (int kc = kc0; kc < kc1; ++kc, ++it) {
                             const int st = it % STAGES;
                             const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
-                            if (!mbar_wait(smem_u32(full + st), ph)) { ok = false; break; }
+                            if (!mbar_wait(smem_u32(full + st), ph, wait_limit)) { ok = false; break; }
                             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                             const uint32_t a0 = smem_u32(sA + st * A_BYTES), b0 = smem_u32(sB + st * B_BYTES);
 #pragma unroll
@@ -417,10 +425,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_gemm_tc(const GemmTile *__restr
                     }
                 }
             }
-            if (!ok) atomicExch(err, 1);
+            if (!ok) atomicOr(err, kErrTimeout);
             // every MMA issued by this thread has completed before tensor memory is freed
             mma_commit(smem_u32(mdone));
-            mbar_wait(smem_u32(mdone), 0u);
+            mbar_wait(smem_u32(mdone), 0u, wait_limit);
         }
     } else {
         // ------------------------------------------------ drains and epilogue
@@ -460,7 +468,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_gemm_tc(const GemmTile *__restr
                 const int shr = erow - Aexp[g.a_exp + t.m0 + m];
                 for (int kc0 = 0; kc0 < g.nkc; kc0 += GKC, ++grp) {
                     // warp-uniform decision: tcgen05.ld below is a warp-wide instruction
-                    if (ok && !__all_sync(0xFFFFFFFFu, mbar_wait(smem_u32(accf), (uint32_t)grp & 1u))) ok = false;
+                    if (ok && !__all_sync(0xFFFFFFFFu, mbar_wait(smem_u32(accf), (uint32_t)grp & 1u, wait_limit)))
+                        ok = false;
                     if (!ok) continue;
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
@@ -501,14 +510,20 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_gemm_tc(const GemmTile *__restr
                 for (int c = 0; c < EPI_COLS; ++c) {
                     const int gn = t.n0 + c_lo + c;
                     if (gn < t.N) {
-                        const int sc = erow + s_ecol[c_lo + c] - 2 * FRAC + 16;
-                        crow[gn] = make_double2(i64_ldexp(cr[c], sc), i64_ldexp(ci[c], sc));
+                        const int ec = s_ecol[c_lo + c];
+                        const int sc = erow + ec - 2 * FRAC + 16;
+                        // a row or column holding Inf or NaN (slicer exponent above the
+                        // FP64 range) gives NaN, as the FP64 product would
+                        crow[gn] = (erow > kMaxFiniteExp || ec > kMaxFiniteExp)
+                                       ? make_double2(__longlong_as_double(0x7FF8000000000000ll),
+                                                      __longlong_as_double(0x7FF8000000000000ll))
+                                       : make_double2(i64_ldexp(cr[c], sc), i64_ldexp(ci[c], sc));
                     }
                 }
             }
             epi_bar();  // every warp has used s_ecol before the next tile rewrites it
         }
-        if (!ok && lane == 0) atomicExch(err, 1);
+        if (!ok && lane == 0) atomicOr(err, kErrTimeout);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -519,8 +534,26 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_gemm_tc(const GemmTile *__restr
     }
 }
 
-int *g_err = nullptr;
-std::once_flag g_attr;
+// Per device: the kernel's shared-memory limit is raised and its error word
+// (kErrTimeout | kErrNonFinite bits, cleared when read) allocated once.
+constexpr int kMaxDevices = 64;
+std::mutex g_dev_mu;
+int *g_err[kMaxDevices] = {};
+// test hook (kv_debug_gemm_stall): copies withheld and a short wait limit
+int g_stall_test = 0;
+
+int *device_err_word(int dev) {
+    KV_REQUIRE(dev >= 0 && dev < kMaxDevices, KV_EINVAL, "device index out of range");
+    std::lock_guard<std::mutex> lk(g_dev_mu);
+    if (!g_err[dev]) {
+        KV_CUDA(cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+        int *e = nullptr;
+        KV_CUDA(cudaMalloc(&e, sizeof(int)));
+        KV_CUDA(cudaMemset(e, 0, sizeof(int)));
+        g_err[dev] = e;
+    }
+    return g_err[dev];
+}
 
 }  // namespace
 
@@ -609,25 +642,19 @@ void launch_gemm_mixed(const GemmPlan &p, const double2 *A, const double2 *B, do
     KV_REQUIRE(p.tile_m == BM && p.tile_n == BN && p.xsegs.size() == p.segs.size(), KV_EINVAL,
                "internal: GEMM plan not prepared for the tensor-core path");
     auto &c = ctx();
-    std::call_once(g_attr, [] {  // once, also when several threads launch
-        KV_CUDA(cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-        int *e = nullptr;
-        KV_CUDA(cudaMalloc(&e, sizeof(int)));
-        KV_CUDA(cudaMemset(e, 0, sizeof(int)));
-        g_err = e;
-    });
+    int *err = device_err_word(c.device);
     DevBuf ap(std::max<int64_t>(1, p.a_planes) * sizeof(__half)), bp(std::max<int64_t>(1, p.b_planes) * sizeof(__half));
     DevBuf ae(std::max<int64_t>(1, p.a_exps) * sizeof(int)), be(std::max<int64_t>(1, p.b_exps) * sizeof(int));
     int n = 0;
     if (!p.aitems.empty()) {
         k_slice<BM><<<(unsigned)p.aitems.size(), 256, 0, c.stream>>>(p.d_ajobs.as<SliceJob>(), p.d_aitems.as<int2>(),
-                                                                     A, ap.as<__half>(), ae.as<int>(), 1.0, skip, step);
+                                                                     A, ap.as<__half>(), ae.as<int>(), 1.0, skip, step, err);
         KV_CUDA(cudaGetLastError());
         ++n;
     }
     if (!p.bitems.empty()) {
         k_slice<BN><<<(unsigned)p.bitems.size(), 256, 0, c.stream>>>(p.d_bjobs.as<SliceJob>(), p.d_bitems.as<int2>(),
-                                                                     B, bp.as<__half>(), be.as<int>(), alpha, skip, step);
+                                                                     B, bp.as<__half>(), be.as<int>(), alpha, skip, step, err);
         KV_CUDA(cudaGetLastError());
         ++n;
     }
@@ -635,19 +662,29 @@ void launch_gemm_mixed(const GemmPlan &p, const double2 *A, const double2 *B, do
     const int ntiles = (int)p.tiles.size();
     k_gemm_tc<<<(unsigned)std::min(ntiles, c.num_sms), NTHREADS, SMEM_BYTES, c.stream>>>(
         p.d_tiles.as<GemmTile>(), ntiles, p.d_xsegs.as<SegX>(), ap.as<__half>(), bp.as<__half>(), ae.as<int>(),
-        be.as<int>(), C, skip, g_err, step, p.write_inactive ? 1 : 0);
+        be.as<int>(), C, skip, err, step, p.write_inactive ? 1 : 0, g_stall_test ? (1ll << 10) : WAIT_LIMIT,
+        g_stall_test);
     KV_CUDA(cudaGetLastError());
     counted(n + 1);
     // the slices are freed stream-ordered after the GEMM
 }
 
-// 0 if no tensor-core wait has timed out since the last call (then cleared)
+// KV_ETIMEOUT if a tensor-core wait gave up, else KV_ENONFINITE if an operand
+// held an Inf or NaN, since the last call on this device (then cleared)
 int mixed_gemm_status() {
-    if (!g_err) return KV_OK;
+    const int dev = ctx().device;
+    int *e = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_dev_mu);
+        if (dev >= 0 && dev < kMaxDevices) e = g_err[dev];
+    }
+    if (!e) return KV_OK;
     int h = 0;
-    KV_CUDA(cudaMemcpy(&h, g_err, sizeof(int), cudaMemcpyDeviceToHost));
-    if (h) KV_CUDA(cudaMemset(g_err, 0, sizeof(int)));
-    return h ? KV_ETIMEOUT : KV_OK;
+    KV_CUDA(cudaMemcpy(&h, e, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h) KV_CUDA(cudaMemset(e, 0, sizeof(int)));
+    return (h & kErrTimeout) ? KV_ETIMEOUT : (h & kErrNonFinite) ? KV_ENONFINITE : KV_OK;
 }
+
+void set_gemm_stall_test(int on) { g_stall_test = on ? 1 : 0; }
 
 }  // namespace kv

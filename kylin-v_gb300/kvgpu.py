@@ -17,7 +17,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libkvgpu.so")
 
 KV_FP64 = 0
-KV_MIXED_TF32 = 1
+KV_MIXED_3M_DIGITS = 1  # 3M products of fixed-point FP16 digits on the tensor cores (include/kvgpu.h)
+KV_MIXED_TF32 = KV_MIXED_3M_DIGITS  # other names of the same mode
+KV_MIXED_3M_TF32 = KV_MIXED_3M_DIGITS
+KV_MIXED_3M_BF16X3 = KV_MIXED_3M_DIGITS
 KV_MIXED_GEMM = 2  # tensor-core contractions, FP64 SVD
 KV_MIXED_SVD = 3   # FP64 contractions, mixed SVD
 OP_N, OP_T, OP_C = 111, 112, 113
@@ -29,6 +32,7 @@ EXPORTS = (
     "kv_svd_truncate", "kv_tdvp_create", "kv_tdvp_sweep", "kv_tdvp_site", "kv_tdvp_stats", "kv_tdvp_free",
     "kv_expectation", "kv_profile", "kv_profile_read", "kv_counters", "kv_expectation_noalloc",
     "kv_tdvp_host_stats", "kv_canonicalize", "kv_sweep_batched", "kv_adjoint_heff", "kv_adjoint_env",
+    "kv_debug_gemm_stall", "kv_debug_pool_usage", "kv_svd_stats",
 )
 
 
@@ -82,6 +86,11 @@ def lib():
         L.kv_adjoint_heff.argtypes = [ctypes.c_int, vp, vp, vp, vp, vp, ctypes.c_double, vp, ctypes.c_int,
                                       pvp, pvp, pvp, pvp, pvp]
         L.kv_adjoint_env.argtypes = [ctypes.c_int, vp, vp, vp, vp, ctypes.c_int, pvp, pvp, pvp]
+        L.kv_debug_gemm_stall.argtypes = [ctypes.c_int]
+        ll = ctypes.POINTER(ctypes.c_longlong)
+        L.kv_svd_stats.argtypes = [ctypes.c_int, ll, ll, ll, ll, ip]
+        L.kv_debug_pool_usage.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_longlong),
+                                          ctypes.POINTER(ctypes.c_longlong)]
         _lib = L
     return _lib
 
@@ -265,6 +274,17 @@ def profile_read() -> dict:
     ms, fl, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
     check(lib().kv_profile_read(ctypes.byref(ms), ctypes.byref(fl), ctypes.byref(n)))
     return {"gemm_ms": ms.value, "gemm_ref_flops": fl.value, "gemm_launches": n.value}
+
+
+def svd_stats(reset: bool = True) -> dict:
+    """Charge sectors through the block SVD since the last reset: count,
+    columns, ranks kept by the mixed path's QR reduction, Jacobi sweeps."""
+    v = [ctypes.c_longlong() for _ in range(4)]
+    mx = ctypes.c_int()
+    check(lib().kv_svd_stats(int(reset), *[ctypes.byref(x) for x in v], ctypes.byref(mx)))
+    n = max(1, v[0].value)
+    return {"sectors": v[0].value, "mean_columns": v[1].value / n, "mean_rank": v[2].value / n,
+            "mean_sweeps": v[3].value / n, "max_sweeps": mx.value}
 
 
 def launches() -> int:

@@ -62,6 +62,11 @@ def cases():
         # the 1-site benchmark shape: L=8, 1 mode, cutoff 8, D=32, 20 steps
         "l8c8d32": dict(chain=HolsteinChain(8, [1.0], [[1.0]] * 8, cutoff=8), D=32, seed=1234, ops_sites=[7],
                         traj=[("[0,0,0,20]", 32, 1e-8)], keep_inputs=False),
+        # the two-site benchmark's local structure (2 modes: omega 0.2 / 1.2, g 0.5 / 1.0, cutoff 16,
+        # D = 128, SVD cutoff 1e-8) on 3 molecules (15 sites), 20 two-site steps: the trajectory the
+        # mixed path's population gate is checked against (too slow for the FP64 trajectory tests)
+        "l32m3": dict(chain=HolsteinChain(3, [0.2, 1.2], [[0.5, 1.0]] * 3, cutoff=16), D=128, seed=1234,
+                      ops_sites=[], traj=[("[0,20,0,0]", 128, 1e-8)], keep_inputs=False, mixed_only=True),
     }
 
 
@@ -93,6 +98,9 @@ def add_missing_trajectories():
     with open(os.path.join(HERE, "manifest.json")) as f:
         manifest = json.load(f)
     for name, c in cases().items():
+        if name not in manifest:
+            manifest[name] = generate_case(name, c)
+            continue
         have = {t["stage"] for t in manifest[name]["trajectories"]}
         todo = [t for t in c["traj"] if t[0] not in have]
         if not todo or not c["keep_inputs"]:
@@ -124,52 +132,58 @@ def run(cmd, cwd):
 
 def main():
     _pkg()
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", "-j4"], check=True,
+                   stdout=subprocess.DEVNULL)
+    manifest = {name: generate_case(name, c) for name, c in cases().items()}
+    with open(os.path.join(HERE, "manifest.json"), "w") as f:
+        json.dump(manifest, f, indent=1)
+
+
+def generate_case(name, c):
+    """Inputs, primitive dumps and trajectories of one case; its manifest entry."""
+    _pkg()
     from kylin_v_gb300 import holstein as H
     from kylin_v_gb300 import kvio
 
-    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", "-j4"], check=True,
-                   stdout=subprocess.DEVNULL)
-    manifest = {}
-    for name, c in cases().items():
-        ch = c["chain"]
-        out = os.path.join(HERE, name)
-        os.makedirs(out, exist_ok=True)
-        work = tempfile.mkdtemp(prefix="kvgold_")
-        os.makedirs(os.path.join(work, "State"))
-        os.makedirs(os.path.join(work, "Op"))
-        mps = H.random_mps(ch, c["D"], seed=c["seed"])
-        mpo = H.hamiltonian_mpo(ch)
-        kvio.write_mps(os.path.join(work, "in.mps"), mps)
-        kvio.write_mpo(os.path.join(work, "H.mpo"), mpo)
-        dens = []
-        for j in ch.exciton_sites():
-            p = os.path.join(work, f"D{j}.mpo")
-            kvio.write_mpo(p, H.density_mpo(ch, j))
-            dens.append(p)
-        entry = {"D": c["D"], "seed": c["seed"], "n_sites": ch.n_sites,
-                 "site_norms2": [float(sum(np.vdot(a, a).real for _, a in t.blocks)) for t in mps]}
-        # reference-built Hamiltonian on the same model
-        with open(os.path.join(work, "chain.inp"), "w") as f:
-            f.write(ch.reference_input())
-        run([os.path.join(REF_BIN, "kln-holstein"), "-i", "chain.inp", "-t", "1e-14"], work)
-        e_ref = run([os.path.join(REF_BIN, "kln-join"), "-a", "in.mps", "-b", "in.mps", "-o", "Op/H_tot"], work)
-        e_mine = run([os.path.join(REF_BIN, "kln-join"), "-a", "in.mps", "-b", "in.mps", "-o", "H.mpo"], work)
-        entry["energy_ref_mpo"] = float(e_ref.strip().strip("()").split(",")[0])
-        entry["energy_own_mpo"] = float(e_mine.strip().strip("()").split(",")[0])
-        if c["keep_inputs"]:
-            for f in ("in.mps", "H.mpo"):
-                shutil.copy(os.path.join(work, f), os.path.join(out, f))
-            shutil.copy(os.path.join(work, "Op", "H_tot"), os.path.join(out, "H_ref.mpo"))
-            for site in c["ops_sites"]:
-                od = os.path.join(out, f"ops_site{site}")
-                os.makedirs(od, exist_ok=True)
-                run([os.path.join(REF_BIN, "kv_ref_ops"), "-w", "in.mps", "-o", "H.mpo", "-i", str(site),
-                     "-v", "0.05", "-k", "11", "-e", "1e-8", "-t", "1e-8", "-D", str(c["D"]), "-O", od], work)
-        entry["trajectories"] = [trajectory(ch, work, out, stage, maxd, tol, dens) for stage, maxd, tol in c["traj"]]
-        manifest[name] = entry
-        shutil.rmtree(work)
-    with open(os.path.join(HERE, "manifest.json"), "w") as f:
-        json.dump(manifest, f, indent=1)
+    ch = c["chain"]
+    out = os.path.join(HERE, name)
+    os.makedirs(out, exist_ok=True)
+    work = tempfile.mkdtemp(prefix="kvgold_")
+    os.makedirs(os.path.join(work, "State"))
+    os.makedirs(os.path.join(work, "Op"))
+    mps = H.random_mps(ch, c["D"], seed=c["seed"])
+    mpo = H.hamiltonian_mpo(ch)
+    kvio.write_mps(os.path.join(work, "in.mps"), mps)
+    kvio.write_mpo(os.path.join(work, "H.mpo"), mpo)
+    dens = []
+    for j in ch.exciton_sites():
+        p = os.path.join(work, f"D{j}.mpo")
+        kvio.write_mpo(p, H.density_mpo(ch, j))
+        dens.append(p)
+    entry = {"D": c["D"], "seed": c["seed"], "n_sites": ch.n_sites,
+             "site_norms2": [float(sum(np.vdot(a, a).real for _, a in t.blocks)) for t in mps]}
+    # reference-built Hamiltonian on the same model
+    with open(os.path.join(work, "chain.inp"), "w") as f:
+        f.write(ch.reference_input())
+    run([os.path.join(REF_BIN, "kln-holstein"), "-i", "chain.inp", "-t", "1e-14"], work)
+    e_ref = run([os.path.join(REF_BIN, "kln-join"), "-a", "in.mps", "-b", "in.mps", "-o", "Op/H_tot"], work)
+    e_mine = run([os.path.join(REF_BIN, "kln-join"), "-a", "in.mps", "-b", "in.mps", "-o", "H.mpo"], work)
+    entry["energy_ref_mpo"] = float(e_ref.strip().strip("()").split(",")[0])
+    entry["energy_own_mpo"] = float(e_mine.strip().strip("()").split(",")[0])
+    if c["keep_inputs"]:
+        for f in ("in.mps", "H.mpo"):
+            shutil.copy(os.path.join(work, f), os.path.join(out, f))
+        shutil.copy(os.path.join(work, "Op", "H_tot"), os.path.join(out, "H_ref.mpo"))
+        for site in c["ops_sites"]:
+            od = os.path.join(out, f"ops_site{site}")
+            os.makedirs(od, exist_ok=True)
+            run([os.path.join(REF_BIN, "kv_ref_ops"), "-w", "in.mps", "-o", "H.mpo", "-i", str(site),
+                 "-v", "0.05", "-k", "11", "-e", "1e-8", "-t", "1e-8", "-D", str(c["D"]), "-O", od], work)
+    entry["trajectories"] = [trajectory(ch, work, out, stage, maxd, tol, dens) for stage, maxd, tol in c["traj"]]
+    if c.get("mixed_only"):
+        entry["mixed_only"] = True
+    shutil.rmtree(work)
+    return entry
 
 
 if __name__ == "__main__":

@@ -16,7 +16,7 @@ from kylin_v_gb300 import kvio  # noqa: E402
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIBDIR = os.path.join(ROOT, "kylin-v_gb300", "_build")
-REF_DRIVER = "/root/reference/src/kln-tdvp.cpp"
+REF_DRIVER = os.path.join(os.environ.get("KYLINV_REFERENCE", "/root/reference"), "src", "kln-tdvp.cpp")
 
 
 def _cxx():

@@ -161,3 +161,36 @@ def test_mixed_svd(gpu, case, site):
         iso = O.product(uh, uh, r1, O.OP_C, O.OP_N) if l2r else O.product(vh, vh, src.rank - r1, O.OP_N, O.OP_C)
         for _, a in iso.as_dict().items():
             assert np.abs(a - np.eye(a.shape[0])).max() < 1e-12
+
+
+@pytest.mark.parametrize("l2r", [True, False])
+def test_mixed_svd_sector_scales_and_ranks(gpu, l2r):
+    """Charge sectors of very different norms (1 down to 1e-30, and an exactly
+    zero one) and numerical ranks, tall and wide, in one tensor, nothing
+    truncated (cutoff 0): every singular value above the mixed path's floor
+    (1e-6 of its sector's largest) is kept, and U.V reproduces each block to
+    1e-5 of that block's own scale."""
+    rng = np.random.default_rng(7)
+    # rank-3 tensor (l, s, r) with dirs (+1, +1, -1); one block per charge sector
+    specs = [(40, 24, 1.0, 24), (24, 40, 1e-5, 10), (64, 64, 1e-12, 30), (30, 50, 1e-18, 5),
+             (20, 20, 1e-30, 20), (16, 16, 0.0, 16)]
+    blocks, expect = [], 0
+    for q, (m, n, scale, rank) in enumerate(specs):
+        x = (rng.standard_normal((m, rank)) + 1j * rng.standard_normal((m, rank))) @ \
+            np.diag(np.logspace(0, -4, rank)) @ (rng.standard_normal((rank, n)) + 1j * rng.standard_normal((rank, n)))
+        x *= scale
+        sv = np.linalg.svd(x, compute_uv=False)
+        if scale > 0:
+            expect += int((sv > 2e-6 * sv[0]).sum())
+        blocks.append(((q, 0, q), x.reshape(m, 1, n)))
+    t = kvio.BlockTensor((1, 1, -1), blocks)
+    u, v, nk, nt = gpu.svd_impl(t, 2 if l2r else 1, l2r, 0.0, 10000, precision=gpu.KV_MIXED_TF32)
+    assert nt == sum(min(m, n) for m, n, _, _ in specs)
+    assert nk >= expect
+    prod = gpu.product(u, v, 1).to_host().as_dict()
+    for (qn, a) in blocks:
+        if not np.abs(a).max() > 0:
+            continue
+        b = prod.get((qn, a.shape))
+        assert b is not None, qn
+        assert np.abs(a - b).max() <= 1e-5 * np.abs(a).max(), qn

@@ -106,7 +106,10 @@ def _traj_case(case, ti):
     return ch, mps, H.hamiltonian_mpo(ch), ent["trajectories"][ti]
 
 
-TRAJ = [(c, i) for c, e in U.manifest().items() for i in range(len(e["trajectories"]))]
+# the FP64 path against every golden trajectory but the large mixed-only one
+# (tests/test_gpu_mixed_trajectory.py runs that one on the mixed path)
+FP64_CASES = sorted(c for c, e in U.manifest().items() if not e.get("mixed_only"))
+TRAJ = [(c, i) for c in FP64_CASES for i in range(len(U.manifest()[c]["trajectories"]))]
 
 
 @pytest.mark.parametrize("case,ti", TRAJ)
@@ -130,7 +133,7 @@ def test_tdvp_trajectory(gpu, case, ti):
         assert maxb == int(ref[k][-1])
 
 
-@pytest.mark.parametrize("case", sorted(U.manifest()))
+@pytest.mark.parametrize("case", FP64_CASES)
 def test_sweep_reference_flops(gpu, case):
     """The flops a sweep credits (8*M*N*K over every zgemm the reference issues,
     Lanczos iterations as actually run) equal the oracle's count of its own
@@ -150,7 +153,7 @@ def test_sweep_reference_flops(gpu, case):
         assert of > 0 and abs(gf - of) <= 1e-9 * of, (gf, of)
 
 
-@pytest.mark.parametrize("case", sorted(U.manifest()))
+@pytest.mark.parametrize("case", FP64_CASES)
 def test_canonicalize(gpu, case):
     """State::canonicalize on a non-canonical MPS: the state is unchanged,
     sites 1..ns-1 are right-orthonormal, and the bond dimensions equal those

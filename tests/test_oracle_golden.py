@@ -88,7 +88,10 @@ def test_tdvp_trajectory_matches_reference(case, ti):
     ident = H.identity_mpo(ch)
     ref = U.read_traj(f"{G}/{case}/{tr['file']}")
     t = O.Tdvp(mps, mpo, tr["tol_svd"], 1e-8, tr["maxD"], 11, 0.05)
-    for k, mode in enumerate(U.stage_modes(tr["stage"])):
+    modes = U.stage_modes(tr["stage"])
+    if ent.get("mixed_only"):
+        modes = modes[:2]  # the D = 128 case: its first two steps (about 15 s a step here)
+    for k, mode in enumerate(modes):
         t.sweep(mode)
         s = t.mps()
         assert abs(O.join(s, ident, s).real - ref[k][1]) < 1e-12
