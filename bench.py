@@ -21,13 +21,16 @@ roofline   the grouped block-sparse GEMM on the tensor cores: reference flops
            of its block pairs / its event-timed duration, against the
            measured dense FP16/BF16 tensor peak (the digit GEMM runs on the
            FP16 pipe); traffic from the committed ncu summary.
-fp64_compare  the mixed path against the FP64 path on a 4-molecule chain of
-           the same structure over --compare-steps steps: time per step and
-           the largest site-population and energy differences.
+fp64_compare  the mixed path against the plain FP64 GPU path on the same
+           chain over --compare-steps steps (default 1): time per step and the
+           largest site-population and energy differences.
 cpu_baseline  the CPU oracle (restatement of the reference on OpenBLAS, all
-           host threads) on a 3-molecule chain of the same local structure.
+           host threads) on the same chain: one molecule's five two-site local
+           updates (sites 20-24) timed after the pass is advanced there, the
+           full step extrapolated (2 x 159 updates).
 
---impl reference  runs only the CPU oracle (rank 0) and prints its line.
+--impl reference  runs only the CPU oracle sample (rank 0) and prints its line,
+           with a one-thread measurement of the same sample beside it.
 --config holstein-1site-batch64  the batched disordered ensemble instead
            (run_batched); under torchrun its chains are split across ranks.
 N > 1 (torchrun): each rank evolves its own replica chain (a single chain's
@@ -48,7 +51,6 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 METRIC = "TDVP sweep s & H_eff TFLOP/s, mixed vs plain FP64 on GB300 at <=1e-6 pop err"
-CPU_SAMPLE_MOL = 3
 
 
 def parse():
@@ -61,13 +63,14 @@ def parse():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-compare", action="store_true", help="skip the mixed-vs-FP64 comparison leg")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--compare-steps", type=int, default=20,
-                    help="time steps of the mixed-vs-FP64 comparison leg (4-molecule chain)")
+    ap.add_argument("--compare-steps", type=int, default=1,
+                    help="time steps of the mixed-vs-FP64 comparison leg (on the benchmark chain itself)")
     ap.add_argument("--chains", type=int, default=64,
                     help=f"{BATCH_CONFIG}: members of the disordered ensemble advanced together")
     ap.add_argument("--max-streams", type=int, default=0, help=f"{BATCH_CONFIG}: worker streams (0: library default)")
     ap.add_argument("--molecules", type=int, default=None,
                     help="shorter chain with the same local structure (profiling runs)")
+    ap.add_argument("--cpu-only-json", action="store_true", help=argparse.SUPPRESS)
     return ap.parse_args()
 
 
@@ -156,43 +159,70 @@ def build_workload(config: str, seed: int, n_mol: int | None = None):
     return chain, D, d, H.random_mps(chain, D, seed=seed), H.hamiltonian_mpo(chain)
 
 
-def cpu_baseline(config: str, sweeps: int = 1, warm: int = 0):
-    """The CPU oracle (reference restatement, OpenBLAS on all host threads)."""
-    cores = os.cpu_count() or 1
+CPU_WINDOW_SITE, CPU_WINDOW_UPDATES = 20, 5  # one molecule (sites 20-24) of the two-site L->R pass
+
+
+def cpu_baseline(config: str, samples: int = 1, warm: int = 0):
+    """The CPU oracle (restatement of the reference on OpenBLAS, the threads
+    OPENBLAS_NUM_THREADS allows, default all host cores) on the same chain as
+    the GPU: its two-site left-to-right pass is advanced once to site 20, then
+    each sample times the 5 local updates of sites 20-24 (one molecule: the
+    exciton site and both modes' phonon and auxiliary sites) on a copy of that
+    state.  value = reference flops of the sample / its time; the full step
+    (2 x 159 local updates) is extrapolated from it."""
+    cores = int(os.environ.get("OPENBLAS_NUM_THREADS", "0")) or (os.cpu_count() or 1)
     os.environ["OPENBLAS_NUM_THREADS"] = str(cores)
-    chain, D, d, mps, mpo = build_workload(config, 1234, n_mol=CPU_SAMPLE_MOL)
+    chain, D, d, mps, mpo = build_workload(config, 1234)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O  # CPU baseline leg only
 
     t = O.Tdvp(mps, mpo, d["tol_svd"], d["tol_exp"], D, d["max_iter"], d["dt"])
-    for _ in range(warm):
-        t.sweep(d["mode"])
+    i0, n = CPU_WINDOW_SITE, CPU_WINDOW_UPDATES
+    for _ in range(max(1, warm)):  # the first call also advances the pass to site 20 (untimed)
+        t.window(i0, n)
     O.flops(True)
-    times = []
-    for _ in range(sweeps):
-        t0 = time.perf_counter()
-        t.sweep(d["mode"])
-        times.append(time.perf_counter() - t0)
+    secs = [t.window(i0, n) for _ in range(samples)]
     f = O.flops(True)
-    tot = sum(times)
+    tot = sum(secs)
+    updates_per_step = 2 * (chain.n_sites - 1)
     return {"value": f / tot / 1e12, "unit": "TFLOP/s", "cores": cores, "kind": "port",
-            "sample": f"{sweeps} time step(s) of a {CPU_SAMPLE_MOL}-molecule chain ({chain.n_sites} sites) with the "
-                      f"same modes, cutoff, D and tolerances ({f / 1e9:.1f} GFLOP in {tot:.1f} s)",
-            "ms_per_step": 1e3 * tot / sweeps}
+            "sample": f"{n} two-site local updates (sites {i0}-{i0 + n - 1}, one molecule) of the left-to-right pass "
+                      f"of the {chain.n_sites}-site chain, same inputs and tolerances as the GPU run; {samples} "
+                      f"sample(s), {f / samples / 1e9:.1f} GFLOP in {tot / samples:.2f} s each",
+            "ms_per_step": 1e3 * tot / samples * updates_per_step / n,
+            "ms_per_step_note": f"extrapolated: {updates_per_step} local updates per step / {n} per sample"}
+
+
+def cpu_single_thread(config: str, samples: int = 2):
+    """The same CPU sample with one OpenBLAS thread (a child process, so the
+    thread count is set before the library loads)."""
+    env = dict(os.environ, OPENBLAS_NUM_THREADS="1")
+    r = subprocess.run([sys.executable, os.path.abspath(__file__), "--impl", "reference", "--cpu-only-json",
+                        "--config", config, "--steps", str(samples), "--warmup", "0"],
+                       env=env, capture_output=True, text=True, timeout=1800)
+    if r.returncode != 0:
+        return {"unavailable": (r.stderr.strip().splitlines() or ["failed"])[-1]}
+    return json.loads(r.stdout.strip().splitlines()[-1])
 
 
 def run_reference(args):
     ws, rank, _ = dist()
     if rank != 0:
         return
-    _, _, d, _, _ = build_workload(args.config, 1234, n_mol=1)
-    cb = cpu_baseline(args.config, sweeps=args.steps, warm=args.warmup)
+    cb = cpu_baseline(args.config, samples=args.steps, warm=args.warmup)
+    if args.cpu_only_json:
+        print(json.dumps(cb), flush=True)
+        return
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "TFLOP/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": cb["ms_per_step"], "higher_is_better": True,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": cb["ms_per_step"],
+            "ms_per_step_note": cb["ms_per_step_note"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-            "config": {"workload": args.config, "sample_molecules": CPU_SAMPLE_MOL},
+            "config": {"workload": args.config, "same_config": True, "window": cb["sample"]},
             "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": cb["value"], "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    one = cpu_single_thread(args.config)
+    line["single_thread"] = {k: one[k] for k in ("value", "unit", "cores", "ms_per_step") if k in one} if "value" in one \
+        else one
     print(json.dumps(line), flush=True)
 
 
@@ -332,14 +362,16 @@ def run_ours(args):
     if not args.no_compare:
         line["fp64_compare"] = compare_fp64(args, G)
     if not args.no_cpu:
-        line["cpu_baseline"] = {k: v for k, v in cpu_baseline(args.config).items() if k != "ms_per_step"}
+        cb = cpu_baseline(args.config)
+        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        line["cpu_baseline"]["ms_per_step"] = cb["ms_per_step"]
     print(json.dumps(line), flush=True)
 
 
 def compare_fp64(args, G):
-    """Mixed vs plain FP64 GPU path on a 4-molecule chain of the same local
-    structure: time per step and max population / energy error over
-    --compare-steps time steps (20: the accuracy target is stated over 20 steps)."""
+    """Mixed vs plain FP64 GPU path on the benchmark chain itself (same seeded
+    inputs) over --compare-steps time steps: device time per step of each and
+    the largest site-population and energy differences after every step."""
     import numpy as np
 
     import __graft_entry__ as ge
@@ -347,12 +379,13 @@ def compare_fp64(args, G):
     ge.load_package()
     from kylin_v_gb300 import holstein as H
 
-    chain, D, d, mps, mpo = build_workload(args.config, 1234, n_mol=4)
+    chain, D, d, mps, mpo = build_workload(args.config, 1234, n_mol=args.molecules)
     dens = [[G.Tensor.from_host(x) for x in H.density_mpo(chain, j)] for j in chain.exciton_sites()]
     hm = [G.Tensor.from_host(x) for x in mpo]
     runs = {p: G.TDVP(mps, mpo, d["tol_svd"], d["tol_exp"], D, d["max_iter"], d["dt"], p)
             for p in (G.KV_FP64, G.KV_MIXED_TF32)}
     ms = {p: 0.0 for p in runs}
+    modules = {p: {} for p in runs}
     perr = eerr = 0.0
     per_step = []
     nsteps = args.compare_steps
@@ -360,16 +393,20 @@ def compare_fp64(args, G):
         obs = {}
         for p, t in runs.items():
             t.two_site() if d["mode"] == 2 else t.one_site()
-            ms[p] += t.stats()["sweep_ms"]
+            st = t.stats()
+            ms[p] += st["sweep_ms"]
+            for k, v in st["modules_ms"].items():
+                modules[p][k] = modules[p].get(k, 0.0) + v / nsteps
             s = t.sites()
             obs[p] = (np.array([G.expectation(s, x, s).real for x in dens]), G.expectation(s, hm, s).real)
         pe = float(np.abs(obs[G.KV_FP64][0] - obs[G.KV_MIXED_TF32][0]).max())
         per_step.append(float("%.3g" % pe))
         perr = max(perr, pe)
         eerr = max(eerr, abs(obs[G.KV_FP64][1] - obs[G.KV_MIXED_TF32][1]))
-    return {"sample": f"4-molecule chain ({chain.n_sites} sites), {nsteps} steps", "fp64_ms_per_step": ms[G.KV_FP64] / nsteps,
-            "mixed_ms_per_step": ms[G.KV_MIXED_TF32] / nsteps,
+    return {"sample": f"{chain.n_sites}-site benchmark chain, {nsteps} step(s), same inputs",
+            "fp64_ms_per_step": ms[G.KV_FP64] / nsteps, "mixed_ms_per_step": ms[G.KV_MIXED_TF32] / nsteps,
             "speedup_mixed_vs_fp64": ms[G.KV_FP64] / max(1e-9, ms[G.KV_MIXED_TF32]),
+            "fp64_modules_ms_per_step": modules[G.KV_FP64],
             "max_pop_err": perr, "max_energy_err": eerr, "pop_err_by_step": per_step,
             "energy_fp64": float(obs[G.KV_FP64][1])}
 

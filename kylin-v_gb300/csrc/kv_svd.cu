@@ -263,11 +263,12 @@ __global__ void __launch_bounds__(NT) k_svd_jacobi_w(const SvdSector *__restrict
     if (threadIdx.x == 0) status[blockIdx.x] = converged ? sweep : -sweep;
 }
 
-// QR-preconditioned one-sided Jacobi (mixed mode).  One CTA per charge
-// sector; the sector is held in shared memory in FP32 as p rows of length q
-// (row stride q + 1, so column reads by consecutive rows fall in distinct
-// banks), scaled by a power of two so that its largest element lies in
-// [0.5, 1).  The wanted singular vectors are T's left ones (its column space).
+// QR-preconditioned one-sided Jacobi (mixed mode).  One CTA of 512 threads
+// per charge sector; the sector is held in shared memory in FP32 as p rows of
+// length q (row stride q + 1, so reads of one column by consecutive rows fall
+// in distinct banks), scaled by a power of two so that its largest element
+// lies in [0.5, 1).  The wanted singular vectors are T's left ones (its
+// column space).
 //
 //  1. Pivoted Householder from the right on T's rows: at step k the row with
 //     the largest trailing norm (positions k..q-1) is the pivot; the unitary
@@ -279,22 +280,26 @@ __global__ void __launch_bounds__(NT) k_svd_jacobi_w(const SvdSector *__restrict
 //     noise level are M's.  One barrier per step: every warp finds the next
 //     pivot itself from the per-warp maxima of the previous step (double
 //     buffered), and each row's exact trailing norm is accumulated while the
-//     row is updated.
-//  2. One-sided Jacobi on M's r columns (round-robin pairs, 16 lanes a pair,
-//     tolerance `tol` on the cosine); M is row-pivoted triangular, so it
-//     converges in fewer sweeps than T, and only r columns are rotated.
+//     row is updated.  A group of 16 lanes updates two rows at once, so each
+//     pivot-row element it loads serves both.
+//  2. One-sided Jacobi on M's r columns (round-robin pairs, 8 lanes a pair,
+//     each lane holding its EPL elements of both columns in registers between
+//     the dot product and the rotation; tolerance `tol` on the cosine).  M is
+//     row-pivoted triangular, so it converges in fewer sweeps than T, and only
+//     r columns are rotated.  The rotation is formed from one reciprocal
+//     square root of |c|^2 and one of 1 + t^2.
 //  3. Columns sorted by norm: S = norms (descending), Us = normalised columns
 //     (column-major p x r at the sector's t_off), S = 0 in the sector's
 //     remaining slots up to q.
 // status[sector] = Jacobi sweeps used (negative: no convergence), ranks[sector] = r.
 template <int EPL>
-__global__ void __launch_bounds__(1024, 1) k_svd_qrj(const SvdSector *__restrict__ secs,
-                                                     const double2 *__restrict__ T64, float2 *__restrict__ Us,
-                                                     double *__restrict__ S, int *status, int *ranks, int max_sweeps,
-                                                     float tol, float qr_floor) {
-    constexpr int NT = 1024, NW = NT / 32;
-    constexpr int GQ = 8;                      // lanes per row in the QR phase
-    constexpr int GJ = 16;                     // lanes per column pair in the Jacobi phase
+__global__ void __launch_bounds__(512, 1) k_svd_qrj(const SvdSector *__restrict__ secs,
+                                                    const double2 *__restrict__ T64, float2 *__restrict__ Us,
+                                                    double *__restrict__ S, int *status, int *ranks, int max_sweeps,
+                                                    float tol, float qr_floor) {
+    constexpr int NT = 512, NW = NT / 32;
+    constexpr int GQ = 16;                     // lanes per row in the QR phase (two rows at a time)
+    constexpr int GJ = 8;                      // lanes per column pair in the Jacobi phase
     extern __shared__ float2 sw[];
     __shared__ float wbest[2][NW];
     __shared__ int wbesti[2][NW];
@@ -303,19 +308,19 @@ __global__ void __launch_bounds__(1024, 1) k_svd_qrj(const SvdSector *__restrict
     __shared__ int rotated;
     const SvdSector s = secs[blockIdx.x];
     const int p = s.p, q = s.q, ldw = q + 1, kmax = min(p, q);
-    float2 *alph = sw + (int64_t)p * ldw;       // [kmax] reflector values conj(alpha_k)
-    float *rn = reinterpret_cast<float *>(alph + kmax);  // [p] trailing row norms^2
-    float *cn = rn + p;                         // [kmax] column norms^2 (Jacobi), then norms
-    int *piv = reinterpret_cast<int *>(cn + kmax);       // [kmax] pivot rows
-    int *done = piv + kmax;                     // [p] row already pivoted
+    float2 *alph = sw + p * ldw;                          // [kmax] conj(alpha_k)
+    float *cn = reinterpret_cast<float *>(alph + kmax);   // [kmax] column norms^2 (Jacobi), then norms
+    int *piv = reinterpret_cast<int *>(cn + kmax);        // [kmax] pivot rows
+    int *done = piv + kmax;                               // [p] row already pivoted
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
     // ---- load (FP64 column-major p x q -> FP32 rows) scaled by a power of two
     // that brings the largest element to [0.5, 1): sectors whose entries are
     // far below 1 would otherwise underflow FP32 in the squared norms
     const double2 *src = T64 + s.t_off;
+    const int pq = p * q;
     double amax = 0.0;  // largest |re|, |im|; +inf if any element is Inf or NaN
-    for (int64_t e = tid; e < (int64_t)p * q; e += NT) {
+    for (int e = tid; e < pq; e += NT) {
         const double2 v = src[e];
         const double m = fmax(fabs(v.x), fabs(v.y));
         amax = (isfinite(v.x) && isfinite(v.y)) ? fmax(amax, m) : INFINITY;
@@ -335,16 +340,18 @@ __global__ void __launch_bounds__(1024, 1) k_svd_qrj(const SvdSector *__restrict
         return;
     }
     int ex = 0;
-    if (amax > 0.0 && isfinite(amax)) frexp(amax, &ex);
+    if (amax > 0.0) frexp(amax, &ex);
     const double down = ldexp(1.0, -ex), up = ldexp(1.0, ex);  // exact powers of two
-    for (int64_t e = tid; e < (int64_t)p * q; e += NT) {
-        const int i = (int)(e % p), c = (int)(e / p);
+    for (int e = tid; e < pq; e += NT) {
+        const int i = e % p, c = e / p;
         const double2 v = src[e];
-        sw[(int64_t)i * ldw + c] = make_float2((float)(v.x * down), (float)(v.y * down));
+        sw[i * ldw + c] = make_float2((float)(v.x * down), (float)(v.y * down));
     }
     __syncthreads();
+
+    // ---- row norms, the first pivot candidates per warp, Frobenius norm
     const int gq = tid / GQ, gql = tid % GQ, ngq = NT / GQ;
-    const unsigned qmask = 0xFFu << (lane & ~(GQ - 1));
+    const unsigned qmask = 0xFFFFu << (lane & ~(GQ - 1));
     float bv = -1.f;
     int bi = 0x7FFFFFFF;
     float fro = 0.f;
@@ -353,17 +360,16 @@ __global__ void __launch_bounds__(1024, 1) k_svd_qrj(const SvdSector *__restrict
         float a = 0.f;
         if (i < p)
             for (int c = gql; c < q; c += GQ) {
-                const float2 w = sw[(int64_t)i * ldw + c];
+                const float2 w = sw[i * ldw + c];
                 a += w.x * w.x + w.y * w.y;
             }
 #pragma unroll
         for (int o = GQ / 2; o > 0; o >>= 1) a += __shfl_xor_sync(qmask, a, o, GQ);
         if (i < p) {
-            if (gql == 0) { rn[i] = a; done[i] = 0; fro += a; }
+            if (gql == 0) { done[i] = 0; fro += a; }
             if (a > bv || (a == bv && i < bi)) { bv = a; bi = i; }
         }
     }
-    // per-warp maximum (value, lowest index) and the Frobenius norm
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         const float ov = __shfl_xor_sync(0xFFFFFFFFu, bv, o);
@@ -381,8 +387,8 @@ __global__ void __launch_bounds__(1024, 1) k_svd_qrj(const SvdSector *__restrict
     int r = 0;
     for (int k = 0; k < kmax; ++k) {
         const int cur = k & 1;
-        float mv = wbest[cur][lane];
-        int mi = wbesti[cur][lane];
+        float mv = lane < NW ? wbest[cur][lane] : -1.f;
+        int mi = lane < NW ? wbesti[cur][lane] : 0x7FFFFFFF;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             const float ov = __shfl_xor_sync(0xFFFFFFFFu, mv, o);
@@ -392,7 +398,7 @@ __global__ void __launch_bounds__(1024, 1) k_svd_qrj(const SvdSector *__restrict
         if (!(mv > thr2) || mi >= p) break;  // uniform: every warp computed the same maximum
         r = k + 1;
         const int ip = mi;
-        const float2 *xr = sw + (int64_t)ip * ldw;
+        const float2 *xr = sw + ip * ldw;
         // u = conj(x), alpha = -e^{i phi} |u| (phi = arg u_0), v = u - alpha e_0,
         // beta = 2 / |v|^2 = 1 / (|u| (|u| + |u_0|));  x H = conj(alpha) e_0^T
         const float nu = sqrtf(mv);
@@ -408,39 +414,56 @@ __global__ void __launch_bounds__(1024, 1) k_svd_qrj(const SvdSector *__restrict
         }
         float gbv = -1.f;
         int gbi = 0x7FFFFFFF;
-        for (int i0 = 0; i0 < p; i0 += ngq) {
-            const int i = i0 + gq;
-            const bool live = i < p && i != ip && !done[i];
-            // group-uniform: every lane of the group has the same i
-            if (live) {
-                float2 *wr = sw + (int64_t)i * ldw;
-                float sr = 0.f, si = 0.f;  // s = sum_c w_c v_c, v_c = conj(x_c) (c > k)
-                for (int c = k + gql; c < q; c += GQ) {
-                    const float2 w = wr[c];
-                    const float2 vc = c == k ? v0 : make_float2(xr[c].x, -xr[c].y);
-                    sr += w.x * vc.x - w.y * vc.y;
-                    si += w.x * vc.y + w.y * vc.x;
-                }
-#pragma unroll
-                for (int o = GQ / 2; o > 0; o >>= 1) {
-                    sr += __shfl_xor_sync(qmask, sr, o, GQ);
-                    si += __shfl_xor_sync(qmask, si, o, GQ);
-                }
-                const float fr = beta * sr, fi = beta * si;
-                float tn = 0.f;
-                for (int c = k + gql; c < q; c += GQ) {
-                    float2 w = wr[c];
-                    const float2 cv = c == k ? make_float2(v0.x, -v0.y) : xr[c];  // conj(v_c)
-                    w.x -= fr * cv.x - fi * cv.y;
-                    w.y -= fr * cv.y + fi * cv.x;
-                    wr[c] = w;
-                    if (c > k) tn += w.x * w.x + w.y * w.y;
-                }
-#pragma unroll
-                for (int o = GQ / 2; o > 0; o >>= 1) tn += __shfl_xor_sync(qmask, tn, o, GQ);
-                if (gql == 0) rn[i] = tn;
-                if (tn > gbv || (tn == gbv && i < gbi)) { gbv = tn; gbi = i; }
+        for (int i0 = gq; i0 < p; i0 += 2 * ngq) {
+            const int iA = i0, iB = i0 + ngq;
+            // group-uniform: every lane of the group has the same rows
+            const bool lA = iA != ip && !done[iA];
+            const bool lB = iB < p && iB != ip && !done[iB];
+            if (!lA && !lB) continue;
+            float2 *wa = sw + iA * ldw, *wb = sw + (lB ? iB : iA) * ldw;
+            // s = sum_c w_c v_c, v_c = conj(x_c) for c > k, v_k = v0
+            float sar = 0.f, sai = 0.f, sbr = 0.f, sbi = 0.f;
+            for (int c = k + gql; c < q; c += GQ) {
+                const float2 xc = xr[c];
+                const float2 vc = c == k ? v0 : make_float2(xc.x, -xc.y);
+                const float2 a = wa[c], b = wb[c];
+                sar += a.x * vc.x - a.y * vc.y;
+                sai += a.x * vc.y + a.y * vc.x;
+                sbr += b.x * vc.x - b.y * vc.y;
+                sbi += b.x * vc.y + b.y * vc.x;
             }
+#pragma unroll
+            for (int o = GQ / 2; o > 0; o >>= 1) {
+                sar += __shfl_xor_sync(qmask, sar, o, GQ);
+                sai += __shfl_xor_sync(qmask, sai, o, GQ);
+                sbr += __shfl_xor_sync(qmask, sbr, o, GQ);
+                sbi += __shfl_xor_sync(qmask, sbi, o, GQ);
+            }
+            const float far = lA ? beta * sar : 0.f, fai = lA ? beta * sai : 0.f;
+            const float fbr = lB ? beta * sbr : 0.f, fbi = lB ? beta * sbi : 0.f;
+            float ta = 0.f, tb = 0.f;
+            for (int c = k + gql; c < q; c += GQ) {
+                const float2 xc = xr[c];
+                const float2 cv = c == k ? make_float2(v0.x, -v0.y) : xc;  // conj(v_c)
+                float2 a = wa[c], b = wb[c];
+                a.x -= far * cv.x - fai * cv.y;
+                a.y -= far * cv.y + fai * cv.x;
+                b.x -= fbr * cv.x - fbi * cv.y;
+                b.y -= fbr * cv.y + fbi * cv.x;
+                if (lA) wa[c] = a;
+                if (lB) wb[c] = b;
+                if (c > k) {
+                    ta += a.x * a.x + a.y * a.y;
+                    tb += b.x * b.x + b.y * b.y;
+                }
+            }
+#pragma unroll
+            for (int o = GQ / 2; o > 0; o >>= 1) {
+                ta += __shfl_xor_sync(qmask, ta, o, GQ);
+                tb += __shfl_xor_sync(qmask, tb, o, GQ);
+            }
+            if (lA && (ta > gbv || (ta == gbv && iA < gbi))) { gbv = ta; gbi = iA; }
+            if (lB && (tb > gbv || (tb == gbv && iB < gbi))) { gbv = tb; gbi = iB; }
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
@@ -454,14 +477,15 @@ __global__ void __launch_bounds__(1024, 1) k_svd_qrj(const SvdSector *__restrict
     // pivot rows: conj(alpha_k) at position k, zeros after it (within the r columns kept)
     for (int e = tid; e < r * r; e += NT) {
         const int kk = e / r, c = e % r;
-        if (c >= kk) sw[(int64_t)piv[kk] * ldw + c] = c == kk ? alph[kk] : make_float2(0.f, 0.f);
+        if (c >= kk) sw[piv[kk] * ldw + c] = c == kk ? alph[kk] : make_float2(0.f, 0.f);
     }
     __syncthreads();
 
     // ---- one-sided Jacobi on the r columns of M
     const int gj = tid / GJ, gjl = tid % GJ, ngj = NT / GJ;
-    const unsigned jmask = 0xFFFFu << (lane & ~(GJ - 1));
+    const unsigned jmask = 0xFFu << (lane & ~(GJ - 1));
     const float zt = 1e-14f * fro2;  // (1e-7 ||T||_F)^2: numerically zero columns
+    const float tol2 = tol * tol;
     const int qe = r + (r & 1), m1 = qe - 1;
     int sweep = 0;
     bool converged = r < 2;
@@ -469,7 +493,7 @@ __global__ void __launch_bounds__(1024, 1) k_svd_qrj(const SvdSector *__restrict
         for (int j = warp; j < r; j += NW) {
             float a = 0.f;
             for (int i = lane; i < p; i += 32) {
-                const float2 x = sw[(int64_t)i * ldw + j];
+                const float2 x = sw[i * ldw + j];
                 a += x.x * x.x + x.y * x.y;
             }
 #pragma unroll
@@ -494,8 +518,8 @@ __global__ void __launch_bounds__(1024, 1) k_svd_qrj(const SvdSector *__restrict
 #pragma unroll
                     for (int kk = 0; kk < EPL; ++kk) {
                         const int i = gjl + kk * GJ;
-                        xv[kk] = i < p ? sw[(int64_t)i * ldw + c0] : make_float2(0.f, 0.f);
-                        yv[kk] = i < p ? sw[(int64_t)i * ldw + c1] : make_float2(0.f, 0.f);
+                        xv[kk] = i < p ? sw[i * ldw + c0] : make_float2(0.f, 0.f);
+                        yv[kk] = i < p ? sw[i * ldw + c1] : make_float2(0.f, 0.f);
                         a1 = __ffma2_rn(xv[kk], yv[kk], a1);
                         a2 = __ffma2_rn(xv[kk], make_float2(yv[kk].y, yv[kk].x), a2);
                     }
@@ -503,7 +527,7 @@ __global__ void __launch_bounds__(1024, 1) k_svd_qrj(const SvdSector *__restrict
                     ci = a2.x - a2.y;
                 } else {
                     for (int i = gjl; i < p; i += GJ) {
-                        const float2 xi = sw[(int64_t)i * ldw + c0], yi = sw[(int64_t)i * ldw + c1];
+                        const float2 xi = sw[i * ldw + c0], yi = sw[i * ldw + c1];
                         cr += xi.x * yi.x + xi.y * yi.y;
                         ci += xi.x * yi.y - xi.y * yi.x;
                     }
@@ -513,15 +537,18 @@ __global__ void __launch_bounds__(1024, 1) k_svd_qrj(const SvdSector *__restrict
                     cr += __shfl_xor_sync(jmask, cr, o, GJ);
                     ci += __shfl_xor_sync(jmask, ci, o, GJ);
                 }
-                const float ac = sqrtf(cr * cr + ci * ci);
-                if (!(ac > tol * sqrtf(a * b))) continue;
-                const float z = (b - a) / (2.f * ac);
-                const float tn = copysignf(1.f, z) / (fabsf(z) + sqrtf(1.f + z * z));
+                // |c|^2 <= tol^2 a b: the pair is orthogonal to the tolerance
+                const float ac2 = cr * cr + ci * ci;
+                if (!(ac2 > tol2 * a * b)) continue;
+                const float rac = rsqrtf(ac2);  // 1 / |c|
+                const float ac = ac2 * rac;
+                const float z = 0.5f * (b - a) * rac;
+                const float tn = copysignf(1.f, z) / (fabsf(z) + sqrtf(fmaf(z, z, 1.f)));
                 kvj::Rot<float> rot;
-                rot.cs = 1.f / sqrtf(1.f + tn * tn);
+                rot.cs = rsqrtf(fmaf(tn, tn, 1.f));
                 const float sn = tn * rot.cs;
-                rot.s_re = sn * cr / ac;
-                rot.s_im = sn * ci / ac;
+                rot.s_re = sn * cr * rac;
+                rot.s_im = sn * ci * rac;
                 if (gjl == 0) {
                     rotated = 1;
                     cn[c0] = a - tn * ac;
@@ -541,16 +568,16 @@ __global__ void __launch_bounds__(1024, 1) k_svd_qrj(const SvdSector *__restrict
                         ny = __ffma2_rn(sr2, xo, ny);
                         ny = __ffma2_rn(pm, make_float2(xo.y, xo.x), ny);
                         if (i < p) {
-                            sw[(int64_t)i * ldw + c0] = nx;
-                            sw[(int64_t)i * ldw + c1] = ny;
+                            sw[i * ldw + c0] = nx;
+                            sw[i * ldw + c1] = ny;
                         }
                     }
                 } else {
                     for (int i = gjl; i < p; i += GJ) {
-                        float2 xi = sw[(int64_t)i * ldw + c0], yi = sw[(int64_t)i * ldw + c1];
+                        float2 xi = sw[i * ldw + c0], yi = sw[i * ldw + c1];
                         kvj::rotate_pair(rot, xi.x, xi.y, yi.x, yi.y);
-                        sw[(int64_t)i * ldw + c0] = xi;
-                        sw[(int64_t)i * ldw + c1] = yi;
+                        sw[i * ldw + c0] = xi;
+                        sw[i * ldw + c1] = yi;
                     }
                 }
             }
@@ -564,7 +591,7 @@ __global__ void __launch_bounds__(1024, 1) k_svd_qrj(const SvdSector *__restrict
     for (int j = warp; j < r; j += NW) {
         float a = 0.f;
         for (int i = lane; i < p; i += 32) {
-            const float2 x = sw[(int64_t)i * ldw + j];
+            const float2 x = sw[i * ldw + j];
             a += x.x * x.x + x.y * x.y;
         }
 #pragma unroll
@@ -578,7 +605,7 @@ __global__ void __launch_bounds__(1024, 1) k_svd_qrj(const SvdSector *__restrict
         for (int i = 0; i < r; ++i) rank += (cn[i] > sj) || (cn[i] == sj && i < j);
         const float inv = sj > 0.f ? 1.f / sj : 0.f;
         for (int i = lane; i < p; i += 32) {
-            const float2 x = sw[(int64_t)i * ldw + j];
+            const float2 x = sw[i * ldw + j];
             Us[s.t_off + (int64_t)rank * p + i] = make_float2(x.x * inv, x.y * inv);
         }
         if (lane == 0) S[s.s_off + rank] = (double)sj * up;
@@ -823,9 +850,9 @@ int qrj_smem_limit(int dev) {
         KV_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
         const int bytes = std::max(0, optin - 1024);  // less the kernel's static arrays
         KV_CUDA(cudaFuncSetAttribute(k_svd_qrj<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-        KV_CUDA(cudaFuncSetAttribute(k_svd_qrj<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
         KV_CUDA(cudaFuncSetAttribute(k_svd_qrj<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
         KV_CUDA(cudaFuncSetAttribute(k_svd_qrj<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        KV_CUDA(cudaFuncSetAttribute(k_svd_qrj<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
         g_qrj_smem[dev] = bytes;
         g_qrj_set[dev] = true;
     }
@@ -911,7 +938,7 @@ void svd_jacobi_f32(const SvdPlan &p, const double2 *T64, float2 *T, int *status
 // shared-memory bytes of k_svd_qrj for a p x q sector
 static size_t qrj_smem(int p, int q) {
     const size_t kmax = (size_t)std::min(p, q);
-    return sizeof(float2) * ((size_t)p * (q + 1) + kmax) + sizeof(float) * (2 * (size_t)p + 2 * kmax);
+    return sizeof(float2) * ((size_t)p * (q + 1) + kmax) + sizeof(float) * ((size_t)p + 2 * kmax);
 }
 
 bool svd_qrjacobi_f32(const SvdPlan &p, const double2 *T64, float2 *Us, double *S, int *status, int *ranks,
@@ -926,12 +953,13 @@ bool svd_qrjacobi_f32(const SvdPlan &p, const double2 *T64, float2 *Us, double *
     }
     if (smem > (size_t)limit) return false;
     auto launch = [&](auto kernel) {
-        kernel<<<(unsigned)p.secs.size(), 1024, smem, ctx().stream>>>(p.d_secs.as<SvdSector>(), T64, Us, S, status,
-                                                                      ranks, max_sweeps, tol, qr_floor);
+        kernel<<<(unsigned)p.secs.size(), 512, smem, ctx().stream>>>(p.d_secs.as<SvdSector>(), T64, Us, S, status,
+                                                                     ranks, max_sweeps, tol, qr_floor);
     };
-    if (max_p <= 32) launch(k_svd_qrj<2>);
-    else if (max_p <= 64) launch(k_svd_qrj<4>);
-    else if (max_p <= 128) launch(k_svd_qrj<8>);
+    // elements per lane from the longest column of the launch (8 lanes a pair)
+    if (max_p <= 32) launch(k_svd_qrj<4>);
+    else if (max_p <= 64) launch(k_svd_qrj<8>);
+    else if (max_p <= 128) launch(k_svd_qrj<16>);
     else launch(k_svd_qrj<0>);
     counted();
     KV_CUDA(cudaGetLastError());

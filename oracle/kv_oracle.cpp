@@ -16,10 +16,13 @@
  *   ops:     kvo_product, kvo_apply_zero/single/double, kvo_env_sweep,
  *            kvo_local_krylov, kvo_svd
  *   sweep:   kvo_tdvp_new / kvo_tdvp_sweep (mode 0: one global-Krylov step,
- *            1: one_site, 2: two_site) / kvo_tdvp_site / kvo_tdvp_free
+ *            1: one_site, 2: two_site) / kvo_tdvp_site / kvo_tdvp_free;
+ *            kvo_tdvp_window times a window of two-site local updates
+ *            (CPU-baseline timing)
  *   observable: kvo_join
  */
 #include <algorithm>
+#include <chrono>
 #include <array>
 #include <cmath>
 #include <complex>
@@ -505,6 +508,7 @@ struct Tdvp {
     std::vector<Tensor> envL, envR;
     double tol_svd, tol_exp, dt;
     int max_dim, max_iter;
+    int window_at = -1;  // two-site L->R pass advanced to this site by kvo_tdvp_window (-1: not started)
 };
 
 Tensor boundary(int rank3_dirs0, int q) {
@@ -555,25 +559,30 @@ void one_site(Tdvp &s) {
     }
 }
 
+// one local update of TDVP::two_site's left-to-right pass at sites (i, i+1)
+// (holstein/tdvp.h:150-185)
+void two_site_lr(Tdvp &s, int i) {
+    const int ns = (int)s.mps.size();
+    Tensor mm = product(s.mps[i], s.mps[i + 1], 1, OP_N, OP_N);
+    local_krylov(2, s.envL.back(), mm, &s.mpo[i], &s.mpo[i + 1], s.envR.back(), s.dt, s.max_iter, s.tol_exp, false);
+    SvdResult r = svd_impl(mm, 2, true, s.tol_svd, s.max_dim);
+    if (i < ns - 2) {
+        s.mps[i] = std::move(r.U);
+        s.envL.push_back(env_sweep(s.envL.back(), s.mps[i], s.mpo[i], true));
+        local_krylov(1, s.envL.back(), r.V, &s.mpo[i + 1], nullptr, s.envR.back(), s.dt, s.max_iter, s.tol_exp, true);
+        s.mps[i + 1] = std::move(r.V);
+        s.envR.pop_back();
+    } else {
+        s.mps[i] = std::move(r.U);
+        s.mps[i + 1] = std::move(r.V);
+    }
+}
+
 // TDVP::two_site (holstein/tdvp.h:144-227)
 void two_site(Tdvp &s) {
     const int ns = (int)s.mps.size();
     s.envR.pop_back();
-    for (int i = 0; i < ns - 1; ++i) {
-        Tensor mm = product(s.mps[i], s.mps[i + 1], 1, OP_N, OP_N);
-        local_krylov(2, s.envL.back(), mm, &s.mpo[i], &s.mpo[i + 1], s.envR.back(), s.dt, s.max_iter, s.tol_exp, false);
-        SvdResult r = svd_impl(mm, 2, true, s.tol_svd, s.max_dim);
-        if (i < ns - 2) {
-            s.mps[i] = std::move(r.U);
-            s.envL.push_back(env_sweep(s.envL.back(), s.mps[i], s.mpo[i], true));
-            local_krylov(1, s.envL.back(), r.V, &s.mpo[i + 1], nullptr, s.envR.back(), s.dt, s.max_iter, s.tol_exp, true);
-            s.mps[i + 1] = std::move(r.V);
-            s.envR.pop_back();
-        } else {
-            s.mps[i] = std::move(r.U);
-            s.mps[i + 1] = std::move(r.V);
-        }
-    }
+    for (int i = 0; i < ns - 1; ++i) two_site_lr(s, i);
     for (int i = ns - 1; i > 0; --i) {
         Tensor mm = product(s.mps[i - 1], s.mps[i], 1, OP_N, OP_N);
         local_krylov(2, s.envL.back(), mm, &s.mpo[i - 1], &s.mpo[i], s.envR.back(), s.dt, s.max_iter, s.tol_exp, false);
@@ -1035,10 +1044,33 @@ int kvo_tdvp_new(int ns, void **mps, void **mpo, double tol_svd, double tol_exp,
 int kvo_tdvp_sweep(void *h, int mode) {
     return guarded([&] {
         auto *s = static_cast<Tdvp *>(h);
+        if (s->window_at >= 0) throw std::runtime_error("the handle is inside a timed window; it cannot sweep");
         if (mode == 1) one_site(*s);
         else if (mode == 2) two_site(*s);
         else if (mode == 0) global_step(*s);
         else throw std::runtime_error("mode must be 0, 1 or 2");
+    });
+}
+
+// Timing hook of the CPU baseline (no reference counterpart): the two-site
+// left-to-right pass is advanced (once, untimed) to site i0, then n local
+// updates from there are run on a copy of that state and timed; the handle
+// stays at i0, so every call with the same (i0, n) repeats the same work.
+int kvo_tdvp_window(void *h, int i0, int n, double *seconds) {
+    return guarded([&] {
+        auto *s = static_cast<Tdvp *>(h);
+        const int ns = (int)s->mps.size();
+        if (n < 1 || i0 < 0 || i0 + n > ns - 2) throw std::runtime_error("window outside the two-site pass");
+        if (s->window_at < 0) {
+            s->envR.pop_back();
+            s->window_at = 0;
+        }
+        if (i0 < s->window_at) throw std::runtime_error("window behind the pass already advanced");
+        for (; s->window_at < i0; ++s->window_at) two_site_lr(*s, s->window_at);
+        Tdvp c = *s;
+        const auto t0 = std::chrono::steady_clock::now();
+        for (int i = i0; i < i0 + n; ++i) two_site_lr(c, i);
+        *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     });
 }
 

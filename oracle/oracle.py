@@ -50,6 +50,7 @@ def lib():
                                    ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                    ctypes.POINTER(vp)]
         L.kvo_tdvp_sweep.argtypes = [vp, ctypes.c_int]
+        L.kvo_tdvp_window.argtypes = [vp, ctypes.c_int, ctypes.c_int, dp]
         L.kvo_tdvp_site.argtypes = [vp, ctypes.c_int, ctypes.POINTER(vp)]
         L.kvo_tdvp_free.argtypes = [vp]
         L.kvo_tdvp_free.restype = None
@@ -175,6 +176,13 @@ class Tdvp:
         _check(lib().kvo_tdvp_new(ns, arr_m, arr_o, tol_svd, tol_exp, max_dim, max_iter, dt, ctypes.byref(out)))
         self.ptr = out.value
         self.ns = ns
+
+    def window(self, i0, n) -> float:
+        """Seconds for n two-site local updates of the left-to-right pass from
+        site i0, on a copy of the state advanced (once) to i0."""
+        sec = ctypes.c_double()
+        _check(lib().kvo_tdvp_window(self.ptr, i0, n, ctypes.byref(sec)))
+        return sec.value
 
     def sweep(self, mode):
         _check(lib().kvo_tdvp_sweep(self.ptr, mode))
