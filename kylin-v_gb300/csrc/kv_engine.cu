@@ -567,7 +567,14 @@ HeffPlan plan_heff(int nsite, const Meta &L, const Meta &psi, const Meta *W1, co
             for (int i = 0; i < K.rank - 1; ++i) M *= b.shape[i];
             add_zero_tiles(H.p2.gemm, b.off, M, b.shape[K.rank - 1], kTileM(precision), kTileN(precision));
         }
+    // Both products contract indices along which the operands' magnitudes
+    // span orders of magnitude: the first the bond index of psi (its entries
+    // fall with the bond's Schmidt values), the second (MPO channel, bond)
+    // (accumulated block energy against identity, and the other bond's
+    // Schmidt values).  The mixed path balances those indices before slicing.
+    H.p1.gemm.balance_k = true;
     H.p1.gemm.upload();
+    H.p2.gemm.balance_k = true;
     H.p2.gemm.upload();
     if (nsite >= 1) H.m1.mix.upload();
     if (nsite == 2) H.m2.mix.upload();

@@ -294,6 +294,7 @@ struct SliceJob {
     int conj;   // negate the imaginary part
     int exp_off, nkc;
     int entry;  // first step at which a segment reading this block is active
+    int ks_off; // balanced plans: first of this view's K power-of-two scale entries (-1: none)
 };
 // Tensor-core path: a segment's sliced A and B blocks.
 struct SegX {
@@ -314,7 +315,13 @@ struct GemmPlan {
     // tiles whose segments are all inactive at the launch's step write zeros
     // (false: they write nothing; for intermediates only read by active consumers)
     bool write_inactive = true;
-    // tensor-core path only
+    // tensor-core path only.  balance_k: the contracted index is balanced
+    // before slicing -- column k of every A view scaled by 2^s_k, row k of
+    // every B view by 2^-s_k, s_k from the largest |A[., k]| and |B[k, .]|
+    // over the views that meet in a segment -- so that digits of operands
+    // whose magnitudes vary along k (MPO channels) keep their precision.
+    bool balance_k = false;
+    int64_t k_scales = 0;  // entries of the per-k maxima arrays
     std::vector<SliceJob> ajobs, bjobs;
     std::vector<SegX> xsegs;
     std::vector<int2> aitems, bitems;  // (job, first of 8 rows) per slicing CTA

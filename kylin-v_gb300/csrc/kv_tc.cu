@@ -7,40 +7,48 @@
 //  1. Slicing (k_slice, once per operand per call).  Every GEMM row of an A
 //     block (and every GEMM column of a B block) gets a binary exponent e
 //     with max_k |x| < 2^e over that row; each real value becomes the
-//     fixed-point integer X = round(x 2^(29-e)), |X| <= 2^29, written as four
-//     balanced base-256 digits X = d0 2^24 + d1 2^16 + d2 2^8 + d3
-//     (|d0| <= 64, |d1..d3| <= 128) in FP16 (exact).  For the 3M complex form
+//     fixed-point integer X = round(x 2^(37-e)), |X| <= 2^37, written as five
+//     balanced base-256 digits X = d0 2^32 + d1 2^24 + d2 2^16 + d3 2^8 + d4
+//     (|d0| <= 33, |d1..d4| <= 128) in FP16 (exact).  For the 3M complex form
 //     three values are sliced per element: re, im and re + im (the last as
-//     the exact integer sum X_re + X_im).  Integer arithmetic only.  The
-//     digits are written directly in the tensor cores' shared-memory panel
-//     layout (K-major, no swizzle: 8-row x 16-byte core matrices, K-adjacent
-//     core matrices 128 B apart, 8-row groups 256 B apart), one 16-deep K
-//     panel after another, all 12 digit planes of a panel contiguous, so a
-//     pipeline stage is one bulk copy per operand.
+//     the exact integer sum X_re + X_im).  Integer arithmetic only.  Where
+//     the contracted index runs over parts of very different magnitude (MPO
+//     channels, Schmidt values), it is first balanced by exact powers of two
+//     (k_kmax, GemmPlan::balance_k).  The digits are written directly in the
+//     tensor cores' shared-memory panel layout (K-major, no swizzle: 8-row x
+//     16-byte core matrices, K-adjacent core matrices 128 B apart, 8-row
+//     groups 256 B apart), one 16-deep K panel after another, all 15 digit
+//     planes of a panel contiguous, so a pipeline stage is one bulk copy per
+//     operand.
 //  2. Products (k_gemm_tc).  T1 = Ar Br, T2 = Ai Bi, T3 = As Bs are formed as
-//     digit-pair products of orders o = i + j <= 4 (13 per real product, 39
+//     digit-pair products of orders o = i + j <= 4 (15 per real product, 45
 //     tcgen05.mma.kind::f16 of M=128, N=32, K=16 per K panel) into 15 FP32
 //     accumulators in tensor memory.  Every digit product is an integer of
-//     at most 2^14 in magnitude, and at most 336 K-steps are accumulated
-//     between drains, so every accumulator is an integer below 2^24 and the
-//     FP32 accumulation is exact.
+//     at most 2^14 in magnitude, an order sums at most 2^16 of them per K
+//     step, and at most 240 K-steps are accumulated between drains, so every
+//     accumulator is an integer below 2^24 and the FP32 accumulation is
+//     exact.
 //  3. Drains (epilogue warps).  At the end of each segment (one block pair)
-//     or every 336 K, the accumulators are read with tcgen05.ld, converted to
-//     int64 (sum_o P_o 2^(8(4-o))), combined into Cr = T1 - T2 and
-//     Ci = T3 - T1 - T2, aligned to the tile's largest row/column exponents
-//     and added to int64 running sums; the final sums are converted to FP64
-//     by integer operations (exponent and mantissa assembled directly).
+//     or every 240 K, the accumulators are read with tcgen05.ld, converted to
+//     int64 (sum_o P_o 2^(8(4-o)) = X Y / 2^32), combined into Cr = T1 - T2
+//     and Ci = T3 - T1 - T2, aligned to the tile's largest row/column
+//     exponents and added to int64 running sums; the final sums are converted
+//     to FP64 by integer operations (exponent and mantissa assembled
+//     directly).
 //
-// Result: each output element is exact up to the rounding of X (2^-30 of
-// the row/column maximum) and the dropped digit orders 5 and 6 (below
-// 2^-34 of the same scale), i.e. ~1e-10 relative to max|A_row| max|B_col| K,
-// with no FP64 arithmetic in the GEMM.
+// Result: each output element is exact up to the rounding of X (2^-38 of
+// the row/column maximum) and the dropped digit orders 5 to 8 (below
+// 2^-33 of the same scale), i.e. ~1e-10 relative to max|A_row| max|B_col| K
+// (the 30-bit form this replaced left ~1e-8 per product, too much for 20
+// time steps of a 160-site chain), with no FP64 arithmetic in the GEMM.
 //
 // Pipeline: warp 0 (one thread) issues the bulk copies of 3 stages
 // (cp.async.bulk completing on mbarriers), warp 1 allocates tensor memory and
 // one thread issues the MMAs (tcgen05.commit frees a stage and signals a
-// drain), warps 2-9 drain (two per 32-lane quarter of tensor memory, each
-// taking half of the tile's columns).
+// drain), warps 2-17 drain (four per 32-lane quarter of tensor memory, each
+// taking a quarter of the tile's columns: the drain is a long chain of
+// dependent integer operations per column, so it is spread thin and four
+// warps per scheduler hide its latency).
 // Every mbarrier wait is bounded; on timeout the CTA records an error, waits
 // (bounded) for its copies and MMAs in flight, frees tensor memory and exits.
 #include <mutex>
@@ -58,7 +66,7 @@ namespace kv {
 namespace {
 
 constexpr int BM = kMixedTileM, BN = kMixedTileN, BKC = 16;
-constexpr int NDIG = 4, NORD = 5, NCOMP = 3;
+constexpr int NDIG = 5, NORD = 5, NCOMP = 3;
 constexpr int NPL = NCOMP * NDIG;              // digit planes per operand
 constexpr int A_PANEL = NPL * BM * BKC;        // FP16 elements per A panel (all planes)
 constexpr int B_PANEL = NPL * BN * BKC;
@@ -67,42 +75,47 @@ constexpr int PLANE_A = BM * BKC * 2, PLANE_B = BN * BKC * 2;  // bytes per plan
 constexpr int STAGES = 3;
 constexpr int NACC = NCOMP * NORD;             // accumulators of BN columns
 constexpr uint32_t TMEM_COLS = 512;            // NACC * BN = 480, rounded to a power of two
-constexpr int KDRAIN = 336;                    // K-steps accumulated exactly between drains
+constexpr int KDRAIN = 240;                    // K-steps accumulated exactly between drains
 constexpr int GKC = KDRAIN / BKC;              // K panels per drain group
-constexpr int FRAC = 29;
+constexpr int FRAC = 37;                       // fixed point: X = round(x 2^(FRAC - e)), |X| <= 2^37
+// a drained combination sum_o P_o 2^(8(NORD-1-o)) is X Y / 2^COMB_SHIFT
+constexpr int COMB_SHIFT = 8 * (2 * (NDIG - 1) - (NORD - 1));
 constexpr int kZeroExp = -4000;                // exponent of an all-zero row
 constexpr int kErrTimeout = 1, kErrNonFinite = 2;  // bits of the per-device error word
 constexpr int kMaxFiniteExp = 1024;            // row / column exponents of finite operands are <= 1024
 constexpr long long WAIT_LIMIT = 1ll << 22;   // try_wait polls before a wait gives up
-constexpr int EPI_WARPS = 8;                   // two per tensor-memory lane quarter, 16 columns each
+constexpr int EPI_WARPS = 16;                  // four per tensor-memory lane quarter, 8 columns each
 constexpr int EPI_COLS = BN / (EPI_WARPS / 4);
 constexpr int NTHREADS = 32 * (2 + EPI_WARPS);
-constexpr int SMEM_BYTES = STAGES * (A_BYTES + B_BYTES) + 1024 + 1024;
+constexpr int SMEM_ALIGN = 128;                // stage base alignment (no-swizzle layout, bulk copies)
+constexpr int SMEM_BYTES = STAGES * (A_BYTES + B_BYTES) + SMEM_ALIGN + 1024;
+static_assert(SMEM_BYTES <= 227 * 1024, "pipeline stages exceed the shared memory of one CTA");
 
 static_assert(NACC * BN <= (int)TMEM_COLS, "accumulators exceed tensor memory");
 static_assert(EPI_COLS % 4 == 0, "the drain loads 4 columns per accumulator at once");
 static_assert(A_BYTES + B_BYTES < (1 << 20), "transaction count per stage");
 
 // ----------------------------------------------------------- slicing
-// round(x 2^(29-e)) for |x| < 2^e, from the bits of x (integer operations only)
-__device__ __forceinline__ int fixq(double x, int e) {
+// round(x 2^(FRAC-e)) for |x| < 2^e, from the bits of x (integer operations only)
+__device__ __forceinline__ long long fixq(double x, int e) {
     const unsigned long long u = (unsigned long long)__double_as_longlong(x);
     const int E = (int)((u >> 52) & 0x7FF);
-    const int s = 1046 + e - E;  // X = m >> s with m the 53-bit significand; s >= 24 when |x| < 2^e
+    // X = m >> s with m the 53-bit significand; s >= 53 - FRAC when |x| < 2^e
+    const int s = 1075 - FRAC + e - E;
     if (E == 0 || s >= 64) return 0;
-    int X;
-    if (s < 24) X = 1 << 29;  // only for non-finite input (the exponent came from an inf/NaN row)
-    else X = (int)((((u & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull) + (1ull << (s - 1))) >> s);
+    long long X;
+    if (s < 53 - FRAC) X = 1ll << FRAC;  // only for non-finite input (the exponent came from an inf/NaN row)
+    else X = (long long)((((u & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull) + (1ull << (s - 1))) >> s);
     return (u >> 63) ? -X : X;
 }
 
-__device__ __forceinline__ void digits(int X, int d[NDIG]) {
+__device__ __forceinline__ void digits(long long X, int d[NDIG]) {
 #pragma unroll
     for (int i = NDIG - 1; i > 0; --i) {
-        d[i] = ((X + 128) & 255) - 128;
+        d[i] = (int)(((X + 128) & 255) - 128);
         X = (X - d[i]) >> 8;  // exact
     }
-    d[0] = X;
+    d[0] = (int)X;
 }
 
 // element offset of (row r, k) inside one plane of a TR x 16 panel
@@ -122,13 +135,67 @@ __device__ __forceinline__ __half2 digits2(int d0, int d1) {
 
 // One CTA per (job, 8 consecutive rows); one warp per row: pass 1 finds the
 // row exponent, pass 2 writes the digits of two adjacent K positions per lane.
+// Balancing of the contracted index k: kmax[k] holds the largest |re|, |im|
+// of A's column k over the A views of a segment component, kmax[kscales + k]
+// that of B's row k.  A's column is scaled by 2^s, B's row by 2^-s, with
+// s = floor((E_B - E_A) / 2) from their binary exponents, so both reach about
+// sqrt(max_A max_B) and every digit product is resolved at the same scale.
+__device__ __forceinline__ double balance_factor(const unsigned long long *kmax, int64_t kscales, int64_t k,
+                                                 int b_side) {
+    const int ea = (int)(kmax[k] >> 52), eb = (int)(kmax[kscales + k] >> 52);
+    if (ea == 0 || eb == 0) return 1.0;
+    int sh = (eb - ea) >> 1;
+    if (b_side) sh = -sh;
+    return __longlong_as_double((long long)(1023 + sh) << 52);
+}
+
+// Per-k maxima for balancing: one CTA per (view, 8 rows), one warp per row;
+// the 8 rows' values are reduced in shared memory, then one atomicMax per k
+// (non-negative doubles order like their bit patterns).
+__global__ void __launch_bounds__(256) k_kmax(const SliceJob *__restrict__ ajobs, const int2 *__restrict__ aitems,
+                                              int na, const SliceJob *__restrict__ bjobs,
+                                              const int2 *__restrict__ bitems, const double2 *__restrict__ A,
+                                              const double2 *__restrict__ B, unsigned long long *kmax,
+                                              int64_t kscales, const int *skip, int step) {
+    if (skip && *skip) return;
+    __shared__ unsigned long long red[8][33];
+    const bool is_b = blockIdx.x >= (unsigned)na;
+    const int2 it = is_b ? bitems[blockIdx.x - na] : aitems[blockIdx.x];
+    const SliceJob j = is_b ? bjobs[it.x] : ajobs[it.x];
+    if (j.entry > step || j.ks_off < 0) return;  // uniform over the CTA
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r = it.y + warp;
+    const double2 *s = (is_b ? B : A) + j.src_off;
+    unsigned long long *dst = kmax + (is_b ? kscales : 0) + j.ks_off;
+    for (int k0 = 0; k0 < j.K; k0 += 32) {
+        const int k = k0 + lane;
+        unsigned long long m = 0;
+        if (r < j.rows && k < j.K) {
+            const double2 v = s[j.trans ? (int64_t)k * j.ld + r : (int64_t)r * j.ld + k];
+            const unsigned long long br = (unsigned long long)__double_as_longlong(v.x) & 0x7FFFFFFFFFFFFFFFull;
+            const unsigned long long bi = (unsigned long long)__double_as_longlong(v.y) & 0x7FFFFFFFFFFFFFFFull;
+            m = max(br, bi);
+        }
+        red[warp][lane] = m;
+        __syncthreads();
+        if (warp == 0) {
+            unsigned long long x = 0;
+#pragma unroll
+            for (int w = 0; w < 8; ++w) x = max(x, red[w][lane]);
+            if (x && k < j.K) atomicMax(dst + k, x);
+        }
+        __syncthreads();
+    }
+}
+
 // A row holding an Inf or NaN sets bit kErrNonFinite of *err: fixed point has
 // no code for it, and the digits written for that row are meaningless.
 template <int TR>
 __global__ void __launch_bounds__(256) k_slice(const SliceJob *__restrict__ jobs, const int2 *__restrict__ items,
                                                const double2 *__restrict__ src, __half *__restrict__ dst,
                                                int *__restrict__ exps, double alpha, const int *skip, int step,
-                                               int *err) {
+                                               int *err, const unsigned long long *kmax, int64_t kscales,
+                                               int b_side) {
     if (skip && *skip) return;
     const int2 it = items[blockIdx.x];
     const SliceJob j = jobs[it.x];
@@ -141,10 +208,16 @@ __global__ void __launch_bounds__(256) k_slice(const SliceJob *__restrict__ jobs
     const int kpad = j.nkc * BKC;
     const double2 *s = src + j.src_off;
     const bool scale = alpha != 1.0;
+    const bool bal = kmax != nullptr && j.ks_off >= 0;
     auto load = [&](int k) {
         double2 v = s[j.trans ? (int64_t)k * j.ld + r : (int64_t)r * j.ld + k];
         if (scale) { v.x *= alpha; v.y *= alpha; }
         if (j.conj) v.y = -v.y;
+        if (bal) {  // exact power-of-two balancing of the contracted index
+            const double f = balance_factor(kmax, kscales, j.ks_off + k, b_side);
+            v.x *= f;
+            v.y *= f;
+        }
         return v;
     };
     unsigned long long mx = 0;
@@ -164,10 +237,10 @@ __global__ void __launch_bounds__(256) k_slice(const SliceJob *__restrict__ jobs
     __half *pan = dst + j.dst_off + (int64_t)(r / TR) * j.nkc * (NPL * TR * BKC);
     const int rr = r % TR;
     for (int k = 2 * lane; k < kpad; k += 64) {  // k even: k and k + 1 are adjacent in the panel
-        int x[2][NCOMP];
+        long long x[2][NCOMP];
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-            int xr = 0, xi = 0;
+            long long xr = 0, xi = 0;
             if (k + h < j.K) {
                 const double2 v = load(k + h);
                 xr = fixq(v.x, e);
@@ -209,11 +282,43 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo, uint
 // (bits 7-9, 10-12 = 0), both K-major, N >> 3 at bit 17, M >> 4 at bit 24
 constexpr uint32_t IDESC = (1u << 4) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
 
-__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
-        "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate));
+// D (+)= A B with the accumulate flag fixed at compile time (no per-MMA predicate set-up)
+template <bool ACC>
+__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc) {
+    if constexpr (ACC)
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tsetp.eq.u32 p, 1, 1;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+            "l"(adesc), "l"(bdesc), "n"(IDESC));
+    else
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, 1, 1;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+            "l"(adesc), "l"(bdesc), "n"(IDESC));
+}
+
+// The 45 MMAs of one K panel.  Shared-memory descriptors are the stage's
+// plane-0 descriptors plus compile-time plane offsets (a plane offset is a
+// multiple of 16 bytes, and no address leaves the 14-bit field, so adding
+// offset / 16 to the descriptor is adding it to the address).  FIRST: the
+// panel opens a drain group, so each order's first digit pair overwrites its
+// accumulator.
+template <bool FIRST>
+__device__ __forceinline__ void mma_panel(uint32_t tmem, uint64_t da, uint64_t db) {
+#pragma unroll
+    for (int c = 0; c < NCOMP; ++c)
+#pragma unroll
+        for (int o = 0; o < NORD; ++o) {
+            const uint32_t d = tmem + (uint32_t)((c * NORD + o) * BN);
+#pragma unroll
+            for (int i = (o > NDIG - 1 ? o - (NDIG - 1) : 0); i <= (o < NDIG - 1 ? o : NDIG - 1); ++i) {
+                const int jj = o - i;
+                const uint64_t ad = da + (uint64_t)(((c * NDIG + i) * PLANE_A) >> 4);
+                const uint64_t bd = db + (uint64_t)(((c * NDIG + jj) * PLANE_B) >> 4);
+                if (FIRST && i == (o > NDIG - 1 ? o - (NDIG - 1) : 0)) mma_f16<false>(d, ad, bd);
+                else mma_f16<true>(d, ad, bd);
+            }
+        }
 }
 
 __device__ __forceinline__ void mma_commit(uint32_t mbar) {
@@ -296,8 +401,9 @@ __device__ __forceinline__ double i64_ldexp(long long v, int sc) {
 
 // sum_o P_o 2^(8(4-o)) from the five order accumulators (exact integers < 2^24)
 __device__ __forceinline__ long long combine(const float *p) {
-    const int t = __float2int_rn(p[0]) * 256 + __float2int_rn(p[1]);
-    long long u = ((long long)t << 8) + __float2int_rn(p[2]);
+    long long u = __float2int_rn(p[0]);
+    u = (u << 8) + __float2int_rn(p[1]);
+    u = (u << 8) + __float2int_rn(p[2]);
     u = (u << 8) + __float2int_rn(p[3]);
     return (u << 8) + __float2int_rn(p[4]);
 }
@@ -319,7 +425,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_gemm_tc(const GemmTile *__restr
                                                     int write_inactive, long long wait_limit, int no_copies) {
     if (skip && *skip) return;
     extern __shared__ uint8_t smem_raw[];
-    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + SMEM_ALIGN - 1) & ~(uintptr_t)(SMEM_ALIGN - 1));
     uint8_t *sA = smem;
     uint8_t *sB = smem + STAGES * A_BYTES;
     uint64_t *bars = (uint64_t *)(smem + STAGES * (A_BYTES + B_BYTES));
@@ -385,6 +491,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_gemm_tc(const GemmTile *__restr
     } else if (warp == 1) {
         // ------------------------------------------------ MMA issue
         if (lane == 0) {
+            // plane-0 descriptors of stage 0; stage st adds st * bytes / 16 to the address field
+            const uint64_t desc_a0 = make_desc(smem_u32(sA), 128, 256), desc_b0 = make_desc(smem_u32(sB), 128, 256);
             int it = 0, grp = 0;
             bool ok = true;
             for (int ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
@@ -402,22 +510,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_gemm_tc(const GemmTile *__restr
                             const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
                             if (!mbar_wait(smem_u32(full + st), ph, wait_limit)) { ok = false; break; }
                             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                            const uint32_t a0 = smem_u32(sA + st * A_BYTES), b0 = smem_u32(sB + st * B_BYTES);
-#pragma unroll
-                            for (int c = 0; c < NCOMP; ++c)
-#pragma unroll
-                                for (int o = 0; o < NORD; ++o) {
-                                    const uint32_t d = tmem + (uint32_t)((c * NORD + o) * BN);
-#pragma unroll
-                                    for (int i = (o > NDIG - 1 ? o - (NDIG - 1) : 0);
-                                         i <= (o < NDIG - 1 ? o : NDIG - 1); ++i) {
-                                        const int jj = o - i;
-                                        const bool first = (i == (o > NDIG - 1 ? o - (NDIG - 1) : 0));
-                                        const uint64_t ad = make_desc(a0 + (c * NDIG + i) * PLANE_A, 128, 256);
-                                        const uint64_t bd = make_desc(b0 + (c * NDIG + jj) * PLANE_B, 128, 256);
-                                        mma_f16(d, ad, bd, (first && kc == kc0) ? 0u : 1u);
-                                    }
-                                }
+                            const uint64_t da = desc_a0 + (uint64_t)(st * (A_BYTES >> 4));
+                            const uint64_t db = desc_b0 + (uint64_t)(st * (B_BYTES >> 4));
+                            if (kc == kc0) mma_panel<true>(tmem, da, db);
+                            else mma_panel<false>(tmem, da, db);
                             mma_commit(smem_u32(empty + st));  // stage free once these MMAs are done
                         }
                         if (!ok) break;
@@ -511,7 +607,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_gemm_tc(const GemmTile *__restr
                     const int gn = t.n0 + c_lo + c;
                     if (gn < t.N) {
                         const int ec = s_ecol[c_lo + c];
-                        const int sc = erow + ec - 2 * FRAC + 16;
+                        const int sc = erow + ec - 2 * FRAC + COMB_SHIFT;
                         // a row or column holding Inf or NaN (slicer exponent above the
                         // FP64 range) gives NaN, as the FP64 product would
                         crow[gn] = (erow > kMaxFiniteExp || ec > kMaxFiniteExp)
@@ -566,6 +662,7 @@ void plan_mixed(GemmPlan &g) {
     g.a_planes = g.b_planes = 0;
     g.a_exps = g.b_exps = 0;
     std::vector<std::pair<int, int>> seg_mn(g.segs.size(), {0, 0});
+    std::vector<std::pair<int, int>> seg_job(g.segs.size(), {0, 0});  // (A view, B view) of each segment
     for (auto &t : g.tiles)
         for (int s = t.seg_begin; s < t.seg_end; ++s) seg_mn[s] = {t.M, t.N};
     // one job per distinct (block offset, operation) of each operand
@@ -590,6 +687,7 @@ void plan_mixed(GemmPlan &g) {
             j.exp_off = (int)g.a_exps;
             j.nkc = nkc;
             j.entry = kAllSteps;
+            j.ks_off = -1;
             const int nrt = (M + BM - 1) / BM;
             g.a_planes += (int64_t)nrt * nkc * A_PANEL;
             g.a_exps += (int64_t)nrt * BM;
@@ -609,18 +707,52 @@ void plan_mixed(GemmPlan &g) {
             j.exp_off = (int)g.b_exps;
             j.nkc = nkc;
             j.entry = kAllSteps;
+            j.ks_off = -1;
             const int nnt = (N + BN - 1) / BN;
             g.b_planes += (int64_t)nnt * nkc * B_PANEL;
             g.b_exps += (int64_t)nnt * BN;
             ib = bmap.emplace(sg.b_off * 4 + sg.opb, (int)g.bjobs.size()).first;
             g.bjobs.push_back(j);
         }
+        seg_job[s] = {ia->second, ib->second};
         const SliceJob &ja = g.ajobs[ia->second], &jb = g.bjobs[ib->second];
         KV_REQUIRE(ja.rows == M && jb.rows == N && ja.K == sg.K && jb.K == sg.K, KV_EINVAL,
                    "internal: inconsistent block views in a mixed-precision plan");
         g.xsegs[s] = SegX{ja.dst_off, jb.dst_off, nkc, ja.exp_off, jb.exp_off, sg.entry};
         g.ajobs[ia->second].entry = std::min(g.ajobs[ia->second].entry, sg.entry);
         g.bjobs[ib->second].entry = std::min(g.bjobs[ib->second].entry, sg.entry);
+    }
+    // balancing: A and B views joined by a segment share one vector of
+    // per-k scales, so the views of each connected component get one range
+    g.k_scales = 0;
+    if (g.balance_k) {
+        const int na = (int)g.ajobs.size(), nb = (int)g.bjobs.size();
+        std::vector<int> parent(na + nb);
+        for (int i = 0; i < na + nb; ++i) parent[i] = i;
+        auto root = [&](int x) {
+            while (parent[x] != x) x = parent[x] = parent[parent[x]];
+            return x;
+        };
+        for (size_t s = 0; s < g.segs.size(); ++s) {
+            if (seg_mn[s].first == 0) continue;
+            const int a = root(seg_job[s].first), b = root(na + seg_job[s].second);
+            if (a != b) parent[a] = b;
+        }
+        std::vector<int64_t> comp_off(na + nb, -1);
+        std::vector<int> comp_k(na + nb, -1);
+        auto assign = [&](SliceJob &j, int id) {
+            const int c = root(id);
+            if (comp_off[c] < 0) {
+                comp_off[c] = g.k_scales;
+                comp_k[c] = j.K;
+                g.k_scales += j.K;
+            }
+            KV_REQUIRE(comp_k[c] == j.K, KV_EINVAL, "internal: views of one segment component differ in K");
+            j.ks_off = (int)comp_off[c];
+        };
+        for (int i = 0; i < na; ++i) assign(g.ajobs[i], i);
+        for (int i = 0; i < nb; ++i) assign(g.bjobs[i], na + i);
+        KV_REQUIRE(g.k_scales < (1ll << 31), KV_EINVAL, "mixed-precision plan too large");
     }
     g.aitems.clear();
     g.bitems.clear();
@@ -646,15 +778,29 @@ void launch_gemm_mixed(const GemmPlan &p, const double2 *A, const double2 *B, do
     DevBuf ap(std::max<int64_t>(1, p.a_planes) * sizeof(__half)), bp(std::max<int64_t>(1, p.b_planes) * sizeof(__half));
     DevBuf ae(std::max<int64_t>(1, p.a_exps) * sizeof(int)), be(std::max<int64_t>(1, p.b_exps) * sizeof(int));
     int n = 0;
+    DevBuf kmax;
+    const unsigned long long *km = nullptr;
+    if (p.balance_k && p.k_scales > 0 && !p.aitems.empty() && !p.bitems.empty()) {
+        kmax.alloc(2 * (size_t)p.k_scales * sizeof(unsigned long long));
+        KV_CUDA(cudaMemsetAsync(kmax.p, 0, 2 * (size_t)p.k_scales * sizeof(unsigned long long), c.stream));
+        k_kmax<<<(unsigned)(p.aitems.size() + p.bitems.size()), 256, 0, c.stream>>>(
+            p.d_ajobs.as<SliceJob>(), p.d_aitems.as<int2>(), (int)p.aitems.size(), p.d_bjobs.as<SliceJob>(),
+            p.d_bitems.as<int2>(), A, B, kmax.as<unsigned long long>(), p.k_scales, skip, step);
+        KV_CUDA(cudaGetLastError());
+        km = kmax.as<unsigned long long>();
+        ++n;
+    }
     if (!p.aitems.empty()) {
         k_slice<BM><<<(unsigned)p.aitems.size(), 256, 0, c.stream>>>(p.d_ajobs.as<SliceJob>(), p.d_aitems.as<int2>(),
-                                                                     A, ap.as<__half>(), ae.as<int>(), 1.0, skip, step, err);
+                                                                     A, ap.as<__half>(), ae.as<int>(), 1.0, skip, step, err,
+                                                                     km, p.k_scales, 0);
         KV_CUDA(cudaGetLastError());
         ++n;
     }
     if (!p.bitems.empty()) {
         k_slice<BN><<<(unsigned)p.bitems.size(), 256, 0, c.stream>>>(p.d_bjobs.as<SliceJob>(), p.d_bitems.as<int2>(),
-                                                                     B, bp.as<__half>(), be.as<int>(), alpha, skip, step, err);
+                                                                     B, bp.as<__half>(), be.as<int>(), alpha, skip, step, err,
+                                                                     km, p.k_scales, 1);
         KV_CUDA(cudaGetLastError());
         ++n;
     }

@@ -22,11 +22,6 @@ pytestmark = pytest.mark.gpu
 G = U.GOLDEN
 POP_TOL = 1e-6   # max |P_i^mixed(t) - P_i^ref(t)| over sites and steps
 ENERGY_TOL = 1e-6  # relative |E^mixed(t) - E^ref(t)| / |E^ref|
-# One-site TDVP cannot grow a bond, so a state the mixed SVD drops for good
-# changes the manifold the later steps evolve in: the FP32 stage resolves
-# singular values down to 1e-6 of its sector's largest, the reference keeps
-# them down to the 1e-8 cutoff.  The one-site trajectories are held to 1e-5.
-POP_TOL_ONE_SITE = 1e-5
 
 CASES = [(c, i) for c, e in U.manifest().items() for i, t in enumerate(e["trajectories"])
          if t["stage"].startswith("[0,")]  # one- and two-site stages (no global-Krylov step)
@@ -57,15 +52,13 @@ def test_mixed_trajectory_within_population_gate(gpu, case, ti):
     hmpo = [gpu.Tensor.from_host(x) for x in mpo]
     t = gpu.TDVP(mps, mpo, tr["tol_svd"], 1e-8, tr["maxD"], 11, 0.05, gpu.KV_MIXED_3M_DIGITS)
     worst_p = worst_e = 0.0
-    modes = U.stage_modes(tr["stage"])
-    pop_tol = POP_TOL if 2 in modes else POP_TOL_ONE_SITE
-    for k, mode in enumerate(modes):
+    for k, mode in enumerate(U.stage_modes(tr["stage"])):
         t.sweep(mode)
         s = t.sites()
         pops = np.array([gpu.expectation(s, d, s).real for d in dens])
         e = gpu.expectation(s, hmpo, s).real
         worst_p = max(worst_p, float(np.abs(pops - ref[k][3:3 + len(dens)]).max()))
         worst_e = max(worst_e, abs(e - ref[k][2]) / abs(ref[k][2]))
-        assert worst_p <= pop_tol, (k, worst_p)
+        assert worst_p <= POP_TOL, (k, worst_p)
         assert worst_e <= ENERGY_TOL, (k, worst_e)
     print(f"{case} {tr['stage']}: max population error {worst_p:.2e}, max relative energy error {worst_e:.2e}")
