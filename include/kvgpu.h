@@ -44,11 +44,11 @@ extern "C" {
 /* KV_FP64: every contraction in complex128 on the CUDA cores.
  * KV_MIXED_3M_DIGITS (the mixed-precision path): block contractions as 3M
  *   (Gauss) real products on the tcgen05 tensor cores.  Each operand is
- *   rounded to 30-bit fixed point against a per-row (A) or per-column (B)
- *   power of two and split into four balanced 8-bit digits, held exactly in
+ *   rounded to 38-bit fixed point against a per-row (A) or per-column (B)
+ *   power of two and split into five balanced 8-bit digits, held exactly in
  *   FP16; the digit products of orders 0-4 accumulate exactly in FP32 tensor
- *   memory and are combined in int64, so a product carries about 2^-29
- *   relative error per operand, below a TF32 or BF16x3 split.  Lanczos,
+ *   memory and are combined in int64, so a product carries about 1e-10
+ *   relative error, far below a TF32 or BF16x3 split.  Lanczos,
  *   norms, the tridiagonal exponential and MPO mixing stay FP64; the SVD
  *   picks the kept subspace in FP32 and rebuilds the kept factors in FP64
  *   (Cholesky-QR, exact projection).
