@@ -160,6 +160,13 @@ int kv_tdvp_create(int nsites, const kv_tensor *mps, const kv_tensor *mpo, doubl
  * built before that stage, so its next sweep mixes two states).  The global
  * step's contractions run in `precision`, its SVDs in FP64. */
 int kv_tdvp_sweep(kv_tdvp s, int mode);
+/* A window of TDVP::two_site's left-to-right pass (holstein/tdvp.h:150-185):
+ * the pass is advanced to site i0 (untimed; n = 0 does only that), then the
+ * n local updates at sites (i0, i0+1) ... (i0+n-1, i0+n) run and
+ * kv_tdvp_stats reports them as the last sweep.  For chains too long to sweep
+ * in a benchmark run; afterwards the handle is inside the pass and takes only
+ * further windows at later sites (kv_tdvp_sweep fails with KV_EINVAL). */
+int kv_tdvp_window(kv_tdvp s, int i0, int n);
 /* New handle with a copy of the current site tensor i. */
 int kv_tdvp_site(kv_tdvp s, int i, kv_tensor *out);
 /* Timings of the last one- or two-site sweep (a global-Krylov step leaves

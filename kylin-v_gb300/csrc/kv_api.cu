@@ -425,6 +425,14 @@ int kv_sweep_batched(int n_chains, const kv_tdvp *chains, int mode, int steps, i
     });
 }
 
+int kv_tdvp_window(kv_tdvp s, int i0, int n) {
+    return guard([&] {
+        kv::require_init();
+        KV_REQUIRE(s && s->s, KV_EINVAL, "null TDVP handle");
+        s->s->window(i0, n);
+    });
+}
+
 int kv_tdvp_site(kv_tdvp s, int i, kv_tensor *out) {
     return guard([&] {
         KV_REQUIRE(s && s->s && i >= 0 && i < (int)s->s->mps.size(), KV_EINVAL, "bad site index");

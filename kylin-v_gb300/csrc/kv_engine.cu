@@ -1278,6 +1278,7 @@ void Tdvp::init_envs() {
 // result that depends on the phases of singular vectors, i.e. on rounding);
 // here they are rebuilt from the new state.
 void Tdvp::global_krylov() {
+    KV_REQUIRE(window_at < 0, KV_EINVAL, "the chain is inside a timed window; it cannot sweep");
     std::vector<TensorP> Hc = mpo;
     Hc[0] = op_scale(*mpo[0], dt);
     global_main(Hc, mps, max_iter, tol_exp, tol_svd, max_dim, precision);
@@ -1379,6 +1380,7 @@ void Tdvp::end_sweep() {
 
 // TDVP::one_site (holstein/tdvp.h:78-141)
 void Tdvp::one_site() {
+    KV_REQUIRE(window_at < 0, KV_EINVAL, "the chain is inside a timed window; it cannot sweep");
     begin_sweep();
     const int ns = (int)mps.size();
     for (int i = 0; i < ns; ++i) {
@@ -1418,31 +1420,64 @@ void Tdvp::one_site() {
     end_sweep();
 }
 
+// one local update of TDVP::two_site's left-to-right pass at sites (i, i+1)
+// (holstein/tdvp.h:150-185)
+void Tdvp::two_site_lr(int i) {
+    const int ns = (int)mps.size();
+    mark(MOD_SWEEP, true);
+    TensorP mm = op_product(*mps[i], *mps[i + 1], 1, KV_OP_N, KV_OP_N, precision, &other);
+    mark(MOD_SWEEP, false);
+    mm = krylov(2, *envL.back(), *mm, mpo[i].get(), mpo[i + 1].get(), *envR.back(), false, MOD_EVL2);
+    mark(MOD_SVD, true);
+    SvdOut r = op_svd(*mm, 2, true, tol_svd, max_dim, precision);
+    mark(MOD_SVD, false);
+    if (i < ns - 2) {
+        mps[i] = r.U;
+        mark(MOD_UPDATE, true);
+        envL.push_back(op_env(true, *envL.back(), *mps[i], *mpo[i], nullptr, precision, &other));
+        mark(MOD_UPDATE, false);
+        mps[i + 1] = krylov(1, *envL.back(), *r.V, mpo[i + 1].get(), nullptr, *envR.back(), true, MOD_EVL1);
+        envR.pop_back();
+    } else {
+        mps[i] = r.U;
+        mps[i + 1] = r.V;
+    }
+}
+
+// A window of the two-site left-to-right pass: the pass is advanced (without
+// the sweep statistics) to site i0, then n local updates are run as one timed
+// "sweep" (module times, reference flops).  Chains too long to sweep in a
+// benchmark run are measured this way; afterwards the handle is inside the
+// pass and can only take further windows.
+void Tdvp::window(int i0, int n) {
+    const int ns = (int)mps.size();
+    KV_REQUIRE(n >= 0 && i0 >= 0 && i0 + n <= ns - 2, KV_EINVAL, "window outside the two-site pass");
+    if (window_at < 0) {
+        envR.pop_back();
+        window_at = 0;
+    }
+    KV_REQUIRE(i0 >= window_at, KV_EINVAL, "window behind the pass already advanced");
+    for (; window_at < i0; ++window_at) {
+        n_marks = 0;  // the advance keeps no statistics
+        n_krylov = 0;
+        krylov_flops.clear();
+        two_site_lr(window_at);
+    }
+    KV_CUDA(cudaStreamSynchronize(ctx().stream));
+    if (n == 0) return;
+    begin_sweep();
+    for (int i = i0; i < i0 + n; ++i) two_site_lr(i);
+    window_at = i0 + n;
+    end_sweep();
+}
+
 // TDVP::two_site (holstein/tdvp.h:144-227)
 void Tdvp::two_site() {
+    KV_REQUIRE(window_at < 0, KV_EINVAL, "the chain is inside a timed window; it cannot sweep");
     begin_sweep();
     const int ns = (int)mps.size();
     envR.pop_back();
-    for (int i = 0; i < ns - 1; ++i) {
-        mark(MOD_SWEEP, true);
-        TensorP mm = op_product(*mps[i], *mps[i + 1], 1, KV_OP_N, KV_OP_N, precision, &other);
-        mark(MOD_SWEEP, false);
-        mm = krylov(2, *envL.back(), *mm, mpo[i].get(), mpo[i + 1].get(), *envR.back(), false, MOD_EVL2);
-        mark(MOD_SVD, true);
-        SvdOut r = op_svd(*mm, 2, true, tol_svd, max_dim, precision);
-        mark(MOD_SVD, false);
-        if (i < ns - 2) {
-            mps[i] = r.U;
-            mark(MOD_UPDATE, true);
-            envL.push_back(op_env(true, *envL.back(), *mps[i], *mpo[i], nullptr, precision, &other));
-            mark(MOD_UPDATE, false);
-            mps[i + 1] = krylov(1, *envL.back(), *r.V, mpo[i + 1].get(), nullptr, *envR.back(), true, MOD_EVL1);
-            envR.pop_back();
-        } else {
-            mps[i] = r.U;
-            mps[i + 1] = r.V;
-        }
-    }
+    for (int i = 0; i < ns - 1; ++i) two_site_lr(i);
     for (int i = ns - 1; i > 0; --i) {
         mark(MOD_SWEEP, true);
         TensorP mm = op_product(*mps[i - 1], *mps[i], 1, KV_OP_N, KV_OP_N, precision, &other);

@@ -120,6 +120,10 @@ class Tdvp {
     ~Tdvp();
     void one_site();
     void two_site();
+    // n timed local updates of the two-site left-to-right pass from site i0
+    // (the pass advanced there first, untimed)
+    void window(int i0, int n);
+    int window_at = -1;  // site the two-site pass has reached in window mode (-1: none)
     // one step of total_start's global-Krylov stage, then the environments
     // rebuilt from the new state
     void global_krylov();
@@ -139,6 +143,7 @@ class Tdvp {
     double last_gemm_flops = 0.0;  // of which in product<> pairs (grouped GEMM)
 
   private:
+    void two_site_lr(int i);
     static constexpr int kStateSlots = 8192;
     static constexpr int kMaxEvents = 16384;
     TensorP krylov(int nsite, const DTensor &L, const DTensor &psi, const DTensor *W1, const DTensor *W2,

@@ -80,3 +80,96 @@ def fd_gradient(n_mol: int, cutoff: int, D: int, theta: dict, steps: int = 10, d
     return {"value": {"msd": float(msd[0]), "energy": float(energy[0])},
             "grad": {"msd": assemble(msd, h, names), "energy": assemble(energy, h, names)},
             "chains": len(ts), "device_ms": device_ms}
+
+
+# ------------------------------------------------------------ reverse mode
+def _energy_envs(mps_dev, W_dev, precision):
+    """Left environments of <psi|H|psi>: envs[0] the boundary, envs[s+1] =
+    env_sweep(envs[s], A_s, W_s) (holstein/product.h:505-521)."""
+    from .kvio import BlockTensor
+
+    envs = [G.Tensor.from_host(BlockTensor((1, -1, -1), [((0, 0, 0), np.ones((1, 1, 1), complex))]))]
+    for a, w in zip(mps_dev, W_dev):
+        envs.append(G.env_sweep(envs[-1], a, w, True, precision))
+    return envs
+
+
+def _energy_value(env_last):
+    """<psi|H|psi> from the final environment, as kv_expectation reads it."""
+    h = env_last.to_host()
+    if not h.blocks:
+        return 0.0, h
+    q = h.blocks[0][0][0]
+    return float(sum(a.ravel()[0].real for qn, a in h.blocks if a.size == 1 and qn == (q, 0, q))), h
+
+
+def energy_forward(chain: H.HolsteinChain, mps, names=PARAMS, precision: int = G.KV_FP64):
+    """E = <psi|H(theta)|psi> on the device, keeping what the reverse pass needs
+    (the left environments and the parameter-linear MPO)."""
+    W, dW = H.hamiltonian_mpo_param(chain, names)
+    A = [t if isinstance(t, G.Tensor) else G.Tensor.from_host(t) for t in mps]
+    Wd = [G.Tensor.from_host(w) for w in W]
+    envs = _energy_envs(A, Wd, precision)
+    e, last = _energy_value(envs[-1])
+    return e, {"A": A, "W": Wd, "dW": dW, "envs": envs, "last": last, "names": names, "precision": precision}
+
+
+def energy_backward(state) -> dict:
+    """dE/dtheta from energy_forward's state: from the cotangent 1 of E the
+    environment adjoints run backward (kv_adjoint_env), giving the cotangent
+    W_bar_s of every MPO site; dE/dtheta_k = sum_s Re<W_bar_s, dW_k[s]>."""
+    from .kvio import BlockTensor
+
+    last, names, dW = state["last"], state["names"], state["dW"]
+    q = last.blocks[0][0][0] if last.blocks else 0
+    ebar = G.Tensor.from_host(BlockTensor(last.dirs, [(qn, (np.ones_like(a) if (a.size == 1 and qn == (q, 0, q))
+                                                           else np.zeros_like(a))) for qn, a in last.blocks]))
+    grad = {k: 0.0 for k in names}
+    for s in reversed(range(len(state["A"]))):
+        out = G.adjoint_env(state["envs"][s], state["A"][s], state["W"][s], True, ebar, state["precision"],
+                            want=("env", "W"))
+        wbar = out["W"].to_host().as_dict()
+        for k in names:
+            for qn, d in dW[k][s].blocks:
+                b = wbar.get((tuple(qn), d.shape))
+                if b is not None:
+                    grad[k] += float(np.sum(np.conj(b) * d).real)
+        ebar = out["env"]
+    return grad
+
+
+def energy_gradient_adjoint(chain: H.HolsteinChain, mps, names=PARAMS, precision: int = G.KV_FP64) -> dict:
+    """E = <psi|H(theta)|psi> and dE/dtheta by reverse mode through the MPS
+    contraction (energy_forward, energy_backward): the environment adjoints of
+    kv_adjoint_env and the exact dW/dtheta of the parameter-linear MPO.
+
+    One-site TDVP without truncation conserves <H> exactly (up to the Krylov
+    tolerance), so this is also the gradient of <H> after any number of such
+    steps from the same state -- the differentiation workload's energy
+    quantity."""
+    e, state = energy_forward(chain, mps, names, precision)
+    return {"value": e, "grad": energy_backward(state)}
+
+
+def torch_energy(chain_of_theta, names=PARAMS, precision: int = G.KV_FP64):
+    """A torch.autograd.Function of theta (a float64 tensor, one entry per
+    name): forward E = <psi|H(theta)|psi> on the GPU library (energy_forward),
+    backward the reverse-mode pass (energy_backward) scaled by the incoming
+    gradient.  ``chain_of_theta(dict)`` builds the chain; call as
+    ``torch_energy(f, names).apply(theta, mps)``."""
+    import torch
+
+    class HolsteinEnergy(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, theta, mps):
+            th = {k: float(v) for k, v in zip(names, theta.detach().cpu().tolist())}
+            e, ctx.kv_state = energy_forward(chain_of_theta(th), mps, names, precision)
+            return torch.tensor(e, dtype=torch.float64)
+
+        @staticmethod
+        def backward(ctx, g):
+            grad = energy_backward(ctx.kv_state)
+            ctx.kv_state = None
+            return g * torch.tensor([grad[k] for k in names], dtype=torch.float64), None
+
+    return HolsteinEnergy

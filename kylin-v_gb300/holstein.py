@@ -165,18 +165,13 @@ def _dense_to_blocks(W: np.ndarray, lq: list, rq: list) -> BlockTensor:
     return BlockTensor(MPO_DIRS, blocks)
 
 
-def _fsm_mpo(chain: HolsteinChain, terms):
-    """Generic finite-state-machine MPO builder.
-
-    ``terms(site, type)`` yields (from_state, to_state, dense local operator);
-    states are named strings with a charge given by ``_STATE_Q``.  Unreachable
-    states (not reachable from 'I' at the left edge, or unable to reach 'F' at
-    the right edge) are pruned, then each site is cut into U(1) blocks."""
+def _fsm_live(chain: HolsteinChain, terms) -> list:
+    """Per bond, the FSM states reachable from 'I' at the left edge that can
+    still reach 'F' at the right edge, in (charge, name) order."""
     types = chain.site_types()
     dims = chain.site_dims()
     ns = len(types)
     trans = [list(terms(s, types[s], dims[s])) for s in range(ns)]
-    # forward reachability
     fwd = [set() for _ in range(ns + 1)]
     fwd[0] = {"I"}
     for s in range(ns):
@@ -189,60 +184,128 @@ def _fsm_mpo(chain: HolsteinChain, terms):
         for a, b, op in trans[s]:
             if b in bwd[s + 1] and np.any(op):
                 bwd[s].add(a)
-    live = [sorted(fwd[s] & bwd[s], key=lambda x: (_STATE_Q[x], _STATE_ORDER.index(x))) for s in range(ns + 1)]
-    sites = []
-    for s in range(ns):
-        L, R = live[s], live[s + 1]
-        W = np.zeros((dims[s], len(L), dims[s], len(R)))
-        for a, b, op in trans[s]:
-            if a in L and b in R:
-                W[:, L.index(a), :, R.index(b)] += op
-        sites.append(_dense_to_blocks(W, [_STATE_Q[x] for x in L], [_STATE_Q[x] for x in R]))
-    return sites
+    return [sorted(fwd[s] & bwd[s], key=lambda x: (_STATE_Q[x], _STATE_ORDER.index(x))) for s in range(ns + 1)]
+
+
+def _fsm_dense(chain: HolsteinChain, terms, live: list, s: int) -> np.ndarray:
+    """Site s of the FSM as a dense W[s_out, wl, s_in, wr] over the live states."""
+    t, d = chain.site_types()[s], chain.site_dims()[s]
+    L, R = live[s], live[s + 1]
+    W = np.zeros((d, len(L), d, len(R)))
+    for a, b, op in terms(s, t, d):
+        if a in L and b in R:
+            W[:, L.index(a), :, R.index(b)] += op
+    return W
+
+
+def _fsm_mpo(chain: HolsteinChain, terms):
+    """Generic finite-state-machine MPO builder.
+
+    ``terms(site, type)`` yields (from_state, to_state, dense local operator);
+    states are named strings with a charge given by ``_STATE_Q``.  Unreachable
+    states (not reachable from 'I' at the left edge, or unable to reach 'F' at
+    the right edge) are pruned, then each site is cut into U(1) blocks."""
+    live = _fsm_live(chain, terms)
+    return [_dense_to_blocks(_fsm_dense(chain, terms, live, s), [_STATE_Q[x] for x in live[s]],
+                             [_STATE_Q[x] for x in live[s + 1]]) for s in range(chain.n_sites)]
 
 
 _STATE_Q = {"I": 0, "F": 0, "N": 0, "Cp": 1, "Cm": -1, "Bp": 1, "Bm": -1}
 _STATE_ORDER = ["I", "N", "F", "Cp", "Bp", "Cm", "Bm"]
 
 
-def hamiltonian_mpo(chain: HolsteinChain) -> list:
-    """The full Holstein Hamiltonian as an MPO (list of BlockTensor)."""
+def _ham_terms(chain: HolsteinChain, coef):
+    """The Holstein Hamiltonian's FSM transitions.  ``coef(kind, value, mode)``
+    gives each transition's coefficient from its kind ("struct" for the
+    identity pass-throughs and the operator strings, "eps", "J", "omega", "g"),
+    its value in the Hamiltonian and, for omega and g, the mode index."""
     nm = chain.n_modes
 
     def terms(s, t, d):
         eye, bp, ap = _local_ops(d)
         bm, am = bp.T.copy(), ap.T.copy()
         n_e = np.diag([0.0, 1.0]) if d == 2 else None
+        one = coef("struct", 1.0, None)
         # hopping states pass through phonon/aux sites only: at the next exciton
         # site they must terminate (nearest-neighbour hopping)
         for st in ("I", "F") if t[0] == "e" else ("I", "F", "Cp", "Cm"):
-            yield st, st, eye
+            yield st, st, one * eye
         if t[0] == "e":
             i = t[1]
-            yield "I", "F", chain.eps[i] * n_e
+            yield "I", "F", coef("eps", chain.eps[i], None) * n_e
             if i + 1 < chain.n_mol:
-                yield "I", "Cp", bp  # c_i^+ (exciton: sqrt(1) = 1)
-                yield "I", "Cm", bm  # c_i
+                yield "I", "Cp", one * bp  # c_i^+ (exciton: sqrt(1) = 1)
+                yield "I", "Cm", one * bm  # c_i
             if i > 0:
-                yield "Cp", "F", chain.J * bm  # J c_{i-1}^+ c_i
-                yield "Cm", "F", chain.J * bp  # J c_i^+ c_{i-1}
+                yield "Cp", "F", coef("J", chain.J, None) * bm  # J c_{i-1}^+ c_i
+                yield "Cm", "F", coef("J", chain.J, None) * bp  # J c_i^+ c_{i-1}
             if nm > 0:
-                yield "I", "N", n_e
+                yield "I", "N", one * n_e
         elif t[0] == "v":
             i, k = t[1], t[2]
-            yield "I", "F", chain.omega[k] * (bp @ bm)
-            yield "N", "Bp", chain.g[i][k] * bp
-            yield "N", "Bm", chain.g[i][k] * bm
+            yield "I", "F", coef("omega", chain.omega[k], k) * (bp @ bm)
+            yield "N", "Bp", coef("g", chain.g[i][k], k) * bp
+            yield "N", "Bm", coef("g", chain.g[i][k], k) * bm
             if k + 1 < nm:
-                yield "N", "N", eye
+                yield "N", "N", one * eye
         else:  # aux site
-            i, k = t[1], t[2]
-            yield "Bp", "F", am
-            yield "Bm", "F", ap
+            k = t[2]
+            yield "Bp", "F", one * am
+            yield "Bm", "F", one * ap
             if k + 1 < nm:
-                yield "N", "N", eye
+                yield "N", "N", one * eye
 
-    return _fsm_mpo(chain, terms)
+    return terms
+
+
+def hamiltonian_mpo(chain: HolsteinChain) -> list:
+    """The full Holstein Hamiltonian as an MPO (list of BlockTensor)."""
+    return _fsm_mpo(chain, _ham_terms(chain, lambda kind, value, mode: value))
+
+
+def hamiltonian_mpo_param(chain: HolsteinChain, names=("J", "omega", "g", "eps")) -> tuple:
+    """The Hamiltonian as a parameter-linear MPO: (W, dW) with W the sites of
+    hamiltonian_mpo(chain) and dW[name][s] the exact derivative of site s with
+    respect to the parameter `name`, on the same block list as W[s] (zero
+    blocks where the site does not depend on it).
+
+    Every term of the Holstein Hamiltonian carries its coefficient on exactly
+    one site tensor (J on the exciton site that closes a hop, eps on the
+    exciton site, omega and g on the phonon site), so W_s is affine in the
+    parameters and H is linear in them: W(theta') = W(theta) +
+    sum_k (theta'_k - theta_k) dW_k, and dH/dtheta_k = sum_s (H with site s
+    replaced by dW_k[s]).  This is the reference's direct-sum construction of
+    H = sum_k theta_k H_k (Operator::operator+=, holstein/operator.h:54-70)
+    without its truncation, so dW/dtheta is exact.  Names: "J"; "eps" (every
+    molecule's site energy together); "omega" and "g" (every mode together)
+    or "omega_k" / "g_k" (mode k: its frequency, or its coupling on every
+    molecule)."""
+    ham = _ham_terms(chain, lambda kind, value, mode: value)
+    live = _fsm_live(chain, ham)
+    W = _fsm_mpo(chain, ham)
+    lq = [[_STATE_Q[x] for x in live[s]] for s in range(len(live))]
+    dW = {}
+    for name in names:
+        terms = _ham_terms(chain, lambda kind, value, mode, name=name:
+                           1.0 if (kind == name or (mode is not None and name == f"{kind}_{mode}")) else 0.0)
+        dW[name] = [_blocks_like(W[s], _fsm_dense(chain, terms, live, s), lq[s], lq[s + 1])
+                    for s in range(chain.n_sites)]
+    return W, dW
+
+
+def _blocks_like(template: BlockTensor, W: np.ndarray, lq: list, rq: list) -> BlockTensor:
+    """Blocks of the dense W[s_out, wl, s_in, wr] on exactly the block list of
+    `template` (same keys, order and shapes; zero blocks kept)."""
+    lsec, rsec = {}, {}
+    for idx, q in enumerate(lq):
+        lsec.setdefault(q, []).append(idx)
+    for idx, q in enumerate(rq):
+        rsec.setdefault(q, []).append(idx)
+    blocks = []
+    for (so, ql, si, qr), blk in template.blocks:
+        sub = W[so][np.ix_(lsec[ql], [si], rsec[qr])][:, 0, :]
+        blocks.append(((so, ql, si, qr), sub.reshape(blk.shape).astype(np.complex128)))
+    return BlockTensor(template.dirs, blocks)
 
 
 def density_mpo(chain: HolsteinChain, site: int) -> list:

@@ -32,7 +32,7 @@ EXPORTS = (
     "kv_svd_truncate", "kv_tdvp_create", "kv_tdvp_sweep", "kv_tdvp_site", "kv_tdvp_stats", "kv_tdvp_free",
     "kv_expectation", "kv_profile", "kv_profile_read", "kv_counters", "kv_expectation_noalloc",
     "kv_tdvp_host_stats", "kv_canonicalize", "kv_sweep_batched", "kv_adjoint_heff", "kv_adjoint_env",
-    "kv_debug_gemm_stall", "kv_debug_pool_usage", "kv_svd_stats",
+    "kv_debug_gemm_stall", "kv_debug_pool_usage", "kv_svd_stats", "kv_tdvp_window",
 )
 
 
@@ -72,6 +72,7 @@ def lib():
         L.kv_tdvp_create.argtypes = [ctypes.c_int, pvp, pvp, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                      ctypes.c_int, ctypes.c_double, ctypes.c_int, pvp]
         L.kv_tdvp_sweep.argtypes = [vp, ctypes.c_int]
+        L.kv_tdvp_window.argtypes = [vp, ctypes.c_int, ctypes.c_int]
         L.kv_tdvp_site.argtypes = [vp, ctypes.c_int, pvp]
         L.kv_tdvp_stats.argtypes = [vp, dp, dp, dp, dp]
         L.kv_tdvp_host_stats.argtypes = [vp, dp, dp, ctypes.POINTER(ctypes.c_longlong), dp]
@@ -327,6 +328,11 @@ class TDVP:
     def sweep(self, mode: int):
         """mode 0: global_krylov, 1: one_site, 2: two_site."""
         check(lib().kv_tdvp_sweep(self.ptr, mode))
+
+    def window(self, i0: int, n: int):
+        """n timed two-site local updates of the left-to-right pass from site
+        i0 (the pass is advanced there first, untimed)."""
+        check(lib().kv_tdvp_window(self.ptr, i0, n))
 
     def one_site(self):
         check(lib().kv_tdvp_sweep(self.ptr, 1))

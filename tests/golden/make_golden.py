@@ -67,6 +67,10 @@ def cases():
         # mixed path's population gate is checked against (too slow for the FP64 trajectory tests)
         "l32m3": dict(chain=HolsteinChain(3, [0.2, 1.2], [[0.5, 1.0]] * 3, cutoff=16), D=128, seed=1234,
                       ops_sites=[], traj=[("[0,20,0,0]", 128, 1e-8)], keep_inputs=False, mixed_only=True),
+        # the large single chain's local structure (4 modes: omega 0.1 / 0.4 / 0.9 / 1.5, g 0.3 / 0.6 /
+        # 0.8 / 1.0, cutoff 8, D = 512, SVD cutoff 1e-9) on 2 molecules (18 sites), 2 two-site steps
+        "l64m2": dict(chain=HolsteinChain(2, [0.1, 0.4, 0.9, 1.5], [[0.3, 0.6, 0.8, 1.0]] * 2, cutoff=8), D=512,
+                      seed=1234, ops_sites=[], traj=[("[0,2,0,0]", 512, 1e-9)], keep_inputs=False, mixed_only=True),
     }
 
 

@@ -5,7 +5,9 @@ every site population and step, and |dE(t)| <= 1e-6 |E|.
 
 l32m3 is the two-site benchmark's local structure (two modes with omega
 0.2 / 1.2 and g 0.5 / 1.0, cutoff 16, D = 128, SVD cutoff 1e-8) on three
-molecules, 20 two-site steps at dt = 0.05; l8c8d32 is the one-site benchmark
+molecules, 20 two-site steps at dt = 0.05; l64m2 the large single chain's
+(four modes, cutoff 8, D = 512, SVD cutoff 1e-9) on two molecules, two
+steps, with charge sectors up to 512 x 512; l8c8d32 is the one-site benchmark
 (L = 8, cutoff 8, D = 32, 20 steps); tiny1 / tiny2m are the small one- and
 two-site cases."""
 import os

@@ -87,6 +87,9 @@ def test_tdvp_trajectory_matches_reference(case, ti):
     dens = [H.density_mpo(ch, j) for j in ch.exciton_sites()]
     ident = H.identity_mpo(ch)
     ref = U.read_traj(f"{G}/{case}/{tr['file']}")
+    if ent["D"] >= 512:
+        pytest.skip("D = 512: minutes per step on the CPU; the trajectory comes from the compiled reference and the "
+                    "GPU gate test checks against it")
     t = O.Tdvp(mps, mpo, tr["tol_svd"], 1e-8, tr["maxD"], 11, 0.05)
     modes = U.stage_modes(tr["stage"])
     if ent.get("mixed_only"):
