@@ -380,7 +380,9 @@ def compare_fp64(args, G):
     from kylin_v_gb300 import holstein as H
 
     chain, D, d, mps, mpo = build_workload(args.config, 1234, n_mol=args.molecules)
-    dens = [[G.Tensor.from_host(x) for x in H.density_mpo(chain, j)] for j in chain.exciton_sites()]
+    # populations: every exciton site's density from one left and one right pass (kv_local_expectations)
+    ident = [G.Tensor.from_host(x) for x in H.identity_mpo(chain)]
+    dens = [(j, G.Tensor.from_host(H.density_mpo(chain, j)[j])) for j in chain.exciton_sites()]
     hm = [G.Tensor.from_host(x) for x in mpo]
     runs = {p: G.TDVP(mps, mpo, d["tol_svd"], d["tol_exp"], D, d["max_iter"], d["dt"], p)
             for p in (G.KV_FP64, G.KV_MIXED_TF32)}
@@ -398,7 +400,7 @@ def compare_fp64(args, G):
             for k, v in st["modules_ms"].items():
                 modules[p][k] = modules[p].get(k, 0.0) + v / nsteps
             s = t.sites()
-            obs[p] = (np.array([G.expectation(s, x, s).real for x in dens]), G.expectation(s, hm, s).real)
+            obs[p] = (np.array([v.real for v in G.local_expectations(s, ident, dens)]), G.expectation(s, hm, s).real)
         pe = float(np.abs(obs[G.KV_FP64][0] - obs[G.KV_MIXED_TF32][0]).max())
         per_step.append(float("%.3g" % pe))
         perr = max(perr, pe)

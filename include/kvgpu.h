@@ -241,6 +241,17 @@ int kv_canonicalize(int nsites, const kv_tensor *mps, double tol_svd, int max_di
 int kv_expectation(int nsites, const kv_tensor *bra, const kv_tensor *mpo, const kv_tensor *ket, double *re,
                    double *im);
 
+/* <psi|O_k|psi> for nops operators that are the identity except on one site
+ * each: Operator::join (holstein/operator.h:178-198) with the MPO that has
+ * op_tensor[k] (a bond-dimension-1 MPO tensor, e.g. the site's exciton
+ * density of Op/Density_j) on site op_site[k] and ident_mpo elsewhere (the
+ * identity MPO's tensors, one per site).  The identity environments are built
+ * once from each end, then each operator costs one environment update: all
+ * site populations of a chain in about three passes.  The reference runs one
+ * kln-join process per observable and step. */
+int kv_local_expectations(int nsites, const kv_tensor *mps, const kv_tensor *ident_mpo, int nops, const int *op_site,
+                          const kv_tensor *op_tensor, double *re, double *im);
+
 /* The same value as kv_expectation without allocating any GPU memory; it has
  * no counterpart in the reference.  For callers that cannot let a library
  * call cudaMalloc: applications that own all device memory through their own

@@ -562,6 +562,27 @@ int kv_expectation(int nsites, const kv_tensor *bra, const kv_tensor *mpo, const
     });
 }
 
+int kv_local_expectations(int nsites, const kv_tensor *mps, const kv_tensor *ident_mpo, int nops, const int *op_site,
+                          const kv_tensor *op_tensor, double *re, double *im) {
+    return guard([&] {
+        kv::require_init();
+        KV_REQUIRE(nsites >= 1 && nops >= 0 && mps && ident_mpo && (nops == 0 || (op_site && op_tensor && re && im)),
+                   KV_EINVAL, "null argument");
+        std::vector<kv::DTensor *> a, w, o;
+        for (int i = 0; i < nsites; ++i) {
+            a.push_back(T(mps[i]));
+            w.push_back(T(ident_mpo[i]));
+        }
+        std::vector<int> sites(op_site, op_site + nops);
+        for (int k = 0; k < nops; ++k) o.push_back(T(op_tensor[k]));
+        std::vector<kv::cplx> r = kv::op_local_expectations(a, w, sites, o);
+        for (int k = 0; k < nops; ++k) {
+            re[k] = r[k].real();
+            im[k] = r[k].imag();
+        }
+    });
+}
+
 int kv_expectation_noalloc(int nsites, const kv_tensor *bra, const kv_tensor *mpo, const kv_tensor *ket, double *re,
                            double *im) {
     return guard([&] {

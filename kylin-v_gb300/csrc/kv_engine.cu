@@ -1523,6 +1523,56 @@ std::vector<TensorP> op_canonicalize(const std::vector<TensorP> &in, double tol,
     return t;
 }
 
+// sum_k E[k] R[k] over the blocks of two environments of one bond that carry
+// the same (shape, charges): the value of <a|O|b> where the left part's
+// environment E meets the right part's R
+static cplx env_meet(const DTensor &E, const DTensor &R) {
+    std::vector<double2> he(std::max<int64_t>(1, E.meta.nelem)), hr(std::max<int64_t>(1, R.meta.nelem));
+    if (E.meta.nelem)
+        KV_CUDA(cudaMemcpyAsync(he.data(), E.data(), E.meta.nelem * sizeof(double2), cudaMemcpyDeviceToHost,
+                                ctx().stream));
+    if (R.meta.nelem)
+        KV_CUDA(cudaMemcpyAsync(hr.data(), R.data(), R.meta.nelem * sizeof(double2), cudaMemcpyDeviceToHost,
+                                ctx().stream));
+    KV_CUDA(cudaStreamSynchronize(ctx().stream));
+    cplx v = 0.0;
+    for (auto &b : E.meta.blocks) {
+        const int k = R.meta.find(b);
+        if (k < 0) continue;
+        const BlockMeta &r = R.meta.blocks[k];
+        for (int64_t i = 0; i < b.size; ++i)
+            v += cplx(he[b.off + i].x, he[b.off + i].y) * cplx(hr[r.off + i].x, hr[r.off + i].y);
+    }
+    return v;
+}
+
+// <psi|O_k|psi> for operators O_k that are the identity except on one site
+// (Operator::join, holstein/operator.h:178-198, with such an MPO): the
+// identity environments from the left (L_s) and from the right (R_s) are
+// built once, then each operator costs one environment update at its site,
+// E = env_sweep(L_s, A_s, O_k), met with R_{s+1} -- all site populations of a
+// chain in about three passes instead of one full contraction each.
+std::vector<cplx> op_local_expectations(const std::vector<DTensor *> &mps, const std::vector<DTensor *> &ident,
+                                        const std::vector<int> &op_site, const std::vector<DTensor *> &op) {
+    const int ns = (int)mps.size();
+    KV_REQUIRE(ns >= 1 && (int)ident.size() == ns, KV_EINVAL, "one identity MPO tensor per site is required");
+    KV_REQUIRE(op_site.size() == op.size(), KV_EINVAL, "one site per local operator");
+    for (int s : op_site) KV_REQUIRE(s >= 0 && s < ns, KV_EINVAL, "local operator site out of range");
+    KV_REQUIRE(!mps.back()->meta.blocks.empty(), KV_EINVAL, "empty last site tensor");
+    std::vector<TensorP> L(ns + 1), R(ns + 1);
+    L[0] = boundary_env(1, 0);
+    for (int s = 0; s < ns; ++s) L[s + 1] = op_env(true, *L[s], *mps[s], *ident[s], nullptr, KV_FP64, nullptr);
+    R[ns] = boundary_env(-1, mps[ns - 1]->meta.blocks[0].qn[2]);
+    for (int s = ns - 1; s >= 0; --s) R[s] = op_env(false, *R[s + 1], *mps[s], *ident[s], nullptr, KV_FP64, nullptr);
+    std::vector<cplx> out;
+    for (size_t k = 0; k < op.size(); ++k) {
+        const int s = op_site[k];
+        TensorP E = op_env(true, *L[s], *mps[s], *op[k], nullptr, KV_FP64, nullptr);
+        out.push_back(env_meet(*E, *R[s + 1]));
+    }
+    return out;
+}
+
 // Operator::join (holstein/operator.h:178-198)
 cplx op_expectation(const std::vector<DTensor *> &a, const std::vector<DTensor *> &w, const std::vector<DTensor *> &b) {
     TensorP env = boundary_env(1, 0);

@@ -92,6 +92,10 @@ void global_main(const std::vector<TensorP> &Hc, std::vector<TensorP> &mps, int 
                  double tol_svd, int maxd, int precision);
 std::vector<TensorP> op_canonicalize(const std::vector<TensorP> &in, double tol, int max_dim, int precision);
 cplx op_expectation(const std::vector<DTensor *> &a, const std::vector<DTensor *> &w, const std::vector<DTensor *> &b);
+// <psi|O_k|psi> for operators that are the identity except on site op_site[k]
+// (its MPO tensor op[k]); ident: the identity MPO's tensors
+std::vector<cplx> op_local_expectations(const std::vector<DTensor *> &mps, const std::vector<DTensor *> &ident,
+                                        const std::vector<int> &op_site, const std::vector<DTensor *> &op);
 // the same value with all device scratch in a fixed static array (kv_noalloc.cu)
 cplx expectation_noalloc(const std::vector<DTensor *> &bra, const std::vector<DTensor *> &w,
                          const std::vector<DTensor *> &ket);

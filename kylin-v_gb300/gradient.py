@@ -63,7 +63,8 @@ def fd_gradient(n_mol: int, cutoff: int, D: int, theta: dict, steps: int = 10, d
     chains = [holstein_chain(n_mol, cutoff, p) for p in pts]
     mps = [G.Tensor.from_host(x) for x in H.random_mps(chains[0], D, seed=seed)]
     mpos = [[G.Tensor.from_host(x) for x in H.hamiltonian_mpo(c)] for c in chains]
-    dens = [[G.Tensor.from_host(x) for x in H.density_mpo(chains[0], j)] for j in chains[0].exciton_sites()]
+    ident = [G.Tensor.from_host(x) for x in H.identity_mpo(chains[0])]
+    dens = [(j, G.Tensor.from_host(H.density_mpo(chains[0], j)[j])) for j in chains[0].exciton_sites()]
     ts = [G.TDVP(mps, w, 0.0, tol_exp, D, max_iter, dt, precision) for w in mpos]
     msd = np.zeros(len(ts))
     weights = np.arange(len(dens), dtype=float)
@@ -72,7 +73,7 @@ def fd_gradient(n_mol: int, cutoff: int, D: int, theta: dict, steps: int = 10, d
         device_ms += G.sweep_batched(ts, 1, 1, max_streams)
         for c, t in enumerate(ts):
             s = t.sites()
-            msd[c] += float(np.dot(weights, [G.expectation(s, d, s).real for d in dens]))
+            msd[c] += float(np.dot(weights, [v.real for v in G.local_expectations(s, ident, dens)]))
     energy = np.zeros(len(ts))
     for c, t in enumerate(ts):
         s = t.sites()

@@ -32,7 +32,7 @@ EXPORTS = (
     "kv_svd_truncate", "kv_tdvp_create", "kv_tdvp_sweep", "kv_tdvp_site", "kv_tdvp_stats", "kv_tdvp_free",
     "kv_expectation", "kv_profile", "kv_profile_read", "kv_counters", "kv_expectation_noalloc",
     "kv_tdvp_host_stats", "kv_canonicalize", "kv_sweep_batched", "kv_adjoint_heff", "kv_adjoint_env",
-    "kv_debug_gemm_stall", "kv_debug_pool_usage", "kv_svd_stats", "kv_tdvp_window",
+    "kv_debug_gemm_stall", "kv_debug_pool_usage", "kv_svd_stats", "kv_tdvp_window", "kv_local_expectations",
 )
 
 
@@ -83,6 +83,7 @@ def lib():
         L.kv_expectation.argtypes = [ctypes.c_int, pvp, pvp, pvp, dp, dp]
         L.kv_canonicalize.argtypes = [ctypes.c_int, pvp, ctypes.c_double, ctypes.c_int, ctypes.c_int, pvp]
         L.kv_expectation_noalloc.argtypes = [ctypes.c_int, pvp, pvp, pvp, dp, dp]
+        L.kv_local_expectations.argtypes = [ctypes.c_int, pvp, pvp, ctypes.c_int, ip, pvp, dp, dp]
         L.kv_sweep_batched.argtypes = [ctypes.c_int, pvp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
         L.kv_adjoint_heff.argtypes = [ctypes.c_int, vp, vp, vp, vp, vp, ctypes.c_double, vp, ctypes.c_int,
                                       pvp, pvp, pvp, pvp, pvp]
@@ -292,6 +293,20 @@ def launches() -> int:
     n = ctypes.c_longlong()
     check(lib().kv_counters(ctypes.byref(n)))
     return n.value
+
+
+def local_expectations(mps, ident_mpo, ops) -> list:
+    """<psi|O|psi> for each (site, MPO tensor) in ops, O the identity elsewhere
+    (kv_local_expectations): all from one left and one right pass."""
+    ms = [_t(x) for x in mps]
+    ws = [_t(x) for x in ident_mpo]
+    os_ = [_t(t) for _, t in ops]
+    ns, no = len(ms), len(ops)
+    arr = lambda hs: (ctypes.c_void_p * max(1, len(hs)))(*[h.ptr for h in hs])  # noqa: E731
+    sites = (ctypes.c_int * max(1, no))(*[s for s, _ in ops])
+    re, im = (ctypes.c_double * max(1, no))(), (ctypes.c_double * max(1, no))()
+    check(lib().kv_local_expectations(ns, arr(ms), arr(ws), no, sites, arr(os_), re, im))
+    return [complex(re[k], im[k]) for k in range(no)]
 
 
 def expectation_noalloc(bra, mpo, ket) -> complex:
