@@ -944,20 +944,22 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
     // singular vectors of the other side,
     //   L->R: X = A_s V S^-1   R->L: X = A_s^H U S^-1,
     // over each sector's FP32-kept columns plus the candidates within 10%
-    // below the cutoff.  The first Cholesky-QR pass is a Gram-Schmidt in
-    // descending order: s_j R_jj is column j's singular value with the FP32
-    // error along the larger columns projected out, accurate to FP64 where
-    // the FP32 value is not (its error is ~1e-7 of the sector's largest).
-    // The truncation is redone with those values so the kept set is the one
-    // FP64 values select; the kept columns are a prefix of the pass-1 basis.
+    // below the cutoff.  The columns of X are orthonormal up to the FP32
+    // error of W, so s_j |x_j| is column j's singular value with that error
+    // entering only at second order -- accurate to FP64 where the FP32 value
+    // is not (its error is ~1e-7 of the sector's largest).  The truncation is
+    // redone with those values; the kept columns are a prefix of X.
     const int side = l2r ? 0 : 1;  // which factor is kept orthonormal
     std::vector<int> kc(nsec, 0);  // columns rebuilt per sector
     std::vector<SvdPolish> pol;
     std::vector<int> pol_of_sector(nsec, -1);
     DevBuf X, Gm, Wb, cst, cdiag;
-    const int tm = kTileM(KV_FP64), tn = kTileN(KV_FP64);
+    // the rebuild's FP64 products are small: 16 x 16 tiles spread them over more SMs
+    const int tm = 16, tn = 16;
     auto add_gemm = [&](GemmPlan &g, int64_t c_off, int M, int N, GemmSeg seg) {
         const int sb = (int)g.segs.size();
+        g.tile_m = tm;
+        g.tile_n = tn;
         g.segs.push_back(seg);
         for (int m0 = 0; m0 < M; m0 += tm)
             for (int n0 = 0; n0 < N; n0 += tn) g.tiles.push_back({c_off, N, M, N, m0, n0, sb, sb + 1});
@@ -1020,21 +1022,21 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
         }
         build.upload();
         launch_gemm_fp64(build, T.as<double2>(), Wb.as<double2>(), X.as<double2>(), 1.0, nullptr);
-        // pass 1 (a 1e-14 relative shift keeps it defined; the span never changes)
-        polish_pass(pol, dpol, 1e-14);
-        // R's diagonals: refined singular values of the rebuilt columns
+        // refined singular values: x_j = A w_j / s~_j, so s_j = s~_j |x_j|.  W's
+        // FP32 error enters |A w_j| only at second order (the columns of X are
+        // orthogonal to that order), which is what the truncation needs.
+        svd_col_norm2(dpol, (int)pol.size(), X.as<double2>(), Gm.as<double2>());
         std::vector<std::vector<double2>> diag(pol.size());
         for (size_t i = 0; i < pol.size(); ++i) {
             diag[i].resize(pol[i].k);
-            KV_CUDA(cudaMemcpy2DAsync(diag[i].data(), sizeof(double2), Gm.as<double2>() + pol[i].g_off,
-                                      (size_t)(pol[i].k + 1) * sizeof(double2), sizeof(double2), pol[i].k,
-                                      cudaMemcpyDeviceToHost, ctx().stream));
+            KV_CUDA(cudaMemcpyAsync(diag[i].data(), Gm.as<double2>() + pol[i].g_off, pol[i].k * sizeof(double2),
+                                    cudaMemcpyDeviceToHost, ctx().stream));
         }
         KV_CUDA(cudaStreamSynchronize(ctx().stream));
         std::vector<double> svr = sv;
         for (size_t i = 0; i < pol.size(); ++i) {
             const SvdSector &sc = P.secs[pol[i].sector];
-            for (int j = 0; j < pol[i].k; ++j) svr[sc.s_off + j] = sv[sc.s_off + j] * std::fabs(diag[i][j].x);
+            for (int j = 0; j < pol[i].k; ++j) svr[sc.s_off + j] = sv[sc.s_off + j] * std::sqrt(diag[i][j].x);
         }
         out.kept_s.clear();
         kfin = truncate(svr, nullptr, nullptr);
@@ -1093,11 +1095,12 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
         svd_scatter(svs, P, Us.as<double2>(), Vs.as<double2>(), S.as<double>(), out.V->data());
         return out;
     }
-    // ---- mixed mode, part 2: the kept prefix of each sector's pass-1 basis
-    // (X keeps its row stride kc), a second Cholesky-QR pass for FP64
-    // orthonormality, and the other factor as the exact projection
-    // (Y = X^H A_s, or A_s X).  With no truncation the factorisation is exact
-    // to FP64 rounding; the FP32 error only enters the choice of directions.
+    // ---- mixed mode, part 2: the kept prefix of each sector's X (row stride
+    // kc), one Cholesky-QR pass for FP64 orthonormality (X's condition number
+    // is 1 up to the FP32 error of W, so one pass reaches FP64 rounding), and
+    // the other factor as the exact projection (Y = X^H A_s, or A_s X).  With
+    // no truncation the factorisation is exact to FP64 rounding; the FP32
+    // error only enters the choice of directions.
     std::vector<SvdPolish> pol2;
     std::vector<int> pol2_of_sector(nsec, -1);
     std::vector<int64_t> y_off(nsec, 0);

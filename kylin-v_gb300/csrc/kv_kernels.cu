@@ -17,22 +17,29 @@ __device__ __forceinline__ void cfma(double2 &acc, double2 a, double2 b) {
 }
 
 // ------------------------------------------------------------------ GEMM
-// One CTA per output tile (32 x 32 complex), 256 threads, 2 x 2 per thread.
-// Each tile sums all block pairs (segments) that accumulate into it, so no
-// atomics are needed and the summation order is fixed.
-constexpr int TM = 32, TN = 32, TK = 16;
+// One CTA per output tile (T x T complex, T = 32 or 16), 256 threads,
+// (T/16) x (T/16) outputs per thread.  Each tile sums all block pairs
+// (segments) that accumulate into it, so no atomics are needed and the
+// summation order is fixed.  GB300 runs FP64 at a few multiply-adds per clock
+// per SM, so a tile's K loop is long in time: the 16 x 16 tiles put four
+// times as many CTAs (SMs) on the same product, for the small products of the
+// SVD's FP64 rebuild.
+constexpr int TK = 16;
 
+template <int T>
 __global__ void __launch_bounds__(256) k_gemm_fp64(const GemmTile *__restrict__ tiles,
                                                    const GemmSeg *__restrict__ segs,
                                                    const double2 *__restrict__ A,
                                                    const double2 *__restrict__ B, double2 *__restrict__ C,
                                                    double alpha, const int *skip, int step, int write_inactive) {
     if (skip && *skip) return;
+    constexpr int TM = T, TN = T, R = T / 16;  // R x R outputs per thread
+    constexpr int LOADS = (TM * TK + 255) / 256;
     __shared__ double2 As[TK][TM + 1];
     __shared__ double2 Bs[TK][TN + 1];
     const GemmTile t = tiles[blockIdx.x];
     const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
-    double2 acc[2][2] = {};
+    double2 acc[R][R] = {};
     bool any = false;
     for (int s = t.seg_begin; s < t.seg_end; ++s) {
         const GemmSeg g = segs[s];
@@ -42,7 +49,7 @@ __global__ void __launch_bounds__(256) k_gemm_fp64(const GemmTile *__restrict__ 
         const double2 *b = B + g.b_off;
         for (int k0 = 0; k0 < g.K; k0 += TK) {
 #pragma unroll
-            for (int r = 0; r < 2; ++r) {
+            for (int r = 0; r < LOADS; ++r) {
                 int idx = tid + r * 256;
                 int m, k;
                 const bool a_kc = (g.opa == 0 || g.opa == 3);  // contiguous along k
@@ -71,22 +78,26 @@ __global__ void __launch_bounds__(256) k_gemm_fp64(const GemmTile *__restrict__ 
             __syncthreads();
 #pragma unroll
             for (int kk = 0; kk < TK; ++kk) {
-                double2 a0 = As[kk][ty * 2], a1 = As[kk][ty * 2 + 1];
-                double2 b0 = Bs[kk][tx * 2], b1 = Bs[kk][tx * 2 + 1];
-                cfma(acc[0][0], a0, b0);
-                cfma(acc[0][1], a0, b1);
-                cfma(acc[1][0], a1, b0);
-                cfma(acc[1][1], a1, b1);
+                double2 a[R], b[R];
+#pragma unroll
+                for (int i = 0; i < R; ++i) {
+                    a[i] = As[kk][ty * R + i];
+                    b[i] = Bs[kk][tx * R + i];
+                }
+#pragma unroll
+                for (int i = 0; i < R; ++i)
+#pragma unroll
+                    for (int j = 0; j < R; ++j) cfma(acc[i][j], a[i], b[j]);
             }
             __syncthreads();
         }
     }
     if (!any && !write_inactive) return;
 #pragma unroll
-    for (int i = 0; i < 2; ++i)
+    for (int i = 0; i < R; ++i)
 #pragma unroll
-        for (int j = 0; j < 2; ++j) {
-            int gm = t.m0 + ty * 2 + i, gn = t.n0 + tx * 2 + j;
+        for (int j = 0; j < R; ++j) {
+            int gm = t.m0 + ty * R + i, gn = t.n0 + tx * R + j;
             if (gm < t.M && gn < t.N)
                 C[t.c_off + (int64_t)gm * t.ldc + gn] = make_double2(alpha * acc[i][j].x, alpha * acc[i][j].y);
         }
@@ -171,8 +182,14 @@ int grid_for(int64_t n, int threads) {
 void launch_gemm_fp64(const GemmPlan &p, const double2 *A, const double2 *B, double2 *C, double alpha,
                       const int *skip, int step) {
     if (p.tiles.empty()) return;
-    k_gemm_fp64<<<(unsigned)p.tiles.size(), 256, 0, ctx().stream>>>(
-        p.d_tiles.as<GemmTile>(), p.d_segs.as<GemmSeg>(), A, B, C, alpha, skip, step, p.write_inactive ? 1 : 0);
+    KV_REQUIRE(p.tile_m == p.tile_n && (p.tile_m == 32 || p.tile_m == 16 || p.tile_m == 0), KV_EINVAL,
+               "internal: FP64 GEMM tiles are 32 x 32 or 16 x 16");
+    if (p.tile_m == 16)
+        k_gemm_fp64<16><<<(unsigned)p.tiles.size(), 256, 0, ctx().stream>>>(
+            p.d_tiles.as<GemmTile>(), p.d_segs.as<GemmSeg>(), A, B, C, alpha, skip, step, p.write_inactive ? 1 : 0);
+    else
+        k_gemm_fp64<32><<<(unsigned)p.tiles.size(), 256, 0, ctx().stream>>>(
+            p.d_tiles.as<GemmTile>(), p.d_segs.as<GemmSeg>(), A, B, C, alpha, skip, step, p.write_inactive ? 1 : 0);
     counted();
     KV_CUDA(cudaGetLastError());
 }

@@ -681,6 +681,22 @@ __global__ void k_svd_extract(const SvdPolish *__restrict__ pol, const SvdSector
     }
 }
 
+// Squared norms of the columns of each polish factor X (rows x k, row stride
+// ldx), written as G[g_off + j].x: one CTA per factor, one warp per column.
+__global__ void k_col_norm2(const SvdPolish *__restrict__ pol, const double2 *__restrict__ X, double2 *__restrict__ G) {
+    const SvdPolish d = pol[blockIdx.x];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int j = warp; j < d.k; j += nw) {
+        double a = 0.0;
+        for (int i = lane; i < d.rows; i += 32) {
+            const double2 v = X[d.x_off + (int64_t)i * d.ldx + j];
+            a += v.x * v.x + v.y * v.y;
+        }
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xFFFFFFFFu, a, o);
+        if (lane == 0) G[d.g_off + j] = make_double2(a, 0.0);
+    }
+}
+
 // In place: G (k x k, row-major, Hermitian positive definite) -> upper R with
 // G = R^H R (lower triangle left as is).  One CTA per sector, column-wise.
 __global__ void k_chol(const SvdPolish *__restrict__ pol, double2 *__restrict__ G, int *status, double *diagv,
@@ -977,6 +993,13 @@ void svd_finalize_f32(const SvdPlan &p, const float2 *T, float2 *Us, double *S) 
 void svd_extract(const DevBuf &pol, int npol, const SvdPlan &p, const float2 *Us, const double *S, double2 *W) {
     if (npol == 0) return;
     k_svd_extract<<<npol, 256, 0, ctx().stream>>>(pol.as<SvdPolish>(), p.d_secs.as<SvdSector>(), Us, S, W);
+    counted();
+    KV_CUDA(cudaGetLastError());
+}
+
+void svd_col_norm2(const DevBuf &pol, int npol, const double2 *X, double2 *G) {
+    if (npol == 0) return;
+    k_col_norm2<<<npol, 256, 0, ctx().stream>>>(pol.as<SvdPolish>(), X, G);
     counted();
     KV_CUDA(cudaGetLastError());
 }

@@ -66,6 +66,8 @@ bool svd_qrjacobi_f32(const SvdPlan &p, const double2 *T64, float2 *Us, double *
 void svd_extract(const DevBuf &pol, int npol, const SvdPlan &p, const float2 *Us, const double *S, double2 *W);
 // rows of X per triangular-solve CTA (one warp per row)
 constexpr int kTrsmRows = 8;
+// squared column norms of each polish factor X into G[g_off + j].x
+void svd_col_norm2(const DevBuf &pol, int npol, const double2 *X, double2 *G);
 void svd_chol(const DevBuf &pol, int npol, double2 *G, int *status, double *diagv, double shift);
 void svd_trsm(const DevBuf &pol, const std::vector<int> &item_pol, const std::vector<int> &item_row0,
               const double2 *G, double2 *X, int kmax);
