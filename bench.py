@@ -262,6 +262,7 @@ def run_ours(args):
     barrier()
     n0 = G.launches()
     G.svd_stats(reset=True)
+    G.krylov_stats(reset=True)
     G.profile(True)
     with Clocks(local) as clk:
         for _ in range(args.steps):
@@ -285,6 +286,7 @@ def run_ours(args):
     G.profile(False)
     launches = G.launches() - n0
     svd = G.svd_stats(reset=True)
+    kry = G.krylov_stats(reset=True)
     clocks = clk.summary()
     tot_flops, max_ms = flops, dev_ms
     if ws > 1:
@@ -358,6 +360,9 @@ def run_ours(args):
         "svd_sectors": {"per_step": svd["sectors"] / args.steps, "mean_columns": svd["mean_columns"],
                         "mean_rank": svd["mean_rank"], "mean_jacobi_sweeps": svd["mean_sweeps"],
                         "max_jacobi_sweeps": svd["max_sweeps"]},
+        "krylov": {"calls_per_step": kry["calls"] / args.steps, "iterations_issued_per_call": kry["issued_per_call"],
+                   "mean_dimension": kry["mean_dimension"]},
+        "gpu_launches_per_step": launches / args.steps,
     }
     if not args.no_compare:
         line["fp64_compare"] = compare_fp64(args, G)

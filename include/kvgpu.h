@@ -218,6 +218,12 @@ int kv_counters(long long *launches);
  * counterpart. */
 int kv_svd_stats(int reset, long long *sectors, long long *columns, long long *rank, long long *sweeps,
                  int *max_sweeps);
+/* local_krylov calls on the calling thread's stream since kv_init (or the
+ * last reset), the Lanczos iterations issued for them, and the Krylov
+ * dimensions they reached.  The host stops issuing iterations two behind the
+ * device's stop test, so issued - used stays at most 2 per call.  reset != 0
+ * clears the counters after reading them.  No reference counterpart. */
+int kv_krylov_stats(int reset, long long *calls, long long *issued, long long *used);
 /* Test hook for the failure path of the tensor-core GEMM; no reference
  * counterpart.  kv_debug_gemm_stall(1): until called with 0, every
  * tensor-core GEMM issues no operand copies and gives up each wait after a

@@ -101,6 +101,10 @@ void context_open(Context &c, int device) {
     KV_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
     KV_CUDA(cudaHostAlloc((void **)&c.ring, (size_t)Context::kRingChunks * Context::kRingChunk, cudaHostAllocDefault));
     for (auto &e : c.ring_ev) KV_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    KV_CUDA(cudaHostAlloc((void **)&c.stop_host, sizeof(int), cudaHostAllocMapped));
+    *c.stop_host = 0;
+    KV_CUDA(cudaHostGetDevicePointer((void **)&c.stop_dev, c.stop_host, 0));
+    for (auto &e : c.iter_ev) KV_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     c.device = device;
 }
 
@@ -114,6 +118,9 @@ void context_close(Context &c) {
     for (auto &e : c.ring_ev) cudaEventDestroy(e);
     cudaFreeHost(c.ring);
     c.ring = nullptr;
+    for (auto &e : c.iter_ev) cudaEventDestroy(e);
+    cudaFreeHost(c.stop_host);
+    c.stop_host = c.stop_dev = nullptr;
     for (auto &e : c.ev_free) cudaEventDestroy(e);
     c.ev_free.clear();
     KV_CUDA(cudaStreamSynchronize(c.stream));
@@ -503,6 +510,17 @@ int kv_svd_stats(int reset, long long *sectors, long long *columns, long long *r
         if (sweeps) *sweeps = v.sweeps;
         if (max_sweeps) *max_sweeps = v.max_sweeps;
         if (reset) v = kv::Context::SvdStats{};
+    });
+}
+
+int kv_krylov_stats(int reset, long long *calls, long long *issued, long long *used) {
+    return guard([&] {
+        kv::require_init();
+        auto &c = kv::ctx();
+        if (calls) *calls = c.krylov_calls;
+        if (issued) *issued = c.krylov_issued;
+        if (used) *used = c.krylov_used;
+        if (reset) c.krylov_calls = c.krylov_issued = c.krylov_used = 0;
     });
 }
 

@@ -732,12 +732,29 @@ TensorP op_lanczos(int nsite, const DTensor &L, const DTensor &psi, const DTenso
     double2 *V = Vbuf.as<double2>();
     // psi's blocks are the layout's first blocks at the same offsets (both laid out in block order)
     KV_REQUIRE(psi.meta.nelem == nl.n[0], KV_EINVAL, "internal: Krylov layout does not start with psi");
-    krylov_start(st_dev, psi.data(), V, nl.n[0], parts.as<double2>());
+    // The iterations are issued ahead of the device, and every kernel of an
+    // iteration past the stop returns at once (skip).  Before issuing
+    // iteration k the host waits for iteration k - kStopLag to finish and
+    // stops if the recurrence had stopped by then, so at most kStopLag
+    // iterations are issued in vain while the device stays kStopLag - 1
+    // iterations ahead of the host.  No kernel of this context is running
+    // here (the previous call on it synchronised), so the flag can be reset.
+    constexpr int kStopLag = 2;
+    Context &c = ctx();
+    *reinterpret_cast<volatile int *>(c.stop_host) = 0;
+    krylov_start(st_dev, psi.data(), V, nl.n[0], parts.as<double2>(), c.stop_dev);
     const int *skip = &st_dev->done;
+    ++c.krylov_calls;
     for (int k = 0; k < max_iter - 1; ++k) {
+        if (k >= kStopLag) {
+            KV_CUDA(cudaEventSynchronize(c.iter_ev[k - kStopLag]));
+            if (*reinterpret_cast<volatile int *>(c.stop_host)) break;
+        }
         run_heff(H, w, L, V + voff[k], W1, W2, R, hv.as<double2>(), dt * 0.5, precision, skip, st_dev, k);
         krylov_step(st_dev, k, hv.as<double2>(), k > 0 ? V + voff[k - 1] : nullptr, V + voff[k], V + voff[k + 1], nl,
-                    parts.as<double2>(), tol, max_iter);
+                    parts.as<double2>(), tol, max_iter, c.stop_dev);
+        KV_CUDA(cudaEventRecord(c.iter_ev[k], c.stream));
+        ++c.krylov_issued;
     }
     std::vector<double2 *> ptrs(nvec);
     for (int i = 0; i < nvec; ++i) ptrs[i] = V + voff[i];
@@ -758,6 +775,7 @@ TensorP op_lanczos(int nsite, const DTensor &L, const DTensor &psi, const DTenso
     out->meta.layout();
     KV_REQUIRE(out->meta.nelem == keep, KV_EINVAL, "internal: Krylov prefix is not block aligned");
     if (iters_out) *iters_out = h.iters;
+    c.krylov_used += h.iters;
     return out;
 }
 

@@ -18,6 +18,7 @@
 namespace kv {
 
 constexpr int kMaxRank = 6;
+constexpr int kMaxKrylov = 32;  // largest Krylov dimension of local_krylov
 using cplx = std::complex<double>;
 
 struct Error : std::runtime_error {
@@ -84,6 +85,13 @@ struct Context {
     } svd;
     long long plans_built = 0;  // plan-cache misses
     double plan_ms = 0.0;       // host ms spent building those plans
+    // Lanczos early stop: a pinned, device-mapped int that the Krylov
+    // kernels set to 1 when the recurrence stops (stop_dev is its device
+    // address), and one event per issued iteration
+    int *stop_host = nullptr, *stop_dev = nullptr;
+    cudaEvent_t iter_ev[kMaxKrylov] = {};
+    // local_krylov calls, iterations issued, Krylov dimensions reached
+    long long krylov_calls = 0, krylov_issued = 0, krylov_used = 0;
 };
 // the calling thread's context: its bound worker context, else the main one
 Context &ctx();
@@ -384,9 +392,9 @@ void launch_zero(double2 *p, int64_t n);
 void launch_copy(double2 *dst, const double2 *src, int64_t n);
 
 // Krylov (FP64) state kept on the device for one local_krylov call.  The
-// loop is launched without host synchronisation: every kernel of an
-// iteration returns immediately once `done` is set.
-constexpr int kMaxKrylov = 32;
+// loop is launched ahead of the device: every kernel of an iteration returns
+// immediately once `done` is set, and the host stops issuing iterations once
+// it sees the stop flag (Context::stop_host) of an iteration two behind.
 struct KrylovState {
     double2 alpha[kMaxKrylov];  // overlap(V_k, hv) as the reference stores it
     double2 beta[kMaxKrylov];   // overlap(V_{k-1}, hv): the upper off-diagonal
@@ -399,8 +407,9 @@ struct KrylovState {
 };
 
 int reduce_parts();  // number of partial sums used by the vector kernels
-// v0 = psi / |psi|; resets the state (err[0] = 1)
-void krylov_start(KrylovState *st, const double2 *psi, double2 *v0, int64_t n, double2 *parts);
+// v0 = psi / |psi|; resets the state (err[0] = 1).  stop (device address,
+// may be null) is set to 1 if the recurrence stops here (psi zero or not finite).
+void krylov_start(KrylovState *st, const double2 *psi, double2 *v0, int64_t n, double2 *parts, int *stop);
 // Support of the Krylov vectors: v_j is zero beyond n[j] complex elements
 // (its blocks are a prefix of the layout, the blocks reached within j
 // applications of H_eff).
@@ -408,9 +417,11 @@ struct KrylovLens {
     int64_t n[kMaxKrylov + 1];
 };
 // after hv = (dt/2) H v_k: Gram-Schmidt against v_{k-1} (k > 0) and v_k,
-// norm, stop test, v_{k+1} = hv / |hv|, each on the vectors' supports
+// norm, stop test, v_{k+1} = hv / |hv|, each on the vectors' supports; one
+// cooperative launch.  stop (device address, may be null) is set to 1 when
+// the recurrence stops at this iteration.
 void krylov_step(KrylovState *st, int k, double2 *hv, const double2 *vprev, const double2 *vk, double2 *vnext,
-                 const KrylovLens &nl, double2 *parts, double tol, int max_iter);
+                 const KrylovLens &nl, double2 *parts, double tol, int max_iter, int *stop);
 // coefficients from the tridiagonal exponential, then out = sum_i c_i v_i on
 // the support of v_{iters-1}
 void krylov_finish(KrylovState *st, double2 *const *dV, double2 *out, const KrylovLens &nl, int reverse);

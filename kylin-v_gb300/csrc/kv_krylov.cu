@@ -6,6 +6,8 @@
 // reduces those partials in a fixed order before using the value, fused with
 // the update that needs it (classical Gram-Schmidt in the reference's order:
 // beta against v_{k-1} first, then alpha against v_k, then the norm).
+#include <cooperative_groups.h>
+#include <mutex>
 #include "kv_internal.h"
 #include "kv_jacobi.cuh"
 
@@ -57,8 +59,16 @@ __global__ void __launch_bounds__(KT) k_norm_part(const double2 *x, int64_t n, d
     if (threadIdx.x == 0) parts[blockIdx.x] = r;
 }
 
+// the host-mapped stop flag: visible to the host once the kernel has finished
+__device__ __forceinline__ void raise_stop(int *stop) {
+    if (stop) {
+        *reinterpret_cast<volatile int *>(stop) = 1;
+        __threadfence_system();
+    }
+}
+
 __global__ void __launch_bounds__(KT) k_start(KrylovState *st, const double2 *psi, double2 *v0, int64_t n,
-                                              const double2 *parts, int nparts) {
+                                              const double2 *parts, int nparts, int *stop) {
     const double nrm = sqrt(reduce_partials(parts, nparts).x);
     const bool bad = !isfinite(nrm) || nrm == 0.0;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -67,6 +77,7 @@ __global__ void __launch_bounds__(KT) k_start(KrylovState *st, const double2 *ps
         st->done = bad ? 1 : 0;
         st->iters = 0;
         st->status = bad ? KV_ENONFINITE : KV_OK;
+        if (bad) raise_stop(stop);
     }
     const double inv = bad ? 0.0 : 1.0 / nrm;
     for (int64_t i = blockIdx.x * (int64_t)KT + threadIdx.x; i < n; i += (int64_t)gridDim.x * KT)
@@ -110,9 +121,9 @@ __global__ void __launch_bounds__(KT) k_sub(KrylovState *st, double2 *hv, const 
 }
 
 // nrm = sqrt(reduce(pin)); err[k+1] = err[k] nrm; stop test; vnext = hv / nrm
-__global__ void __launch_bounds__(KT) k_normalize(KrylovState *st, const double2 *hv, double2 *vnext, int64_t n,
-                                                  const double2 *pin, int nparts, int k, double tol, int max_iter) {
-    if (st->done) return;
+__device__ __forceinline__ void normalize_body(KrylovState *st, const double2 *hv, double2 *vnext, int64_t n,
+                                               const double2 *pin, int nparts, int k, double tol, int max_iter,
+                                               int *stop) {
     const double nrm = sqrt(reduce_partials(pin, nparts).x);
     const double e = st->err[k] * nrm;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -121,15 +132,86 @@ __global__ void __launch_bounds__(KT) k_normalize(KrylovState *st, const double2
             st->status = KV_ENONFINITE;
             st->done = 1;
             st->iters = k + 1;
+            raise_stop(stop);
         } else if (e <= tol || k + 1 >= max_iter - 1) {
             st->done = 1;
             st->iters = k + 1;
+            raise_stop(stop);
         }
     }
     if (!(nrm > 0.0) || !isfinite(nrm)) return;
     const double inv = 1.0 / nrm;
     for (int64_t i = blockIdx.x * (int64_t)KT + threadIdx.x; i < n; i += (int64_t)gridDim.x * KT)
         vnext[i] = make_double2(hv[i].x * inv, hv[i].y * inv);
+}
+
+__global__ void __launch_bounds__(KT) k_normalize(KrylovState *st, const double2 *hv, double2 *vnext, int64_t n,
+                                                  const double2 *pin, int nparts, int k, double tol, int max_iter,
+                                                  int *stop) {
+    if (st->done) return;
+    normalize_body(st, hv, vnext, n, pin, nparts, k, tol, max_iter, stop);
+}
+
+// One Lanczos iteration after hv = (dt/2) H v_k, as one cooperative launch of
+// the same grid the separate kernels use (k_dot_part, k_sub, k_sub,
+// k_normalize), with a grid barrier where they end: the partial sums, their
+// fixed-order reductions and so every result are the same bits.
+__global__ void __launch_bounds__(KT) k_lanczos_step(KrylovState *st, int k, double2 *hv, const double2 *vprev,
+                                                     const double2 *vk, double2 *vnext, int64_t n_prev, int64_t n_k,
+                                                     int64_t n_next, double2 *P0, double2 *P1, int nparts, double tol,
+                                                     int max_iter, int *stop) {
+    namespace cg = cooperative_groups;
+    cg::grid_group grid = cg::this_grid();
+    // read once, before the first barrier: this launch sets it only after the last one
+    if (*reinterpret_cast<volatile int *>(&st->done)) return;  // uniform over the grid
+    const int64_t i0 = blockIdx.x * (int64_t)KT + threadIdx.x, di = (int64_t)gridDim.x * KT;
+    if (k > 0) {
+        double2 s = make_double2(0.0, 0.0);
+        for (int64_t i = i0; i < n_prev; i += di) s = cadd(s, cdotc(hv[i], vprev[i]));
+        double2 r = block_sum(s);
+        if (threadIdx.x == 0) P0[blockIdx.x] = r;
+        grid.sync();
+        const double2 c = reduce_partials(P0, nparts);
+        if (blockIdx.x == 0 && threadIdx.x == 0) st->beta[k - 1] = c;
+        s = make_double2(0.0, 0.0);
+        for (int64_t i = i0; i < n_k; i += di) {
+            double2 h = hv[i];
+            if (i < n_prev) {
+                const double2 x = vprev[i];
+                h.x -= c.x * x.x - c.y * x.y;
+                h.y -= c.x * x.y + c.y * x.x;
+                hv[i] = h;
+            }
+            s = cadd(s, cdotc(h, vk[i]));
+        }
+        r = block_sum(s);
+        if (threadIdx.x == 0) P1[blockIdx.x] = r;
+    } else {
+        double2 s = make_double2(0.0, 0.0);
+        for (int64_t i = i0; i < n_k; i += di) s = cadd(s, cdotc(hv[i], vk[i]));
+        const double2 r = block_sum(s);
+        if (threadIdx.x == 0) P1[blockIdx.x] = r;
+    }
+    grid.sync();
+    {
+        const double2 c = reduce_partials(P1, nparts);
+        if (blockIdx.x == 0 && threadIdx.x == 0) st->alpha[k] = c;
+        double2 s = make_double2(0.0, 0.0);
+        for (int64_t i = i0; i < n_next; i += di) {
+            double2 h = hv[i];
+            if (i < n_k) {
+                const double2 x = vk[i];
+                h.x -= c.x * x.x - c.y * x.y;
+                h.y -= c.x * x.y + c.y * x.x;
+                hv[i] = h;
+            }
+            s.x += h.x * h.x + h.y * h.y;
+        }
+        const double2 r = block_sum(s);
+        if (threadIdx.x == 0) P0[blockIdx.x] = r;
+    }
+    grid.sync();
+    normalize_body(st, hv, vnext, n_next, P0, nparts, k, tol, max_iter, stop);
 }
 
 // T = tridiag(Re alpha, beta upper); c = exp(img T) e0 with img = -i (forward)
@@ -227,21 +309,47 @@ __global__ void k_store_norm2(const double2 *parts, int nparts, double *result) 
 
 int reduce_parts() { return std::max(1, std::min(512, 2 * ctx().num_sms)); }
 
-void krylov_start(KrylovState *st, const double2 *psi, double2 *v0, int64_t n, double2 *parts) {
+void krylov_start(KrylovState *st, const double2 *psi, double2 *v0, int64_t n, double2 *parts, int *stop) {
     const int np = reduce_parts();
     k_norm_part<<<np, KT, 0, ctx().stream>>>(psi, n, parts);
     counted();
-    k_start<<<np, KT, 0, ctx().stream>>>(st, psi, v0, n, parts, np);
+    k_start<<<np, KT, 0, ctx().stream>>>(st, psi, v0, n, parts, np, stop);
     counted();
     KV_CUDA(cudaGetLastError());
 }
 
+// Whether the fused step fits one co-resident wave on this device (checked
+// once per device).  The fused step runs only on the main context's stream:
+// kernels of one stream never overlap, so its grid barrier waits on no
+// other launch of this library.
+static bool lanczos_step_fused(int device, int np) {
+    static std::mutex mu;
+    static int ok[64] = {};  // 0 unknown, 1 yes, -1 no
+    if (device < 0 || device >= 64) return false;
+    std::lock_guard<std::mutex> lk(mu);
+    if (ok[device] == 0) {
+        int coop = 0, per_sm = 0, sms = 0;
+        KV_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device));
+        KV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+        KV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lanczos_step, KT, 0));
+        ok[device] = (coop && (int64_t)per_sm * sms >= np) ? 1 : -1;
+    }
+    return ok[device] > 0;
+}
+
 void krylov_step(KrylovState *st, int k, double2 *hv, const double2 *vprev, const double2 *vk, double2 *vnext,
-                 const KrylovLens &nl, double2 *parts, double tol, int max_iter) {
-    const int np = reduce_parts();
+                 const KrylovLens &nl, double2 *parts, double tol, int max_iter, int *stop) {
+    int np = reduce_parts();
     double2 *P0 = parts, *P1 = parts + np;
     cudaStream_t s = ctx().stream;
-    const int64_t n_prev = k > 0 ? nl.n[k - 1] : 0, n_k = nl.n[k], n_next = nl.n[k + 1];
+    int64_t n_prev = k > 0 ? nl.n[k - 1] : 0, n_k = nl.n[k], n_next = nl.n[k + 1];
+    if (&ctx() == &main_ctx() && lanczos_step_fused(ctx().device, np)) {
+        void *args[] = {&st, &k, &hv, &vprev, &vk, &vnext, &n_prev, &n_k, &n_next, &P0, &P1, &np, &tol, &max_iter,
+                        &stop};
+        KV_CUDA(cudaLaunchCooperativeKernel((const void *)k_lanczos_step, dim3(np), dim3(KT), args, 0, s));
+        counted();
+        return;
+    }
     if (k > 0) {
         k_dot_part<<<np, KT, 0, s>>>(st, hv, vprev, n_prev, P0);
         counted();
@@ -253,7 +361,7 @@ void krylov_step(KrylovState *st, int k, double2 *hv, const double2 *vprev, cons
     }
     k_sub<<<np, KT, 0, s>>>(st, hv, vk, nullptr, n_k, n_next, P1, P0, np, &st->alpha[k]);
     counted();
-    k_normalize<<<np, KT, 0, s>>>(st, hv, vnext, n_next, P0, np, k, tol, max_iter);
+    k_normalize<<<np, KT, 0, s>>>(st, hv, vnext, n_next, P0, np, k, tol, max_iter, stop);
     counted();
     KV_CUDA(cudaGetLastError());
 }

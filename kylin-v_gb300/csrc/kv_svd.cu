@@ -263,6 +263,138 @@ __global__ void __launch_bounds__(NT) k_svd_jacobi_w(const SvdSector *__restrict
     if (threadIdx.x == 0) status[blockIdx.x] = converged ? sweep : -sweep;
 }
 
+// One-sided Jacobi on the r columns of the row-major block sw (p rows, row
+// stride ldw) by a CTA of 512 threads: round-robin pairs, one group of GJ
+// lanes a pair, tolerance tol2 on the squared cosine, columns with norm^2 at
+// or below zt left alone.  With E > 0 each lane holds its E elements of both
+// columns (rows gjl + k GJ; p <= E GJ) in registers between the dot product
+// and the rotation; E == 0 loops over the rows.  The caller picks GJ from r so
+// that the r/2 pairs of a round keep most of the 16 warps busy.  cn: [r]
+// scratch.  Returns the sweeps used, negative if max_sweeps ran out.
+template <int GJ, int E>
+__device__ __forceinline__ int qrj_jacobi(float2 *sw, int ldw, int p, int r, float *cn, int *rotated,
+                                          int max_sweeps, float tol2, float zt) {
+    constexpr int NT = 512, NW = NT / 32;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int gj = tid / GJ, gjl = tid % GJ, ngj = NT / GJ;
+    const unsigned jmask = GJ == 32 ? 0xFFFFFFFFu : (((1u << GJ) - 1u) << (lane & ~(GJ - 1)));
+    const int qe = r + (r & 1), m1 = qe - 1;
+    int sweep = 0;
+    bool converged = r < 2;
+    for (; sweep < max_sweeps && !converged; ++sweep) {
+        for (int j = warp; j < r; j += NW) {
+            float a = 0.f;
+            for (int i = lane; i < p; i += 32) {
+                const float2 x = sw[i * ldw + j];
+                a += x.x * x.x + x.y * x.y;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xFFFFFFFFu, a, o);
+            if (lane == 0) cn[j] = a;
+        }
+        if (tid == 0) *rotated = 0;
+        __syncthreads();
+        for (int rr = 0; rr < m1; ++rr) {
+            for (int pi = gj; pi < qe / 2; pi += ngj) {
+                int c0 = 0, c1;
+                if (pi > 0) { c0 = pi - 1 + rr; if (c0 >= m1) c0 -= m1; ++c0; }
+                c1 = qe - 2 - pi + rr; if (c1 >= m1) c1 -= m1; ++c1;
+                if (c0 > c1) { const int x = c0; c0 = c1; c1 = x; }
+                if (c1 >= r) continue;  // group-uniform from here on
+                const float a = cn[c0], b = cn[c1];
+                if (!(a > zt) || !(b > zt)) continue;
+                float cr = 0.f, ci = 0.f;
+                float2 xv[E > 0 ? E : 1], yv[E > 0 ? E : 1];
+                if constexpr (E > 0) {
+                    // two accumulator pairs (even / odd k) halve the dependent
+                    // chain where registers allow (E <= 8)
+                    float2 a1 = make_float2(0.f, 0.f), a2 = a1, a3 = a1, a4 = a1;
+#pragma unroll
+                    for (int kk = 0; kk < E; ++kk) {
+                        const int i = gjl + kk * GJ;
+                        xv[kk] = i < p ? sw[i * ldw + c0] : make_float2(0.f, 0.f);
+                        yv[kk] = i < p ? sw[i * ldw + c1] : make_float2(0.f, 0.f);
+                        const float2 ys = make_float2(yv[kk].y, yv[kk].x);
+                        if ((kk & 1) && E <= 8) {
+                            a3 = __ffma2_rn(xv[kk], yv[kk], a3);
+                            a4 = __ffma2_rn(xv[kk], ys, a4);
+                        } else {
+                            a1 = __ffma2_rn(xv[kk], yv[kk], a1);
+                            a2 = __ffma2_rn(xv[kk], ys, a2);
+                        }
+                    }
+                    cr = (a1.x + a3.x) + (a1.y + a3.y);
+                    ci = (a2.x + a4.x) - (a2.y + a4.y);
+                } else {
+                    for (int i = gjl; i < p; i += GJ) {
+                        const float2 xi = sw[i * ldw + c0], yi = sw[i * ldw + c1];
+                        cr += xi.x * yi.x + xi.y * yi.y;
+                        ci += xi.x * yi.y - xi.y * yi.x;
+                    }
+                }
+#pragma unroll
+                for (int o = GJ / 2; o > 0; o >>= 1) {
+                    cr += __shfl_xor_sync(jmask, cr, o, GJ);
+                    ci += __shfl_xor_sync(jmask, ci, o, GJ);
+                }
+                // |c|^2 <= tol^2 a b: the pair is orthogonal to the tolerance
+                const float ac2 = cr * cr + ci * ci;
+                if (!(ac2 > tol2 * a * b)) continue;
+                // t = sign(z) / (|z| + sqrt(1 + z^2)), z = (b - a) / (2|c|), from
+                // hardware reciprocal square roots and one fast reciprocal: an
+                // inexact t only changes the angle, and (cs, sn) below stay a
+                // rotation to FP32 rounding whatever t is.  |z| is clamped so
+                // 1 + z^2 stays finite.
+                const float rac = rsqrtf(ac2);  // 1 / |c|
+                const float ac = ac2 * rac;
+                const float z = fminf(fmaxf(0.5f * (b - a) * rac, -1e18f), 1e18f);
+                const float w = fmaf(z, z, 1.f);
+                const float tn = copysignf(__fdividef(1.f, fabsf(z) + w * rsqrtf(w)), z);
+                kvj::Rot<float> rot;
+                rot.cs = rsqrtf(fmaf(tn, tn, 1.f));
+                const float sn = tn * rot.cs;
+                rot.s_re = sn * cr * rac;
+                rot.s_im = sn * ci * rac;
+                if (gjl == 0) {
+                    *rotated = 1;
+                    cn[c0] = a - tn * ac;
+                    cn[c1] = b + tn * ac;
+                }
+                if constexpr (E > 0) {
+                    const float2 cs2 = make_float2(rot.cs, rot.cs), sr2 = make_float2(rot.s_re, rot.s_re);
+                    const float2 msr2 = make_float2(-rot.s_re, -rot.s_re), pm = make_float2(-rot.s_im, rot.s_im);
+#pragma unroll
+                    for (int kk = 0; kk < E; ++kk) {
+                        const int i = gjl + kk * GJ;
+                        const float2 xo = xv[kk], yo = yv[kk];
+                        float2 nx = __fmul2_rn(cs2, xo);
+                        nx = __ffma2_rn(msr2, yo, nx);
+                        nx = __ffma2_rn(pm, make_float2(yo.y, yo.x), nx);
+                        float2 ny = __fmul2_rn(cs2, yo);
+                        ny = __ffma2_rn(sr2, xo, ny);
+                        ny = __ffma2_rn(pm, make_float2(xo.y, xo.x), ny);
+                        if (i < p) {
+                            sw[i * ldw + c0] = nx;
+                            sw[i * ldw + c1] = ny;
+                        }
+                    }
+                } else {
+                    for (int i = gjl; i < p; i += GJ) {
+                        float2 xi = sw[i * ldw + c0], yi = sw[i * ldw + c1];
+                        kvj::rotate_pair(rot, xi.x, xi.y, yi.x, yi.y);
+                        sw[i * ldw + c0] = xi;
+                        sw[i * ldw + c1] = yi;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        converged = (*rotated == 0);
+        __syncthreads();
+    }
+    return converged ? sweep : -sweep;
+}
+
 // QR-preconditioned one-sided Jacobi (mixed mode).  One CTA of 512 threads
 // per charge sector; the sector is held in shared memory in FP32 as p rows of
 // length q (row stride q + 1, so reads of one column by consecutive rows fall
@@ -282,12 +414,12 @@ __global__ void __launch_bounds__(NT) k_svd_jacobi_w(const SvdSector *__restrict
 //     buffered), and each row's exact trailing norm is accumulated while the
 //     row is updated.  A group of 16 lanes updates two rows at once, so each
 //     pivot-row element it loads serves both.
-//  2. One-sided Jacobi on M's r columns (round-robin pairs, 8 lanes a pair,
-//     each lane holding its EPL elements of both columns in registers between
-//     the dot product and the rotation; tolerance `tol` on the cosine).  M is
-//     row-pivoted triangular, so it converges in fewer sweeps than T, and only
-//     r columns are rotated.  The rotation is formed from one reciprocal
-//     square root of |c|^2 and one of 1 + t^2.
+//  2. One-sided Jacobi on M's r columns (qrj_jacobi: round-robin pairs, 32,
+//     16 or 8 lanes a pair for r <= 32, <= 64 or more, so that a round's r/2
+//     pairs occupy most warps; each lane holds its elements of both columns in
+//     registers between the dot product and the rotation, 8 EPL rows per pair
+//     in all; tolerance `tol` on the cosine).  M is row-pivoted triangular, so
+//     it converges in fewer sweeps than T, and only r columns are rotated.
 //  3. Columns sorted by norm: S = norms (descending), Us = normalised columns
 //     (column-major p x r at the sector's t_off), S = 0 in the sector's
 //     remaining slots up to q.
@@ -299,7 +431,6 @@ __global__ void __launch_bounds__(512, 1) k_svd_qrj(const SvdSector *__restrict_
                                                     float tol, float qr_floor) {
     constexpr int NT = 512, NW = NT / 32;
     constexpr int GQ = 16;                     // lanes per row in the QR phase (two rows at a time)
-    constexpr int GJ = 8;                      // lanes per column pair in the Jacobi phase
     extern __shared__ float2 sw[];
     __shared__ float wbest[2][NW];
     __shared__ int wbesti[2][NW];
@@ -481,110 +612,17 @@ __global__ void __launch_bounds__(512, 1) k_svd_qrj(const SvdSector *__restrict_
     }
     __syncthreads();
 
-    // ---- one-sided Jacobi on the r columns of M
-    const int gj = tid / GJ, gjl = tid % GJ, ngj = NT / GJ;
-    const unsigned jmask = 0xFFu << (lane & ~(GJ - 1));
+    // ---- one-sided Jacobi on the r columns of M; the group width follows r
+    // (r/2 pairs a round), the register capacity per lane follows EPL
     const float zt = 1e-14f * fro2;  // (1e-7 ||T||_F)^2: numerically zero columns
     const float tol2 = tol * tol;
-    const int qe = r + (r & 1), m1 = qe - 1;
-    int sweep = 0;
-    bool converged = r < 2;
-    for (; sweep < max_sweeps && !converged; ++sweep) {
-        for (int j = warp; j < r; j += NW) {
-            float a = 0.f;
-            for (int i = lane; i < p; i += 32) {
-                const float2 x = sw[i * ldw + j];
-                a += x.x * x.x + x.y * x.y;
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xFFFFFFFFu, a, o);
-            if (lane == 0) cn[j] = a;
-        }
-        if (tid == 0) rotated = 0;
-        __syncthreads();
-        for (int rr = 0; rr < m1; ++rr) {
-            for (int pi = gj; pi < qe / 2; pi += ngj) {
-                int c0 = 0, c1;
-                if (pi > 0) { c0 = pi - 1 + rr; if (c0 >= m1) c0 -= m1; ++c0; }
-                c1 = qe - 2 - pi + rr; if (c1 >= m1) c1 -= m1; ++c1;
-                if (c0 > c1) { const int x = c0; c0 = c1; c1 = x; }
-                if (c1 >= r) continue;
-                const float a = cn[c0], b = cn[c1];
-                if (!(a > zt) || !(b > zt)) continue;
-                float cr = 0.f, ci = 0.f;
-                float2 xv[EPL > 0 ? EPL : 1], yv[EPL > 0 ? EPL : 1];
-                if constexpr (EPL > 0) {
-                    float2 a1 = make_float2(0.f, 0.f), a2 = make_float2(0.f, 0.f);
-#pragma unroll
-                    for (int kk = 0; kk < EPL; ++kk) {
-                        const int i = gjl + kk * GJ;
-                        xv[kk] = i < p ? sw[i * ldw + c0] : make_float2(0.f, 0.f);
-                        yv[kk] = i < p ? sw[i * ldw + c1] : make_float2(0.f, 0.f);
-                        a1 = __ffma2_rn(xv[kk], yv[kk], a1);
-                        a2 = __ffma2_rn(xv[kk], make_float2(yv[kk].y, yv[kk].x), a2);
-                    }
-                    cr = a1.x + a1.y;
-                    ci = a2.x - a2.y;
-                } else {
-                    for (int i = gjl; i < p; i += GJ) {
-                        const float2 xi = sw[i * ldw + c0], yi = sw[i * ldw + c1];
-                        cr += xi.x * yi.x + xi.y * yi.y;
-                        ci += xi.x * yi.y - xi.y * yi.x;
-                    }
-                }
-#pragma unroll
-                for (int o = GJ / 2; o > 0; o >>= 1) {
-                    cr += __shfl_xor_sync(jmask, cr, o, GJ);
-                    ci += __shfl_xor_sync(jmask, ci, o, GJ);
-                }
-                // |c|^2 <= tol^2 a b: the pair is orthogonal to the tolerance
-                const float ac2 = cr * cr + ci * ci;
-                if (!(ac2 > tol2 * a * b)) continue;
-                const float rac = rsqrtf(ac2);  // 1 / |c|
-                const float ac = ac2 * rac;
-                const float z = 0.5f * (b - a) * rac;
-                const float tn = copysignf(1.f, z) / (fabsf(z) + sqrtf(fmaf(z, z, 1.f)));
-                kvj::Rot<float> rot;
-                rot.cs = rsqrtf(fmaf(tn, tn, 1.f));
-                const float sn = tn * rot.cs;
-                rot.s_re = sn * cr * rac;
-                rot.s_im = sn * ci * rac;
-                if (gjl == 0) {
-                    rotated = 1;
-                    cn[c0] = a - tn * ac;
-                    cn[c1] = b + tn * ac;
-                }
-                if constexpr (EPL > 0) {
-                    const float2 cs2 = make_float2(rot.cs, rot.cs), sr2 = make_float2(rot.s_re, rot.s_re);
-                    const float2 msr2 = make_float2(-rot.s_re, -rot.s_re), pm = make_float2(-rot.s_im, rot.s_im);
-#pragma unroll
-                    for (int kk = 0; kk < EPL; ++kk) {
-                        const int i = gjl + kk * GJ;
-                        const float2 xo = xv[kk], yo = yv[kk];
-                        float2 nx = __fmul2_rn(cs2, xo);
-                        nx = __ffma2_rn(msr2, yo, nx);
-                        nx = __ffma2_rn(pm, make_float2(yo.y, yo.x), nx);
-                        float2 ny = __fmul2_rn(cs2, yo);
-                        ny = __ffma2_rn(sr2, xo, ny);
-                        ny = __ffma2_rn(pm, make_float2(xo.y, xo.x), ny);
-                        if (i < p) {
-                            sw[i * ldw + c0] = nx;
-                            sw[i * ldw + c1] = ny;
-                        }
-                    }
-                } else {
-                    for (int i = gjl; i < p; i += GJ) {
-                        float2 xi = sw[i * ldw + c0], yi = sw[i * ldw + c1];
-                        kvj::rotate_pair(rot, xi.x, xi.y, yi.x, yi.y);
-                        sw[i * ldw + c0] = xi;
-                        sw[i * ldw + c1] = yi;
-                    }
-                }
-            }
-            __syncthreads();
-        }
-        converged = (rotated == 0);
-        __syncthreads();
+    int sweeps;
+    if constexpr (EPL > 0) {
+        if (r <= 32) sweeps = qrj_jacobi<32, (EPL >= 4 ? EPL / 4 : 1)>(sw, ldw, p, r, cn, &rotated, max_sweeps, tol2, zt);
+        else if (r <= 64) sweeps = qrj_jacobi<16, EPL / 2>(sw, ldw, p, r, cn, &rotated, max_sweeps, tol2, zt);
+        else sweeps = qrj_jacobi<8, EPL>(sw, ldw, p, r, cn, &rotated, max_sweeps, tol2, zt);
+    } else {
+        sweeps = qrj_jacobi<8, 0>(sw, ldw, p, r, cn, &rotated, max_sweeps, tol2, zt);
     }
 
     // ---- sorted singular values and normalised columns
@@ -612,7 +650,7 @@ __global__ void __launch_bounds__(512, 1) k_svd_qrj(const SvdSector *__restrict_
     }
     for (int j = r + tid; j < q; j += NT) S[s.s_off + j] = 0.0;  // every one of the sector's q slots
     if (tid == 0) {
-        status[blockIdx.x] = converged ? sweep : -sweep;
+        status[blockIdx.x] = sweeps;
         ranks[blockIdx.x] = r;
     }
 }

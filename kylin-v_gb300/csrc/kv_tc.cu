@@ -4,7 +4,7 @@
 // GB300 runs FP64 arithmetic at a small fraction of its FP32 and tensor
 // rates, so no FP64 instruction is issued per element of a tile.  Instead:
 //
-//  1. Slicing (k_slice, once per operand per call).  Every GEMM row of an A
+//  1. Slicing (slice_item; one launch per call for both operands).  Every GEMM row of an A
 //     block (and every GEMM column of a B block) gets a binary exponent e
 //     with max_k |x| < 2^e over that row; each real value becomes the
 //     fixed-point integer X = round(x 2^(37-e)), |X| <= 2^37, written as five
@@ -14,7 +14,9 @@
 //     the exact integer sum X_re + X_im).  Integer arithmetic only.  Where
 //     the contracted index runs over parts of very different magnitude (MPO
 //     channels, Schmidt values), it is first balanced by exact powers of two
-//     (k_kmax, GemmPlan::balance_k).  The digits are written directly in the
+//     (kmax_item, GemmPlan::balance_k; on the main stream the maxima and the
+//     slicing are one cooperative launch, k_slice_coop, with grid barriers
+//     between zeroing, maxima and slicing).  The digits are written directly in the
 //     tensor cores' shared-memory panel layout (K-major, no swizzle: 8-row x
 //     16-byte core matrices, K-adjacent core matrices 128 B apart, 8-row
 //     groups 256 B apart), one 16-deep K panel after another, all 15 digit
@@ -52,6 +54,7 @@
 // Every mbarrier wait is bounded; on timeout the CTA records an error, waits
 // (bounded) for its copies and MMAs in flight, frees tensor memory and exits.
 #include <mutex>
+#include <cooperative_groups.h>
 #include <cuda_fp16.h>
 
 #include <cstdint>
@@ -152,15 +155,14 @@ __device__ __forceinline__ double balance_factor(const unsigned long long *kmax,
 // Per-k maxima for balancing: one CTA per (view, 8 rows), one warp per row;
 // the 8 rows' values are reduced in shared memory, then one atomicMax per k
 // (non-negative doubles order like their bit patterns).
-__global__ void __launch_bounds__(256) k_kmax(const SliceJob *__restrict__ ajobs, const int2 *__restrict__ aitems,
-                                              int na, const SliceJob *__restrict__ bjobs,
-                                              const int2 *__restrict__ bitems, const double2 *__restrict__ A,
-                                              const double2 *__restrict__ B, unsigned long long *kmax,
-                                              int64_t kscales, const int *skip, int step) {
-    if (skip && *skip) return;
+// item bid of the A items followed by the B items (CTA-uniform)
+__device__ __forceinline__ void kmax_item(const SliceJob *__restrict__ ajobs, const int2 *__restrict__ aitems, int na,
+                                          const SliceJob *__restrict__ bjobs, const int2 *__restrict__ bitems,
+                                          const double2 *__restrict__ A, const double2 *__restrict__ B,
+                                          unsigned long long *kmax, int64_t kscales, int step, int bid) {
     __shared__ unsigned long long red[8][33];
-    const bool is_b = blockIdx.x >= (unsigned)na;
-    const int2 it = is_b ? bitems[blockIdx.x - na] : aitems[blockIdx.x];
+    const bool is_b = bid >= na;
+    const int2 it = is_b ? bitems[bid - na] : aitems[bid];
     const SliceJob j = is_b ? bjobs[it.x] : ajobs[it.x];
     if (j.entry > step || j.ks_off < 0) return;  // uniform over the CTA
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -188,16 +190,23 @@ __global__ void __launch_bounds__(256) k_kmax(const SliceJob *__restrict__ ajobs
     }
 }
 
-// A row holding an Inf or NaN sets bit kErrNonFinite of *err: fixed point has
-// no code for it, and the digits written for that row are meaningless.
-template <int TR>
-__global__ void __launch_bounds__(256) k_slice(const SliceJob *__restrict__ jobs, const int2 *__restrict__ items,
-                                               const double2 *__restrict__ src, __half *__restrict__ dst,
-                                               int *__restrict__ exps, double alpha, const int *skip, int step,
-                                               int *err, const unsigned long long *kmax, int64_t kscales,
-                                               int b_side) {
+__global__ void __launch_bounds__(256) k_kmax(const SliceJob *__restrict__ ajobs, const int2 *__restrict__ aitems,
+                                              int na, const SliceJob *__restrict__ bjobs,
+                                              const int2 *__restrict__ bitems, const double2 *__restrict__ A,
+                                              const double2 *__restrict__ B, unsigned long long *kmax,
+                                              int64_t kscales, const int *skip, int step) {
     if (skip && *skip) return;
-    const int2 it = items[blockIdx.x];
+    kmax_item(ajobs, aitems, na, bjobs, bitems, A, B, kmax, kscales, step, (int)blockIdx.x);
+}
+
+// One slicing item (a job's 8 rows from it.y, one per warp).  A row holding
+// an Inf or NaN sets bit kErrNonFinite of *err: fixed point has no code for
+// it, and the digits written for that row are meaningless.  Warps return on
+// their own; there is no barrier here.
+template <int TR>
+__device__ __forceinline__ void slice_item(const SliceJob *__restrict__ jobs, int2 it, const double2 *__restrict__ src,
+                                           __half *__restrict__ dst, int *__restrict__ exps, double alpha, int step,
+                                           int *err, const unsigned long long *kmax, int64_t kscales, int b_side) {
     const SliceJob j = jobs[it.x];
     if (j.entry > step) return;  // no active segment reads this block
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -260,6 +269,52 @@ __global__ void __launch_bounds__(256) k_slice(const SliceJob *__restrict__ jobs
             for (int i = 0; i < NDIG; ++i)
                 *reinterpret_cast<__half2 *>(p + (c * NDIG + i) * (TR * BKC)) = digits2(d0[i], d1[i]);
         }
+    }
+}
+
+// Both operands' slicing in one launch: CTAs [0, na) take the A items, the
+// rest the B items.
+__global__ void __launch_bounds__(256) k_slice_ab(const SliceJob *__restrict__ ajobs, const int2 *__restrict__ aitems,
+                                                  int na, const SliceJob *__restrict__ bjobs,
+                                                  const int2 *__restrict__ bitems, const double2 *__restrict__ A,
+                                                  const double2 *__restrict__ B, __half *__restrict__ ap,
+                                                  __half *__restrict__ bp, int *__restrict__ ae,
+                                                  int *__restrict__ be, double alpha, const int *skip, int step,
+                                                  int *err, const unsigned long long *kmax, int64_t kscales) {
+    if (skip && *skip) return;
+    const int bid = (int)blockIdx.x;
+    if (bid < na) slice_item<BM>(ajobs, aitems[bid], A, ap, ae, 1.0, step, err, kmax, kscales, 0);
+    else slice_item<BN>(bjobs, bitems[bid - na], B, bp, be, alpha, step, err, kmax, kscales, 1);
+}
+
+// The balanced slicing as one cooperative launch: zero the per-index maxima,
+// grid barrier, the maxima of every contracted index (k_kmax's work), grid
+// barrier, both operands' slicing (k_slice_ab's work); each CTA walks the
+// items with a stride of the grid.  kmax == nullptr: no balancing, no barrier.
+__global__ void __launch_bounds__(256) k_slice_coop(const SliceJob *__restrict__ ajobs,
+                                                    const int2 *__restrict__ aitems, int na,
+                                                    const SliceJob *__restrict__ bjobs,
+                                                    const int2 *__restrict__ bitems, int nb,
+                                                    const double2 *__restrict__ A, const double2 *__restrict__ B,
+                                                    __half *__restrict__ ap, __half *__restrict__ bp,
+                                                    int *__restrict__ ae, int *__restrict__ be, double alpha,
+                                                    const int *skip, int step, int *err, unsigned long long *kmax,
+                                                    int64_t kscales) {
+    namespace cg = cooperative_groups;
+    if (skip && *skip) return;  // uniform over the grid: nothing in this launch writes it
+    const int nitems = na + nb;
+    if (kmax) {
+        cg::grid_group grid = cg::this_grid();
+        for (int64_t e = blockIdx.x * 256ll + threadIdx.x; e < 2 * kscales; e += (int64_t)gridDim.x * 256)
+            kmax[e] = 0;
+        grid.sync();
+        for (int bid = blockIdx.x; bid < nitems; bid += gridDim.x)
+            kmax_item(ajobs, aitems, na, bjobs, bitems, A, B, kmax, kscales, step, bid);
+        grid.sync();
+    }
+    for (int bid = blockIdx.x; bid < nitems; bid += gridDim.x) {
+        if (bid < na) slice_item<BM>(ajobs, aitems[bid], A, ap, ae, 1.0, step, err, kmax, kscales, 0);
+        else slice_item<BN>(bjobs, bitems[bid - na], B, bp, be, alpha, step, err, kmax, kscales, 1);
     }
 }
 
@@ -768,6 +823,23 @@ void plan_mixed(GemmPlan &g) {
     g.d_bitems = upload_vec(g.bitems);
 }
 
+// Grid of the cooperative slicing launch on a device: every CTA resident at
+// once (0: cooperative launches unavailable).  Checked once per device.
+static int slice_coop_grid(int device) {
+    static std::mutex mu;
+    static int grid[kMaxDevices] = {};  // 0 unknown, > 0 the grid, -1 unavailable
+    if (device < 0 || device >= kMaxDevices) return 0;
+    std::lock_guard<std::mutex> lk(mu);
+    if (grid[device] == 0) {
+        int coop = 0, per_sm = 0, sms = 0;
+        KV_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device));
+        KV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+        KV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_slice_coop, 256, 0));
+        grid[device] = (coop && per_sm > 0) ? per_sm * sms : -1;
+    }
+    return std::max(0, grid[device]);
+}
+
 void launch_gemm_mixed(const GemmPlan &p, const double2 *A, const double2 *B, double2 *C, double alpha,
                        const int *skip, int step) {
     if (p.tiles.empty()) return;
@@ -778,29 +850,37 @@ void launch_gemm_mixed(const GemmPlan &p, const double2 *A, const double2 *B, do
     DevBuf ap(std::max<int64_t>(1, p.a_planes) * sizeof(__half)), bp(std::max<int64_t>(1, p.b_planes) * sizeof(__half));
     DevBuf ae(std::max<int64_t>(1, p.a_exps) * sizeof(int)), be(std::max<int64_t>(1, p.b_exps) * sizeof(int));
     int n = 0;
-    DevBuf kmax;
-    const unsigned long long *km = nullptr;
-    if (p.balance_k && p.k_scales > 0 && !p.aitems.empty() && !p.bitems.empty()) {
-        kmax.alloc(2 * (size_t)p.k_scales * sizeof(unsigned long long));
-        KV_CUDA(cudaMemsetAsync(kmax.p, 0, 2 * (size_t)p.k_scales * sizeof(unsigned long long), c.stream));
-        k_kmax<<<(unsigned)(p.aitems.size() + p.bitems.size()), 256, 0, c.stream>>>(
-            p.d_ajobs.as<SliceJob>(), p.d_aitems.as<int2>(), (int)p.aitems.size(), p.d_bjobs.as<SliceJob>(),
-            p.d_bitems.as<int2>(), A, B, kmax.as<unsigned long long>(), p.k_scales, skip, step);
-        KV_CUDA(cudaGetLastError());
-        km = kmax.as<unsigned long long>();
+    const bool bal = p.balance_k && p.k_scales > 0 && !p.aitems.empty() && !p.bitems.empty();
+    DevBuf kmax(bal ? 2 * (size_t)p.k_scales * sizeof(unsigned long long) : 8);
+    unsigned long long *km = bal ? kmax.as<unsigned long long>() : nullptr;
+    int na = (int)p.aitems.size(), nb = (int)p.bitems.size();
+    const int grid = slice_coop_grid(c.device);
+    if (na + nb > 0 && &c == &main_ctx() && grid > 0) {
+        // one cooperative launch (zero, maxima, slicing); only on the main
+        // context's stream, whose kernels never overlap, so its grid barrier
+        // waits on no other launch of this library
+        const SliceJob *aj = p.d_ajobs.as<SliceJob>(), *bj = p.d_bjobs.as<SliceJob>();
+        const int2 *ai = p.d_aitems.as<int2>(), *bi = p.d_bitems.as<int2>();
+        __half *aph = ap.as<__half>(), *bph = bp.as<__half>();
+        int *aex = ae.as<int>(), *bex = be.as<int>();
+        int64_t ks = p.k_scales;
+        void *args[] = {&aj, &ai, &na, &bj, &bi, &nb, &A, &B, &aph, &bph, &aex, &bex, &alpha, &skip, &step, &err, &km,
+                        &ks};
+        KV_CUDA(cudaLaunchCooperativeKernel((const void *)k_slice_coop, dim3((unsigned)std::min(na + nb, grid)),
+                                            dim3(256), args, 0, c.stream));
         ++n;
-    }
-    if (!p.aitems.empty()) {
-        k_slice<BM><<<(unsigned)p.aitems.size(), 256, 0, c.stream>>>(p.d_ajobs.as<SliceJob>(), p.d_aitems.as<int2>(),
-                                                                     A, ap.as<__half>(), ae.as<int>(), 1.0, skip, step, err,
-                                                                     km, p.k_scales, 0);
-        KV_CUDA(cudaGetLastError());
-        ++n;
-    }
-    if (!p.bitems.empty()) {
-        k_slice<BN><<<(unsigned)p.bitems.size(), 256, 0, c.stream>>>(p.d_bjobs.as<SliceJob>(), p.d_bitems.as<int2>(),
-                                                                     B, bp.as<__half>(), be.as<int>(), alpha, skip, step, err,
-                                                                     km, p.k_scales, 1);
+    } else if (na + nb > 0) {
+        if (bal) {
+            KV_CUDA(cudaMemsetAsync(kmax.p, 0, 2 * (size_t)p.k_scales * sizeof(unsigned long long), c.stream));
+            k_kmax<<<(unsigned)(na + nb), 256, 0, c.stream>>>(p.d_ajobs.as<SliceJob>(), p.d_aitems.as<int2>(), na,
+                                                              p.d_bjobs.as<SliceJob>(), p.d_bitems.as<int2>(), A, B,
+                                                              km, p.k_scales, skip, step);
+            KV_CUDA(cudaGetLastError());
+            ++n;
+        }
+        k_slice_ab<<<(unsigned)(na + nb), 256, 0, c.stream>>>(
+            p.d_ajobs.as<SliceJob>(), p.d_aitems.as<int2>(), na, p.d_bjobs.as<SliceJob>(), p.d_bitems.as<int2>(), A, B,
+            ap.as<__half>(), bp.as<__half>(), ae.as<int>(), be.as<int>(), alpha, skip, step, err, km, p.k_scales);
         KV_CUDA(cudaGetLastError());
         ++n;
     }

@@ -32,7 +32,7 @@ EXPORTS = (
     "kv_svd_truncate", "kv_tdvp_create", "kv_tdvp_sweep", "kv_tdvp_site", "kv_tdvp_stats", "kv_tdvp_free",
     "kv_expectation", "kv_profile", "kv_profile_read", "kv_counters", "kv_expectation_noalloc",
     "kv_tdvp_host_stats", "kv_canonicalize", "kv_sweep_batched", "kv_adjoint_heff", "kv_adjoint_env",
-    "kv_debug_gemm_stall", "kv_debug_pool_usage", "kv_svd_stats", "kv_tdvp_window", "kv_local_expectations",
+    "kv_debug_gemm_stall", "kv_debug_pool_usage", "kv_svd_stats", "kv_krylov_stats", "kv_tdvp_window", "kv_local_expectations",
 )
 
 
@@ -91,6 +91,7 @@ def lib():
         L.kv_debug_gemm_stall.argtypes = [ctypes.c_int]
         ll = ctypes.POINTER(ctypes.c_longlong)
         L.kv_svd_stats.argtypes = [ctypes.c_int, ll, ll, ll, ll, ip]
+        L.kv_krylov_stats.argtypes = [ctypes.c_int, ll, ll, ll]
         L.kv_debug_pool_usage.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_longlong),
                                           ctypes.POINTER(ctypes.c_longlong)]
         _lib = L
@@ -287,6 +288,15 @@ def svd_stats(reset: bool = True) -> dict:
     n = max(1, v[0].value)
     return {"sectors": v[0].value, "mean_columns": v[1].value / n, "mean_rank": v[2].value / n,
             "mean_sweeps": v[3].value / n, "max_sweeps": mx.value}
+
+
+def krylov_stats(reset: bool = True) -> dict:
+    """local_krylov calls since the last reset, Lanczos iterations issued per
+    call and the mean Krylov dimension reached."""
+    v = [ctypes.c_longlong() for _ in range(3)]
+    check(lib().kv_krylov_stats(int(reset), *[ctypes.byref(x) for x in v]))
+    n = max(1, v[0].value)
+    return {"calls": v[0].value, "issued_per_call": v[1].value / n, "mean_dimension": v[2].value / n}
 
 
 def launches() -> int:
