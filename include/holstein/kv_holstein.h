@@ -10,13 +10,19 @@
  * (holstein/state.h:107-157, holstein/operator.h:117-143), parse_stage
  * (holstein/tdvp.h:19-32), the TDVP constructor's arguments
  * (holstein/tdvp.h:60-76) and total_start's stages with a checkpoint
- * State/T-<sweep>.mps after every sweep (holstein/tdvp.h:297-385); errors print
- * a message and exit(1) as the reference does.  Differences: the SA-1TDVP
- * stage (r[2] > 0) is not available and stops with a message; after the
- * global-Krylov stage (r[0] > 0) the sweep environments are rebuilt from the
- * new state (the reference keeps the ones built before that stage); the timer
- * table lists device milliseconds per module.  Environment: KV_PRECISION=mixed selects the mixed-precision path
- * (default FP64), KV_DEVICE the GPU (default 0). */
+ * State/T-<sweep>.mps after every sweep (holstein/tdvp.h:297-385), including
+ * the SA-1TDVP stage: the two-site sweeps append the SVS log
+ * (holstein/svd.h:390-402), the stage runs `nls.py` from PATH to fit it and
+ * reads the widths it writes to `beta`, as the reference does (this
+ * package's kylin-v_gb300/sa_fit.py restates that fit and can be installed
+ * under that name); errors print a message and exit(1) as the reference does.
+ * Differences: after the global-Krylov stage (r[0] > 0) the sweep
+ * environments are rebuilt from the new state (the reference keeps the ones
+ * built before that stage); the SA stage's draws come from one seed
+ * (std::random_device, or KV_SA_SEED when set) instead of a fresh
+ * random_device per draw group; the timer table lists device milliseconds
+ * per module.  Environment: KV_PRECISION=mixed selects the mixed-precision
+ * path (default FP64), KV_DEVICE the GPU (default 0). */
 #ifndef KV_HOLSTEIN_DROPIN_H
 #define KV_HOLSTEIN_DROPIN_H
 
@@ -27,7 +33,9 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <iomanip>
 #include <iostream>
+#include <random>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -281,6 +289,9 @@ class TDVP {
              << (detail::precision() == KV_FP64 ? "\nprecision: FP64" : "\nprecision: mixed") << endl;
         ofstream ofs("SVS");
         ofs << "Total Site = " << ns << endl;
+        int nr = 0;
+        long long nv = 0;
+        detail::check(kv_tdvp_svs(s_, &nr, &nv, nullptr, nullptr), "kv_tdvp_svs");  // starts the record
     }
     TDVP(const TDVP &) = delete;
     TDVP &operator=(const TDVP &) = delete;
@@ -289,14 +300,23 @@ class TDVP {
     }
 
     void one_site() { sweep(1); }
-    void two_site() { sweep(2); }
+    void two_site() {
+        sweep(2);
+        append_svs();
+    }
+    // TDVP::sa_site (holstein/tdvp.h:230-294)
+    void sa_site(vector<double> &betaSet) {
+        unsigned long long seed = std::random_device{}();
+        if (const char *e = getenv("KV_SA_SEED")) seed = strtoull(e, nullptr, 10);
+        if (!sa_set_) {
+            detail::check(kv_tdvp_set_sa(s_, betaSet.data(), (int)betaSet.size(), seed, nullptr), "kv_tdvp_set_sa");
+            sa_set_ = true;
+        }
+        sweep(3);
+    }
     const State &state() const { return mps_; }
 
     void total_start(const array<INT, 4> &r) {
-        if (r[2] != 0) {
-            cout << "The SA-1TDVP stage is not available in libkvgpu." << endl;
-            exit(1);
-        }
         INT swp = 0;
         cout << "\n ---------------- Start Krylov stage ----------------" << endl;
         for (; swp < r[0]; ++swp) {
@@ -309,8 +329,31 @@ class TDVP {
             two_site();
             checkpoint(swp);
         }
+        if (r[2] != 0) {
+            vector<double> betaSet;
+            int ifos = system("nls.py");
+            (void)ifos;
+            cout << "Fitting OK!" << endl;
+            ifstream ifsBeta("beta");
+            if (!ifsBeta.is_open()) cout << "Fail to open beta file" << endl;
+            string tmp;
+            while (getline(ifsBeta, tmp))
+                if (tmp.size() > 3) betaSet.push_back(1.0 / stod(tmp));
+            cout << "Read betas OK!" << endl;
+            if ((INT)betaSet.size() < mps_.nsite() - 1) {
+                cout << "The beta file holds " << betaSet.size() << " widths; the SA-1TDVP stage needs one per bond."
+                     << endl;
+                exit(1);
+            }
+            cout << "\n ---------------- Start SA-1TDVP stage -------------" << endl;
+            for (; swp < r[0] + r[1] + r[2]; ++swp) {
+                cout << "\nSweep " << swp + 1 << ":" << endl;
+                sa_site(betaSet);
+                checkpoint(swp);
+            }
+        }
         cout << "\n ---------------- Start 1TDVP stage ----------------" << endl;
-        for (; swp < r[0] + r[1] + r[3]; ++swp) {
+        for (; swp < r[0] + r[1] + r[2] + r[3]; ++swp) {
             cout << "\nSweep " << swp + 1 << ":" << endl;
             one_site();
             checkpoint(swp);
@@ -336,6 +379,27 @@ class TDVP {
         }
     }
 
+    // the two-site splits' records of the SVS log, in svd_impl's format
+    // (holstein/svd.h:390-402): the kept count, then log10(s_i s_{i-2} / s_{i-1}^2)
+    void append_svs() {
+        int nr = 0;
+        long long nv = 0;
+        detail::check(kv_tdvp_svs(s_, &nr, &nv, nullptr, nullptr), "kv_tdvp_svs");
+        vector<int> counts(nr > 0 ? nr : 1);
+        vector<double> vals(nv > 0 ? nv : 1);
+        detail::check(kv_tdvp_svs(s_, nullptr, nullptr, counts.data(), vals.data()), "kv_tdvp_svs");
+        ofstream ofs("SVS", ofstream::app);
+        long long k = 0;
+        for (int r = 0; r < nr; ++r) {
+            const double *v = vals.data() + k;
+            ofs << counts[r] << endl;
+            for (int i = 2; i < counts[r]; ++i)
+                ofs << std::left << setw(20) << std::scientific << setprecision(11)
+                    << log10(v[i] * v[i - 2] / pow(v[i - 1], 2.0)) << endl;
+            k += counts[r];
+        }
+    }
+
     void checkpoint(INT swp) {
         mps_.max_bond();
         mkdir("State", 0755);
@@ -346,6 +410,7 @@ class TDVP {
     State mps_;
     Operator ham_;
     kv_tdvp s_ = nullptr;
+    bool sa_set_ = false;
     double total_ms_[6] = {};
 };
 

@@ -158,8 +158,27 @@ int kv_tdvp_create(int nsites, const kv_tensor *mps, const kv_tensor *mpo, doubl
  * dt, tolExp / maxIter / tolSVD / maxDim as given); after it the sweep
  * environments are rebuilt from the new state (the reference keeps the ones
  * built before that stage, so its next sweep mixes two states).  The global
- * step's contractions run in `precision`, its SVDs in FP64. */
+ * step's contractions run in `precision`, its SVDs in FP64.  mode 3 = one
+ * SA-1TDVP sweep, TDVP::sa_site (holstein/tdvp.h:230-294) with the widths
+ * and seed of kv_tdvp_set_sa: one_site with sa_svd_impl's split
+ * (holstein/svd.h:443-614; FP64 SVD in every precision mode). */
 int kv_tdvp_sweep(kv_tdvp s, int mode);
+/* SA-1TDVP settings: beta[i] is bond i's width (betaSet[i] of
+ * holstein/tdvp.h:343-358, i.e. 1 / the fitted value bin/nls.py writes),
+ * nbeta >= nsites - 1; seed starts the seed stream.  The reference seeds a
+ * fresh mt19937 from std::random_device before each group of draws (one
+ * synthetic singular value; one new vector); here each group's mt19937 is
+ * seeded by the next 32-bit value of an mt19937 stream started at `seed`, so a
+ * run repeats.  beta == NULL leaves the settings unchanged.  added_last (may
+ * be NULL) receives the states the SA splits of the last sweep added. */
+int kv_tdvp_set_sa(kv_tdvp s, const double *beta, int nbeta, unsigned long long seed, long long *added_last);
+/* The kept singular values (descending) of every two-site split since the
+ * last read, the record svd_impl appends to its SVS file for the SA stage's
+ * fit (holstein/svd.h:356-402, holstein/tdvp.h:166, 202).  values == NULL:
+ * only the number of records and of values; else counts[n_records] and
+ * values[n_values] (sized by a previous query) are filled, in order, and the
+ * records are cleared.  Records are kept from the first call on a handle. */
+int kv_tdvp_svs(kv_tdvp s, int *n_records, long long *n_values, int *counts, double *values);
 /* A window of TDVP::two_site's left-to-right pass (holstein/tdvp.h:150-185):
  * the pass is advanced to site i0 (untimed; n = 0 does only that), then the
  * n local updates at sites (i0, i0+1) ... (i0+n-1, i0+n) run and

@@ -325,7 +325,38 @@ int kv_tdvp_sweep(kv_tdvp s, int mode) {
         if (mode == 1) s->s->one_site();
         else if (mode == 2) s->s->two_site();
         else if (mode == 0) s->s->global_krylov();
-        else throw kv::Error(KV_EINVAL, "mode must be 0, 1 or 2");
+        else if (mode == 3) s->s->sa_site();
+        else throw kv::Error(KV_EINVAL, "mode must be 0, 1, 2 or 3");
+    });
+}
+
+int kv_tdvp_svs(kv_tdvp s, int *n_records, long long *n_values, int *counts, double *values) {
+    return guard([&] {
+        kv::require_init();
+        KV_REQUIRE(s && s->s, KV_EINVAL, "null TDVP handle");
+        s->s->svs_on = true;
+        auto &v = s->s->svs;
+        long long nv = 0;
+        for (auto &r : v) nv += (long long)r.size();
+        if (n_records) *n_records = (int)v.size();
+        if (n_values) *n_values = nv;
+        if (!values) return;
+        KV_REQUIRE(counts, KV_EINVAL, "null count array");
+        long long k = 0;
+        for (size_t i = 0; i < v.size(); ++i) {
+            counts[i] = (int)v[i].size();
+            for (double x : v[i]) values[k++] = x;
+        }
+        v.clear();
+    });
+}
+
+int kv_tdvp_set_sa(kv_tdvp s, const double *beta, int nbeta, unsigned long long seed, long long *added_last) {
+    return guard([&] {
+        kv::require_init();
+        KV_REQUIRE(s && s->s, KV_EINVAL, "null TDVP handle");
+        if (added_last) *added_last = s->s->sa_added;
+        if (beta) s->s->set_sa(beta, nbeta, seed);
     });
 }
 

@@ -832,7 +832,55 @@ static void fill_side(std::vector<Macro> &info, int q, const BlockMeta &b, int l
     info.push_back(mac);
 }
 
-SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int precision) {
+// ---- SA-1TDVP helpers (util/allocation.h:232-256, holstein/svd.h:525-560),
+// written as the reference writes them so the host draws and the synthetic
+// spectrum agree with it value for value
+static double quasi_gauss(double x, double bet) {
+    double r = std::exp(-0.25 * bet * std::pow(x, 2.0)) * std::abs(0.25 * x / bet);
+    r += (0.5 / bet - 0.25 * std::pow(x, 2.0)) * std::erfc(0.5 * std::pow(bet, 0.5) * std::abs(x)) * 0.5 *
+         std::pow(3.1415926 / bet, 0.5);
+    r *= std::exp(-0.25 * bet * std::pow(x, 2.0)) * 4.0 * bet * std::pow(bet / 3.1415926, 0.5);
+    return r;
+}
+
+// the root of quasi_gauss(x) = y on [0, 2] by bisection to 1e-8
+static double inv_quasi_gauss(double y, double bet) {
+    double hi = 2.0, lo = 0.0, mid = 0.0;
+    while (hi - lo > 1e-8) {
+        mid = 0.5 * (hi + lo);
+        if ((quasi_gauss(mid, bet) - y) * (quasi_gauss(lo, bet) - y) < 0) hi = mid;
+        else lo = mid;
+    }
+    return mid;
+}
+
+// States the SA split adds: the descending spectrum's tail continued by
+// s' = 10^(+-r) s_last^2 / s_prev with r = inv_quasi_gauss(u, beta), u uniform
+// in [0, 1) from a fresh generator per value, the sign alternating, clamped
+// to be non-increasing, until a value reaches thres or the spectrum max_dim;
+// only spectra with 5 < n < max_dim values grow.
+static int sa_added(const std::vector<double> &desc, int max_dim, double thres, double beta, std::mt19937 &seeds) {
+    const int n = (int)desc.size();
+    if (n < 2 || !(n < max_dim && n > 5)) return 0;
+    std::vector<double> t = {desc[n - 2], desc[n - 1]};
+    int added = 0;
+    for (int i = n; i < max_dim; ++i) {
+        std::mt19937 gen{(std::mt19937::result_type)(unsigned int)seeds()};
+        std::uniform_real_distribution<double> u(0, 1);
+        const double r = inv_quasi_gauss(u(gen), beta);
+        const double f = (i + n) % 2 == 0 ? std::pow(10, r) : std::pow(10, -1.0 * r);
+        t.push_back(f * std::pow(t[t.size() - 1], 2.0) / t[t.size() - 2]);
+        if (t.back() <= thres) {
+            t.pop_back();
+            break;
+        }
+        if (t.back() > t[t.size() - 2]) t.back() = t[t.size() - 2];
+        added = (int)t.size() - 2;
+    }
+    return added;
+}
+
+SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int precision, SaParams *sa) {
     const Meta &M = A.meta;
     KV_REQUIRE(r1 >= 1 && r1 < M.rank, KV_EINVAL, "svd split must be in [1, rank-1]");
     KV_REQUIRE(max_dim >= 1, KV_EINVAL, "max_dim must be >= 1");
@@ -847,7 +895,7 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
     }
     SvdPlan P;
     std::vector<std::pair<int, int>> sec_rc;
-    const bool mixed = svd_mixed(precision);
+    const bool mixed = svd_mixed(precision) && !sa;
     for (int ri = 0; ri < (int)rows.size(); ++ri)
         for (int ci = 0; ci < (int)cols.size(); ++ci) {
             if (rows[ri].q + cols[ci].q != 0) continue;
@@ -957,6 +1005,30 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
     };
     SvdOut out;
     std::vector<int> kfin = truncate(sv, &out.kept_s, &out.n_total);
+    std::vector<int> ext(nsec, 0);  // SA: states added per sector
+    if (sa) {
+        // sa_svd_impl keeps min(m, n) states per sector; the added states go
+        // to the sectors in order, each taking what its kept side has room for
+        std::vector<double> all;
+        for (int s_ = 0; s_ < nsec; ++s_) {
+            const SvdSector &sc = P.secs[s_];
+            kfin[s_] = std::min(sc.m, sc.n);
+            for (int i = 0; i < kfin[s_]; ++i) all.push_back(sv[sc.s_off + i]);
+        }
+        std::sort(all.begin(), all.end(), std::greater<double>());
+        out.kept_s = all;
+        out.n_total = (int)all.size();
+        int add = sa_added(all, max_dim, thres, sa->beta, *sa->seeds);
+        sa->added = 0;
+        for (int s_ = 0; s_ < nsec && add > 0; ++s_) {
+            const SvdSector &sc = P.secs[s_];
+            const int room = (l2r ? sc.m : sc.n) - kfin[s_];
+            if (kfin[s_] <= 0 || room <= 0) continue;
+            ext[s_] = std::min(add, room);
+            add -= ext[s_];
+            sa->added += ext[s_];
+        }
+    }
     // ---- mixed mode, part 1: FP64 rebuild of the candidate columns.  The
     // kept factor is rebuilt in FP64 from the sector matrix and the FP32
     // singular vectors of the other side,
@@ -1066,9 +1138,9 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
     }
     out.n_kept = 0;
     for (int s_ = 0; s_ < nsec; ++s_) {
-        rows[sec_rc[s_].first].kept = kfin[s_];
-        cols[sec_rc[s_].second].kept = kfin[s_];
-        out.n_kept += kfin[s_];
+        rows[sec_rc[s_].first].kept = kfin[s_] + ext[s_];
+        cols[sec_rc[s_].second].kept = kfin[s_] + ext[s_];
+        out.n_kept += kfin[s_] + ext[s_];
     }
     // redistribution, holstein/svd.h:405-428 with LeftDir = -1
     Meta mu, mv;
@@ -1101,16 +1173,90 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
             pv.push_back({s_, 1, ca.pos, ca.len, cl.kept});
         }
     }
-    out.U = DTensor::make(mu, false);
-    out.V = DTensor::make(mv, false);
+    const bool extended = sa && sa->added > 0;
+    out.U = DTensor::make(mu, extended);  // the added states' other side stays zero
+    out.V = DTensor::make(mv, extended);
     if (!mixed) {
         std::vector<SvdScatter> su, svs;
         for (size_t i = 0; i < pu.size(); ++i)
-            su.push_back({out.U->meta.blocks[i].off, pu[i].sector, 0, pu[i].pos, pu[i].len, pu[i].kept, l2r ? 0 : 1});
+            su.push_back({out.U->meta.blocks[i].off, pu[i].sector, 0, pu[i].pos, pu[i].len, kfin[pu[i].sector],
+                          l2r ? 0 : 1, pu[i].kept});
         for (size_t i = 0; i < pv.size(); ++i)
-            svs.push_back({out.V->meta.blocks[i].off, pv[i].sector, 1, pv[i].pos, pv[i].len, pv[i].kept, l2r ? 1 : 0});
+            svs.push_back({out.V->meta.blocks[i].off, pv[i].sector, 1, pv[i].pos, pv[i].len, kfin[pv[i].sector],
+                           l2r ? 1 : 0, pv[i].kept});
         svd_scatter(su, P, Us.as<double2>(), Vs.as<double2>(), S.as<double>(), out.U->data());
         svd_scatter(svs, P, Us.as<double2>(), Vs.as<double2>(), S.as<double>(), out.V->data());
+        if (!extended) return out;
+        // ---- SA: the new directions of the kept side (gs_ortho,
+        // util/allocation.h:260-320).  Each new vector's entries are drawn
+        // uniform(-1, 1) (real) from a fresh generator seeded by the stream;
+        // X = (I - B B^H) R twice and a Cholesky-QR twice give the vectors the
+        // reference's one-at-a-time Gram-Schmidt gives (the Q factor of [B R]
+        // beyond B), to rounding.
+        std::vector<SaSector> sas;
+        std::vector<int64_t> c_off;
+        std::vector<int64_t> x_of_sector(nsec, -1);
+        int64_t b_elems = 0, x_elems = 0, c_elems = 0;
+        for (int s_ = 0; s_ < nsec; ++s_) {
+            if (ext[s_] <= 0) continue;
+            const SvdSector &sc = P.secs[s_];
+            const int n = l2r ? sc.m : sc.n;
+            sas.push_back({b_elems, x_elems, s_, l2r ? 0 : 1, n, kfin[s_], ext[s_]});
+            c_off.push_back(c_elems);
+            x_of_sector[s_] = x_elems;
+            b_elems += (int64_t)n * kfin[s_];
+            x_elems += (int64_t)n * ext[s_];
+            c_elems += (int64_t)kfin[s_] * ext[s_];
+        }
+        std::vector<double2> xr(x_elems);
+        for (auto &a : sas)
+            for (int c = 0; c < a.ext; ++c) {
+                std::mt19937 gen((std::mt19937::result_type)(unsigned int)(*sa->seeds)());
+                std::uniform_real_distribution<double> dis(-1, 1);
+                for (int r = 0; r < a.n; ++r) xr[a.x_off + (int64_t)r * a.ext + c] = make_double2(dis(gen), 0.0);
+            }
+        DevBuf Bd(std::max<int64_t>(1, b_elems) * sizeof(double2)), Cb(std::max<int64_t>(1, c_elems) * sizeof(double2));
+        DevBuf Pb(std::max<int64_t>(1, x_elems) * sizeof(double2));
+        X = DevBuf(std::max<int64_t>(1, x_elems) * sizeof(double2));
+        upload_bytes(X.p, xr.data(), xr.size() * sizeof(double2));
+        sa_basis(sas, P, Us.as<double2>(), Vs.as<double2>(), Bd.as<double2>());
+        GemmPlan proj, back;  // C = B^H X, P = B C
+        std::vector<SvdPolish> pl;
+        int64_t g_elems = 0;
+        for (size_t i = 0; i < sas.size(); ++i) {
+            const SaSector &a = sas[i];
+            add_gemm(proj, c_off[i], a.kept, a.ext, GemmSeg{a.b_off, a.x_off, a.n, a.kept, a.ext, 1, 0});
+            add_gemm(back, a.x_off, a.n, a.ext, GemmSeg{a.b_off, c_off[i], a.kept, a.kept, a.ext, 0, 0});
+            pl.push_back({a.x_off, g_elems, 0, a.sector, a.n, a.ext, a.ext});
+            g_elems += (int64_t)a.ext * a.ext;
+        }
+        proj.upload();
+        back.upload();
+        for (int pass = 0; pass < 2; ++pass) {
+            launch_gemm_fp64(proj, Bd.as<double2>(), X.as<double2>(), Cb.as<double2>(), 1.0, nullptr);
+            launch_gemm_fp64(back, Bd.as<double2>(), Cb.as<double2>(), Pb.as<double2>(), 1.0, nullptr);
+            sa_subtract(X.as<double2>(), Pb.as<double2>(), x_elems);
+        }
+        Gm = DevBuf(std::max<int64_t>(1, g_elems) * sizeof(double2));
+        cst = DevBuf(std::max<size_t>(1, pl.size()) * sizeof(int));
+        cdiag = DevBuf(std::max<size_t>(1, pl.size()) * sizeof(double));
+        KV_CUDA(cudaMemsetAsync(cst.p, 0, std::max<size_t>(1, pl.size()) * sizeof(int), ctx().stream));
+        DevBuf dpl = upload_vec(pl);
+        polish_pass(pl, dpl, 0.0);
+        polish_pass(pl, dpl, 0.0);
+        std::vector<SaOut> so;
+        if (l2r) {
+            for (size_t i = 0; i < pu.size(); ++i)
+                if (ext[pu[i].sector] > 0)
+                    so.push_back({out.U->meta.blocks[i].off, x_of_sector[pu[i].sector], 0, pu[i].pos, pu[i].len,
+                                  kfin[pu[i].sector], ext[pu[i].sector]});
+        } else {
+            for (size_t i = 0; i < pv.size(); ++i)
+                if (ext[pv[i].sector] > 0)
+                    so.push_back({out.V->meta.blocks[i].off, x_of_sector[pv[i].sector], 1, pv[i].pos, pv[i].len,
+                                  kfin[pv[i].sector], ext[pv[i].sector]});
+        }
+        sa_scatter(so, X.as<double2>(), l2r ? out.U->data() : out.V->data());
         return out;
     }
     // ---- mixed mode, part 2: the kept prefix of each sector's X (row stride
@@ -1441,6 +1587,65 @@ void Tdvp::one_site() {
     end_sweep();
 }
 
+void Tdvp::set_sa(const double *beta, int nbeta, unsigned long long seed) {
+    KV_REQUIRE(nbeta >= 0 && (nbeta == 0 || beta), KV_EINVAL, "null width array");
+    sa_beta.assign(beta, beta + nbeta);
+    sa_seeds.seed((std::mt19937::result_type)seed);
+}
+
+// TDVP::sa_site (holstein/tdvp.h:230-294): one_site with the SA split in place
+// of svd_impl; bond i (between sites i and i+1) takes width sa_beta[i]
+void Tdvp::sa_site() {
+    KV_REQUIRE(window_at < 0, KV_EINVAL, "the chain is inside a timed window; it cannot sweep");
+    const int ns = (int)mps.size();
+    KV_REQUIRE((int)sa_beta.size() >= ns - 1, KV_EINVAL, "SA-1TDVP needs one width per bond (kv_tdvp_set_sa)");
+    begin_sweep();
+    sa_added = 0;
+    for (int i = 0; i < ns; ++i) {
+        mps[i] = krylov(1, *envL.back(), *mps[i], mpo[i].get(), nullptr, *envR.back(), false, MOD_EVL1);
+        if (i < ns - 1) {
+            SaParams sp;
+            sp.beta = sa_beta[i];
+            sp.seeds = &sa_seeds;
+            mark(MOD_SVD, true);
+            SvdOut r = op_svd(*mps[i], 2, true, tol_svd, max_dim, precision, &sp);
+            mark(MOD_SVD, false);
+            sa_added += sp.added;
+            mps[i] = r.U;
+            mark(MOD_UPDATE, true);
+            envL.push_back(op_env(true, *envL.back(), *mps[i], *mpo[i], nullptr, precision, &other));
+            mark(MOD_UPDATE, false);
+            TensorP c = krylov(0, *envL.back(), *r.V, nullptr, nullptr, *envR.back(), true, MOD_EVL0);
+            mark(MOD_SWEEP, true);
+            mps[i + 1] = op_product(*c, *mps[i + 1], 1, KV_OP_N, KV_OP_N, precision, &other);
+            mark(MOD_SWEEP, false);
+            envR.pop_back();
+        }
+    }
+    for (int i = ns - 1; i >= 0; --i) {
+        mps[i] = krylov(1, *envL.back(), *mps[i], mpo[i].get(), nullptr, *envR.back(), false, MOD_EVL1);
+        if (i > 0) {
+            SaParams sp;
+            sp.beta = sa_beta[i - 1];
+            sp.seeds = &sa_seeds;
+            mark(MOD_SVD, true);
+            SvdOut r = op_svd(*mps[i], 1, false, tol_svd, max_dim, precision, &sp);
+            mark(MOD_SVD, false);
+            sa_added += sp.added;
+            mps[i] = r.V;
+            mark(MOD_UPDATE, true);
+            envR.push_back(op_env(false, *envR.back(), *mps[i], *mpo[i], mpo_t[i].get(), precision, &other));
+            mark(MOD_UPDATE, false);
+            TensorP c = krylov(0, *envL.back(), *r.U, nullptr, nullptr, *envR.back(), true, MOD_EVL0);
+            mark(MOD_SWEEP, true);
+            mps[i - 1] = op_product(*mps[i - 1], *c, 1, KV_OP_N, KV_OP_N, precision, &other);
+            mark(MOD_SWEEP, false);
+            envL.pop_back();
+        }
+    }
+    end_sweep();
+}
+
 // one local update of TDVP::two_site's left-to-right pass at sites (i, i+1)
 // (holstein/tdvp.h:150-185)
 void Tdvp::two_site_lr(int i) {
@@ -1452,6 +1657,7 @@ void Tdvp::two_site_lr(int i) {
     mark(MOD_SVD, true);
     SvdOut r = op_svd(*mm, 2, true, tol_svd, max_dim, precision);
     mark(MOD_SVD, false);
+    if (svs_on) svs.push_back(r.kept_s);
     if (i < ns - 2) {
         mps[i] = r.U;
         mark(MOD_UPDATE, true);
@@ -1507,6 +1713,7 @@ void Tdvp::two_site() {
         mark(MOD_SVD, true);
         SvdOut r = op_svd(*mm, 2, false, tol_svd, max_dim, precision);
         mark(MOD_SVD, false);
+        if (svs_on) svs.push_back(r.kept_s);
         if (i > 1) {
             mps[i] = r.V;
             mark(MOD_UPDATE, true);

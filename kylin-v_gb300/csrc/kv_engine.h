@@ -1,6 +1,7 @@
 // Host-side engine declarations: plans, operations, TDVP driver.
 #pragma once
 #include <chrono>
+#include <random>
 
 #include "kv_internal.h"
 
@@ -76,7 +77,16 @@ TensorP op_heff(int nsite, const DTensor &L, const DTensor &psi, const DTensor *
 TensorP op_lanczos(int nsite, const DTensor &L, const DTensor &psi, const DTensor *W1, const DTensor *W2,
                    const DTensor &R, double dt, int max_iter, double tol, bool reverse, int precision,
                    KrylovState *st_dev, std::vector<Flops> *per_iter, int *iters_out = nullptr);
-SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int precision);
+// The SA-1TDVP split (sa_svd_impl, holstein/svd.h:443-614): every sector's
+// full SVD is kept and the bond is extended by synthetic states (FP64 SVD in
+// every precision mode).  seeds: the seed stream every random draw's
+// generator is seeded from, in the reference's order of draws.
+struct SaParams {
+    double beta = 1.0;              // width of the quasi-Gaussian draws (betaSet[bond])
+    std::mt19937 *seeds = nullptr;
+    int added = 0;                  // out: states added to the bond
+};
+SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int precision, SaParams *sa = nullptr);
 TensorP op_env(bool l2r, const DTensor &env, const DTensor &A, const DTensor &W, const DTensor *Wt, int precision,
                Flops *fl);
 TensorP op_permute(const DTensor &t, const std::vector<int> &ax);
@@ -124,6 +134,18 @@ class Tdvp {
     ~Tdvp();
     void one_site();
     void two_site();
+    // TDVP::sa_site (holstein/tdvp.h:230-294) with the widths and seed of set_sa
+    void sa_site();
+    void set_sa(const double *beta, int nbeta, unsigned long long seed);
+    std::vector<double> sa_beta;  // one width per bond (betaSet)
+    std::mt19937 sa_seeds;        // seed stream of the SA draws
+    long long sa_added = 0;       // states the SA splits added in the last sweep
+    // the kept singular values (descending) of every two-site split since they
+    // were last read: the record svd_impl appends to the SVS file
+    // (holstein/svd.h:390-402) for the SA stage's fit; kept once svs_on is set
+    // (the first kv_tdvp_svs call on the handle)
+    std::vector<std::vector<double>> svs;
+    bool svs_on = false;
     // n timed local updates of the two-site left-to-right pass from site i0
     // (the pass advanced there first, untimed)
     void window(int i0, int n);

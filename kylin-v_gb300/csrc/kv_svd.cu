@@ -849,7 +849,7 @@ __global__ void __launch_bounds__(256) k_svd_scatter(const SvdScatter *__restric
     for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
         int i, j;  // i: position inside the micro block (row or column), j: kept state
         int64_t dst;
-        if (d.side == 0) { i = (int)(e / d.kept); j = (int)(e % d.kept); dst = e; }
+        if (d.side == 0) { i = (int)(e / d.kept); j = (int)(e % d.kept); dst = (int64_t)i * d.ld + j; }
         else { j = (int)(e / d.len); i = (int)(e % d.len); dst = e; }
         const int r = d.pos + i;
         double2 val;
@@ -865,6 +865,46 @@ __global__ void __launch_bounds__(256) k_svd_scatter(const SvdScatter *__restric
             val.y *= sj;
         }
         out[d.out_off + dst] = val;
+    }
+}
+
+// SA-1TDVP: B[r, j] = U_A[r, j] (side 0) or conj(V_A[r, j]) (side 1), the
+// sources k_svd_scatter reads
+__global__ void __launch_bounds__(256) k_sa_basis(const SaSector *__restrict__ sa, const SvdSector *__restrict__ secs,
+                                                  const double2 *__restrict__ Us, const double2 *__restrict__ Vs,
+                                                  double2 *__restrict__ B) {
+    const SaSector d = sa[blockIdx.x];
+    const SvdSector s = secs[d.sector];
+    for (int64_t e = threadIdx.x; e < (int64_t)d.n * d.kept; e += blockDim.x) {
+        const int r = (int)(e / d.kept), j = (int)(e % d.kept);
+        double2 v;
+        if (d.side == 0) {
+            v = s.transposed ? Vs[s.v_off + (int64_t)j * s.q + r] : Us[s.t_off + (int64_t)j * s.p + r];
+        } else {
+            v = s.transposed ? Us[s.t_off + (int64_t)j * s.p + r] : Vs[s.v_off + (int64_t)j * s.q + r];
+            v.y = -v.y;
+        }
+        B[d.b_off + e] = v;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_sa_subtract(double2 *__restrict__ x, const double2 *__restrict__ y,
+                                                     int64_t n) {
+    for (int64_t i = blockIdx.x * 256ll + threadIdx.x; i < n; i += (int64_t)gridDim.x * 256) {
+        x[i].x -= y[i].x;
+        x[i].y -= y[i].y;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_sa_scatter(const SaOut *__restrict__ v, const double2 *__restrict__ X,
+                                                    double2 *__restrict__ out) {
+    const SaOut d = v[blockIdx.x];
+    const int ld = d.kept + d.ext;
+    for (int64_t e = threadIdx.x; e < (int64_t)d.len * d.ext; e += blockDim.x) {
+        const int i = (int)(e / d.ext), c = (int)(e % d.ext);
+        const double2 x = X[d.x_off + (int64_t)(d.pos + i) * d.ext + c];
+        if (d.side == 0) out[d.out_off + (int64_t)i * ld + d.kept + c] = x;
+        else out[d.out_off + (int64_t)(d.kept + c) * d.len + i] = x;
     }
 }
 
@@ -956,6 +996,30 @@ void svd_scatter(const std::vector<SvdScatter> &sc, const SvdPlan &p, const doub
     DevBuf d = upload_vec(sc);
     k_svd_scatter<<<(unsigned)sc.size(), 256, 0, ctx().stream>>>(d.as<SvdScatter>(), p.d_secs.as<SvdSector>(), Us,
                                                                   Vs, S, out);
+    counted();
+    KV_CUDA(cudaGetLastError());
+}
+
+void sa_basis(const std::vector<SaSector> &v, const SvdPlan &p, const double2 *Us, const double2 *Vs, double2 *B) {
+    if (v.empty()) return;
+    DevBuf d = upload_vec(v);
+    k_sa_basis<<<(unsigned)v.size(), 256, 0, ctx().stream>>>(d.as<SaSector>(), p.d_secs.as<SvdSector>(), Us, Vs, B);
+    counted();
+    KV_CUDA(cudaGetLastError());
+}
+
+void sa_subtract(double2 *x, const double2 *y, int64_t n) {
+    if (n <= 0) return;
+    const unsigned grid = (unsigned)std::min<int64_t>((n + 255) / 256, 4 * ctx().num_sms);
+    k_sa_subtract<<<grid, 256, 0, ctx().stream>>>(x, y, n);
+    counted();
+    KV_CUDA(cudaGetLastError());
+}
+
+void sa_scatter(const std::vector<SaOut> &v, const double2 *X, double2 *out) {
+    if (v.empty()) return;
+    DevBuf d = upload_vec(v);
+    k_sa_scatter<<<(unsigned)v.size(), 256, 0, ctx().stream>>>(d.as<SaOut>(), X, out);
     counted();
     KV_CUDA(cudaGetLastError());
 }

@@ -22,6 +22,22 @@ struct SvdGather {  // one block of A into its sector matrix
 struct SvdScatter {  // one output block of U (side 0) or S.V^H / V^H (side 1)
     int64_t out_off;
     int sector, side, pos, len, kept, scale_s;
+    int ld;  // side 0: the block's row length (>= kept; larger where SA-1TDVP adds columns)
+};
+
+// SA-1TDVP bond extension of one sector (holstein/svd.h:562-600): the kept
+// vectors of the extended side as a dense row-major basis B (n x kept;
+// side 0: U's columns, side 1: V^H's rows as vectors) and the new vectors X
+// (n x ext, row-major)
+struct SaSector {
+    int64_t b_off, x_off;
+    int sector, side, n, kept, ext;
+};
+// one output block's share of the new vectors: side 0 columns kept.. of a U
+// block (rows pos.. of the sector), side 1 rows kept.. of a V^H block
+struct SaOut {
+    int64_t out_off, x_off;
+    int side, pos, len, kept, ext;
 };
 
 struct SvdPlan {
@@ -76,5 +92,10 @@ void svd_jacobi(const SvdPlan &p, double2 *T, double2 *V, int *status, int max_s
 void svd_finalize(const SvdPlan &p, const double2 *T, const double2 *V, double2 *Us, double2 *Vs, double *S);
 void svd_scatter(const std::vector<SvdScatter> &sc, const SvdPlan &p, const double2 *Us, const double2 *Vs,
                  const double *S, double2 *out);
+// FP64 path: the kept vectors of each SA sector into B (after svd_finalize)
+void sa_basis(const std::vector<SaSector> &v, const SvdPlan &p, const double2 *Us, const double2 *Vs, double2 *B);
+// x -= y over n elements
+void sa_subtract(double2 *x, const double2 *y, int64_t n);
+void sa_scatter(const std::vector<SaOut> &v, const double2 *X, double2 *out);
 
 }  // namespace kv

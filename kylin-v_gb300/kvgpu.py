@@ -32,7 +32,8 @@ EXPORTS = (
     "kv_svd_truncate", "kv_tdvp_create", "kv_tdvp_sweep", "kv_tdvp_site", "kv_tdvp_stats", "kv_tdvp_free",
     "kv_expectation", "kv_profile", "kv_profile_read", "kv_counters", "kv_expectation_noalloc",
     "kv_tdvp_host_stats", "kv_canonicalize", "kv_sweep_batched", "kv_adjoint_heff", "kv_adjoint_env",
-    "kv_debug_gemm_stall", "kv_debug_pool_usage", "kv_svd_stats", "kv_krylov_stats", "kv_tdvp_window", "kv_local_expectations",
+    "kv_debug_gemm_stall", "kv_debug_pool_usage", "kv_svd_stats", "kv_krylov_stats", "kv_tdvp_set_sa",
+    "kv_tdvp_svs", "kv_tdvp_window", "kv_local_expectations",
 )
 
 
@@ -92,6 +93,8 @@ def lib():
         ll = ctypes.POINTER(ctypes.c_longlong)
         L.kv_svd_stats.argtypes = [ctypes.c_int, ll, ll, ll, ll, ip]
         L.kv_krylov_stats.argtypes = [ctypes.c_int, ll, ll, ll]
+        L.kv_tdvp_set_sa.argtypes = [vp, dp, ctypes.c_int, ctypes.c_ulonglong, ll]
+        L.kv_tdvp_svs.argtypes = [vp, ip, ll, ip, dp]
         L.kv_debug_pool_usage.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_longlong),
                                           ctypes.POINTER(ctypes.c_longlong)]
         _lib = L
@@ -351,8 +354,34 @@ class TDVP:
         check(lib().kv_tdvp_sweep(self.ptr, 0))
 
     def sweep(self, mode: int):
-        """mode 0: global_krylov, 1: one_site, 2: two_site."""
+        """mode 0: global_krylov, 1: one_site, 2: two_site, 3: sa_site (set_sa first)."""
         check(lib().kv_tdvp_sweep(self.ptr, mode))
+
+    def set_sa(self, betas, seed: int):
+        """SA-1TDVP widths per bond (betaSet, holstein/tdvp.h:343-358) and the
+        seed of the stream every SA draw's generator is seeded from."""
+        b = (ctypes.c_double * max(1, len(betas)))(*[float(x) for x in betas])
+        check(lib().kv_tdvp_set_sa(self.ptr, b, len(betas), int(seed), None))
+
+    def svs(self) -> list:
+        """Kept singular values (descending) of every two-site split since the
+        last call (the SVS record of holstein/svd.h:390-402), then cleared."""
+        nr, nv = ctypes.c_int(), ctypes.c_longlong()
+        check(lib().kv_tdvp_svs(self.ptr, ctypes.byref(nr), ctypes.byref(nv), None, None))
+        counts = (ctypes.c_int * max(1, nr.value))()
+        vals = (ctypes.c_double * max(1, nv.value))()
+        check(lib().kv_tdvp_svs(self.ptr, None, None, counts, vals))
+        out, k = [], 0
+        for i in range(nr.value):
+            out.append([vals[k + j] for j in range(counts[i])])
+            k += counts[i]
+        return out
+
+    def sa_added(self) -> int:
+        """States the SA splits of the last SA sweep added."""
+        n = ctypes.c_longlong()
+        check(lib().kv_tdvp_set_sa(self.ptr, None, 0, 0, ctypes.byref(n)))
+        return n.value
 
     def window(self, i0: int, n: int):
         """n timed two-site local updates of the left-to-right pass from site

@@ -16,7 +16,8 @@
  *   ops:     kvo_product, kvo_apply_zero/single/double, kvo_env_sweep,
  *            kvo_local_krylov, kvo_svd
  *   sweep:   kvo_tdvp_new / kvo_tdvp_sweep (mode 0: one global-Krylov step,
- *            1: one_site, 2: two_site) / kvo_tdvp_site / kvo_tdvp_free;
+ *            1: one_site, 2: two_site, 3: one SA-1TDVP sweep with the widths
+ *            and seed of kvo_tdvp_set_sa) / kvo_tdvp_site / kvo_tdvp_free;
  *            kvo_tdvp_window times a window of two-site local updates
  *            (CPU-baseline timing)
  *   observable: kvo_join
@@ -31,6 +32,7 @@
 #include <cstring>
 #include <map>
 #include <numeric>
+#include <random>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -502,6 +504,234 @@ SvdResult svd_impl(const Tensor &A, int r1, bool l2r, double thres, int max_dim)
     return out;
 }
 
+// ------------------------------------------------------------ SA-1TDVP SVD
+// The reference seeds a fresh mt19937 from std::random_device before every
+// group of draws (one synthetic value; one new vector), a different sequence
+// every run.  Here each group's mt19937 is seeded by the next value of a seed
+// stream (an mt19937 seeded by the caller), the order of
+// oracle/shim/seeded_device.h, under which the compiled reference repeats
+// the same run: golden SA trajectories come from it.
+
+// quasi-Gaussian density and its inversion by bisection on [0, 2]
+// (util/allocation.h:232-256), written as the reference writes them
+double quasi_gauss(double x, double bet) {
+    double r = std::exp(-0.25 * bet * std::pow(x, 2.0)) * std::abs(0.25 * x / bet);
+    r += (0.5 / bet - 0.25 * std::pow(x, 2.0)) * std::erfc(0.5 * std::pow(bet, 0.5) * std::abs(x)) * 0.5 *
+         std::pow(3.1415926 / bet, 0.5);
+    r *= std::exp(-0.25 * bet * std::pow(x, 2.0)) * 4.0 * bet * std::pow(bet / 3.1415926, 0.5);
+    return r;
+}
+
+double inv_quasi_gauss(double y, double bet) {
+    double hi = 2.0, lo = 0.0, res = 0.0;
+    while (hi - lo > 1e-8) {
+        res = 0.5 * (hi + lo);
+        if ((quasi_gauss(res, bet) - y) * (quasi_gauss(lo, bet) - y) < 0) hi = res;
+        else lo = res;
+    }
+    return res;
+}
+
+// Number of synthetic states sa_svd_impl adds (holstein/svd.h:525-560): the
+// sorted spectrum's tail is continued by s_new = 10^(+-r) s_last^2 / s_prev,
+// r = inv_quasi_gauss(u, beta), sign alternating, clamped to non-increasing,
+// until a value falls to the threshold or the spectrum reaches max_dim; only
+// for spectra with 5 < n < max_dim values.
+int sa_added(const std::vector<double> &sorted_desc, int max_dim, double thres, double beta, std::mt19937 &seeds) {
+    const int n = (int)sorted_desc.size();
+    if (n < 2) return 0;
+    std::vector<double> t = {sorted_desc[n - 2], sorted_desc[n - 1]};
+    int added = 0;
+    if (n < max_dim && n > 5) {
+        for (int i = n; i < max_dim; ++i) {
+            std::mt19937 gen{(std::mt19937::result_type)(unsigned int)seeds()};
+            std::uniform_real_distribution<double> d(0, 1);
+            const double rds = inv_quasi_gauss(d(gen), beta);
+            const double f = (i + n) % 2 == 0 ? std::pow(10, rds) : std::pow(10, -1.0 * rds);
+            t.push_back(f * std::pow(t[t.size() - 1], 2.0) / t[t.size() - 2]);
+            if (t.back() <= thres) {
+                t.pop_back();
+                break;
+            }
+            if (t.back() > t[t.size() - 2]) t.back() = t[t.size() - 2];
+            added = (int)t.size() - 2;
+        }
+    }
+    return added;
+}
+
+// gs_ortho (util/allocation.h:260-320) on a row-major matrix a (nrow x ncol):
+// extend_rows appends `inc` rows, else `inc` columns; fill_zero leaves them 0,
+// else each new vector is drawn uniform(-1, 1) (real parts), normalised,
+// orthogonalised one after another against every earlier vector (modified
+// Gram-Schmidt, zdotc / zaxpy) and normalised again.
+void gs_ortho(int nrow, int ncol, std::vector<cplx> &a, bool extend_rows, int inc, bool fill_zero,
+              std::mt19937 &seeds) {
+    if (extend_rows) {
+        std::vector<cplx> b((size_t)(nrow + inc) * ncol, cplx(0.0, 0.0));
+        std::copy(a.begin(), a.begin() + (size_t)nrow * ncol, b.begin());
+        a.swap(b);
+        if (fill_zero) return;
+        auto row = [&](int r) { return a.data() + (size_t)r * ncol; };
+        for (int i = 0; i < inc; ++i) {
+            std::mt19937 gen((std::mt19937::result_type)(unsigned int)seeds());
+            std::uniform_real_distribution<double> dis(-1, 1);
+            cplx *v = row(nrow + i);
+            for (int k = 0; k < ncol; ++k) v[k] = dis(gen);
+            double nrm = 0.0;
+            for (int k = 0; k < ncol; ++k) nrm += std::norm(v[k]);
+            nrm = std::sqrt(nrm);
+            for (int k = 0; k < ncol; ++k) v[k] *= 1.0 / nrm;
+            for (int j = 0; j < nrow + i; ++j) {
+                cplx d(0.0, 0.0);
+                for (int k = 0; k < ncol; ++k) d += std::conj(row(j)[k]) * v[k];
+                for (int k = 0; k < ncol; ++k) v[k] -= d * row(j)[k];
+            }
+            nrm = 0.0;
+            for (int k = 0; k < ncol; ++k) nrm += std::norm(v[k]);
+            nrm = std::sqrt(nrm);
+            for (int k = 0; k < ncol; ++k) v[k] *= 1.0 / nrm;
+        }
+    } else {
+        const int ld = ncol + inc;
+        std::vector<cplx> b((size_t)nrow * ld, cplx(0.0, 0.0));
+        for (int r = 0; r < nrow; ++r)
+            for (int c = 0; c < ncol; ++c) b[(size_t)r * ld + c] = a[(size_t)r * ncol + c];
+        a.swap(b);
+        if (fill_zero) return;
+        auto at = [&](int r, int c) -> cplx & { return a[(size_t)r * ld + c]; };
+        for (int i = 0; i < inc; ++i) {
+            std::mt19937 gen((std::mt19937::result_type)(unsigned int)seeds());
+            std::uniform_real_distribution<double> dis(-1, 1);
+            const int c = ncol + i;
+            for (int r = 0; r < nrow; ++r) at(r, c) = dis(gen);
+            double nrm = 0.0;
+            for (int r = 0; r < nrow; ++r) nrm += std::norm(at(r, c));
+            nrm = std::sqrt(nrm);
+            for (int r = 0; r < nrow; ++r) at(r, c) *= 1.0 / nrm;
+            for (int j = 0; j < c; ++j) {
+                cplx d(0.0, 0.0);
+                for (int r = 0; r < nrow; ++r) d += std::conj(at(r, j)) * at(r, c);
+                for (int r = 0; r < nrow; ++r) at(r, c) -= d * at(r, j);
+            }
+            nrm = 0.0;
+            for (int r = 0; r < nrow; ++r) nrm += std::norm(at(r, c));
+            nrm = std::sqrt(nrm);
+            for (int r = 0; r < nrow; ++r) at(r, c) *= 1.0 / nrm;
+        }
+    }
+}
+
+// sa_svd_impl (holstein/svd.h:443-614): every sector's full SVD is kept (no
+// truncation); if the spectrum is short of max_dim, sa_added states are given
+// to the sectors in order, each taking as many as its kept side has room for:
+// new orthonormal directions on the kept side (U for left-to-right, V^H
+// for right-to-left), zero rows / columns on the other, so the state is
+// unchanged and only the bond grows.
+SvdResult sa_svd_impl(const Tensor &A, int r1, bool l2r, double thres, int max_dim, double beta,
+                      std::mt19937 &seeds) {
+    const int rank = A.rank;
+    std::vector<Macro> rows, cols;
+    for (int k = 0; k < (int)A.blocks.size(); ++k) {
+        const Block &b = A.blocks[k];
+        int qr = 0, qc = 0;
+        for (int i = 0; i < r1; ++i) qr += b.qn[i] * A.dirs[i];
+        for (int i = r1; i < rank; ++i) qc += b.qn[i] * A.dirs[i];
+        fill_side(rows, qr, b, 0, r1, k);
+        fill_side(cols, qc, b, r1, rank, k);
+    }
+    struct Sector { int r, c, m, n, ldu; std::vector<cplx> U, Vt; };
+    std::vector<Sector> secs;
+    std::vector<double> svals;
+    for (int ri = 0; ri < (int)rows.size(); ++ri)
+        for (int ci = 0; ci < (int)cols.size(); ++ci) {
+            Macro &rw = rows[ri], &cl = cols[ci];
+            if (rw.q + cl.q != 0) continue;
+            const int m = rw.len, n = cl.len, ldu = std::min(m, n);
+            rw.kept = ldu;
+            cl.kept = ldu;
+            std::vector<cplx> Ar((size_t)m * n, cplx(0.0, 0.0));
+            for (auto &ra : rw.subs)
+                for (auto &ca : cl.subs)
+                    for (int x : ra.idx)
+                        for (int y : ca.idx) {
+                            if (x != y) continue;
+                            const Block &b = A.blocks[x];
+                            for (int i = 0; i < ra.len; ++i)
+                                for (int j = 0; j < ca.len; ++j)
+                                    Ar[(size_t)(ra.pos + i) * n + ca.pos + j] = b.data[(size_t)i * ca.len + j];
+                        }
+            Sector s{ri, ci, m, n, ldu, std::vector<cplx>((size_t)m * ldu), std::vector<cplx>((size_t)ldu * n)};
+            std::vector<double> sv(ldu), sup(std::max(1, ldu - 1));
+            if (scipy_LAPACKE_zgesvd(kRowMajor, 'S', 'S', m, n, Ar.data(), n, sv.data(), s.U.data(), ldu,
+                                     s.Vt.data(), n, sup.data()) != 0)
+                throw std::runtime_error("zgesvd failed");
+            for (int i = 0; i < ldu; ++i) {
+                if (l2r) for (int j = 0; j < n; ++j) s.Vt[(size_t)i * n + j] *= sv[i];
+                else for (int j = 0; j < m; ++j) s.U[(size_t)j * ldu + i] *= sv[i];
+                svals.push_back(sv[i]);
+            }
+            secs.push_back(std::move(s));
+        }
+    std::sort(svals.begin(), svals.end(), std::greater<double>());
+    SvdResult out;
+    out.total = (int)svals.size();
+    int add = sa_added(svals, max_dim, thres, beta, seeds);
+    for (auto &s : secs) {
+        Macro &rw = rows[s.r], &cl = cols[s.c];
+        if (rw.kept <= 0 || cl.kept <= 0 || add == 0) continue;
+        const int room = l2r ? rw.len - rw.kept : cl.len - cl.kept;
+        if (room <= 0) continue;
+        const int a = std::min(add, room);
+        if (l2r) {
+            gs_ortho(s.m, rw.kept, s.U, false, a, false, seeds);
+            gs_ortho(cl.kept, s.n, s.Vt, true, a, true, seeds);
+        } else {
+            gs_ortho(s.m, rw.kept, s.U, false, a, true, seeds);
+            gs_ortho(cl.kept, s.n, s.Vt, true, a, false, seeds);
+        }
+        rw.kept += a;
+        cl.kept += a;
+        s.ldu += a;
+        add -= a;
+    }
+    out.kept_s = svals;
+    const int left_dir = -1;
+    out.U.rank = r1 + 1;
+    out.V.rank = rank - r1 + 1;
+    for (int i = 0; i < r1; ++i) out.U.dirs[i] = A.dirs[i];
+    out.U.dirs[r1] = left_dir;
+    out.V.dirs[0] = -left_dir;
+    for (int i = r1; i < rank; ++i) out.V.dirs[i - r1 + 1] = A.dirs[i];
+    for (auto &s : secs) {
+        Macro &rw = rows[s.r], &cl = cols[s.c];
+        if (rw.kept <= 0 || cl.kept <= 0) continue;
+        for (auto &ra : rw.subs) {  // redist_row
+            Block b;
+            b.rank = r1 + 1;
+            for (int i = 0; i < r1; ++i) { b.shape[i] = ra.shape[i]; b.qn[i] = ra.qn[i]; }
+            b.shape[r1] = rw.kept;
+            b.qn[r1] = -left_dir * rw.q;
+            b.data.resize((size_t)ra.len * rw.kept);
+            for (int i = 0; i < ra.len; ++i)
+                for (int j = 0; j < rw.kept; ++j) b.data[(size_t)i * rw.kept + j] = s.U[(size_t)(ra.pos + i) * s.ldu + j];
+            out.U.push_merge(b);
+        }
+        for (auto &ca : cl.subs) {  // redist_col
+            Block b;
+            b.rank = rank - r1 + 1;
+            b.shape[0] = cl.kept;
+            b.qn[0] = left_dir * cl.q;
+            for (int i = 0; i < rank - r1; ++i) { b.shape[i + 1] = ca.shape[i]; b.qn[i + 1] = ca.qn[i]; }
+            b.data.resize((size_t)ca.len * cl.kept);
+            for (int j = 0; j < cl.kept; ++j)
+                for (int c = 0; c < ca.len; ++c) b.data[(size_t)j * ca.len + c] = s.Vt[(size_t)j * s.n + ca.pos + c];
+            out.V.push_merge(b);
+        }
+    }
+    return out;
+}
+
 // --------------------------------------------------------------- TDVP
 struct Tdvp {
     std::vector<Tensor> mps, mpo;
@@ -509,6 +739,8 @@ struct Tdvp {
     double tol_svd, tol_exp, dt;
     int max_dim, max_iter;
     int window_at = -1;  // two-site L->R pass advanced to this site by kvo_tdvp_window (-1: not started)
+    std::vector<double> sa_beta;  // SA-1TDVP widths per bond (kvo_tdvp_set_sa)
+    std::mt19937 sa_seeds;        // the seed stream of the SA draws
 };
 
 Tensor boundary(int rank3_dirs0, int q) {
@@ -550,6 +782,35 @@ void one_site(Tdvp &s) {
         local_krylov(1, s.envL.back(), s.mps[i], &s.mpo[i], nullptr, s.envR.back(), s.dt, s.max_iter, s.tol_exp, false);
         if (i > 0) {
             SvdResult r = svd_impl(s.mps[i], 1, false, s.tol_svd, s.max_dim);
+            s.mps[i] = std::move(r.V);
+            s.envR.push_back(env_sweep(s.envR.back(), s.mps[i], s.mpo[i], false));
+            local_krylov(0, s.envL.back(), r.U, nullptr, nullptr, s.envR.back(), s.dt, s.max_iter, s.tol_exp, true);
+            s.mps[i - 1] = product(s.mps[i - 1], r.U, 1, OP_N, OP_N);
+            s.envL.pop_back();
+        }
+    }
+}
+
+// TDVP::sa_site (holstein/tdvp.h:230-294): one_site with sa_svd_impl in
+// place of svd_impl, bond i taking width beta[i]
+void sa_site(Tdvp &s) {
+    const int ns = (int)s.mps.size();
+    if ((int)s.sa_beta.size() < ns - 1) throw std::runtime_error("SA-1TDVP needs one width per bond");
+    for (int i = 0; i < ns; ++i) {
+        local_krylov(1, s.envL.back(), s.mps[i], &s.mpo[i], nullptr, s.envR.back(), s.dt, s.max_iter, s.tol_exp, false);
+        if (i < ns - 1) {
+            SvdResult r = sa_svd_impl(s.mps[i], 2, true, s.tol_svd, s.max_dim, s.sa_beta[i], s.sa_seeds);
+            s.mps[i] = std::move(r.U);
+            s.envL.push_back(env_sweep(s.envL.back(), s.mps[i], s.mpo[i], true));
+            local_krylov(0, s.envL.back(), r.V, nullptr, nullptr, s.envR.back(), s.dt, s.max_iter, s.tol_exp, true);
+            s.mps[i + 1] = product(r.V, s.mps[i + 1], 1, OP_N, OP_N);
+            s.envR.pop_back();
+        }
+    }
+    for (int i = ns - 1; i >= 0; --i) {
+        local_krylov(1, s.envL.back(), s.mps[i], &s.mpo[i], nullptr, s.envR.back(), s.dt, s.max_iter, s.tol_exp, false);
+        if (i > 0) {
+            SvdResult r = sa_svd_impl(s.mps[i], 1, false, s.tol_svd, s.max_dim, s.sa_beta[i - 1], s.sa_seeds);
             s.mps[i] = std::move(r.V);
             s.envR.push_back(env_sweep(s.envR.back(), s.mps[i], s.mpo[i], false));
             local_krylov(0, s.envL.back(), r.U, nullptr, nullptr, s.envR.back(), s.dt, s.max_iter, s.tol_exp, true);
@@ -1048,7 +1309,18 @@ int kvo_tdvp_sweep(void *h, int mode) {
         if (mode == 1) one_site(*s);
         else if (mode == 2) two_site(*s);
         else if (mode == 0) global_step(*s);
-        else throw std::runtime_error("mode must be 0, 1 or 2");
+        else if (mode == 3) sa_site(*s);
+        else throw std::runtime_error("mode must be 0, 1, 2 or 3");
+    });
+}
+
+// SA-1TDVP widths (one per bond: beta, as betaSet holds it) and the seed of
+// the generator every SA draw comes from
+int kvo_tdvp_set_sa(void *h, const double *beta, int nbeta, unsigned long long seed) {
+    return guarded([&] {
+        auto *s = static_cast<Tdvp *>(h);
+        s->sa_beta.assign(beta, beta + nbeta);
+        s->sa_seeds.seed((std::mt19937::result_type)seed);
     });
 }
 

@@ -50,6 +50,7 @@ def lib():
                                    ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                    ctypes.POINTER(vp)]
         L.kvo_tdvp_sweep.argtypes = [vp, ctypes.c_int]
+        L.kvo_tdvp_set_sa.argtypes = [vp, dp, ctypes.c_int, ctypes.c_ulonglong]
         L.kvo_tdvp_window.argtypes = [vp, ctypes.c_int, ctypes.c_int, dp]
         L.kvo_tdvp_site.argtypes = [vp, ctypes.c_int, ctypes.POINTER(vp)]
         L.kvo_tdvp_free.argtypes = [vp]
@@ -185,7 +186,15 @@ class Tdvp:
         return sec.value
 
     def sweep(self, mode):
+        """mode 0: one global-Krylov step, 1: one_site, 2: two_site, 3: sa_site
+        (widths and seed from set_sa)."""
         _check(lib().kvo_tdvp_sweep(self.ptr, mode))
+
+    def set_sa(self, betas, seed):
+        """SA-1TDVP widths per bond (betaSet of holstein/tdvp.h:343-358) and
+        the seed of the generator every SA draw comes from."""
+        b = (ctypes.c_double * len(betas))(*[float(x) for x in betas])
+        _check(lib().kvo_tdvp_set_sa(self.ptr, b, len(betas), int(seed)))
 
     def mps(self):
         out = []

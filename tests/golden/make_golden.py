@@ -52,12 +52,13 @@ def cases():
     return {
         # 3 molecules x 1 mode, cutoff 4: 9 sites
         "tiny1": dict(chain=HolsteinChain(3, [1.0], [[1.0], [0.8], [1.2]], cutoff=4, eps=[0.1, -0.2, 0.3]),
-                      D=8, seed=11, ops_sites=[1, 4], traj=[("[0,0,0,4]", 8, 1e-8), ("[0,3,0,0]", 8, 1e-8), ("[3,0,0,0]", 8, 1e-8)],
+                      D=8, seed=11, ops_sites=[1, 4], traj=[("[0,0,0,4]", 8, 1e-8), ("[0,3,0,0]", 8, 1e-8), ("[3,0,0,0]", 8, 1e-8),
+                            ("[0,2,2,0]", 16, 1e-8)],
                       keep_inputs=True),
         # 2 molecules x 2 modes, cutoff 3: 10 sites
         "tiny2m": dict(chain=HolsteinChain(2, [1.0, 0.4], [[1.0, 0.6], [0.9, 0.5]], cutoff=3),
                        D=10, seed=12, ops_sites=[2, 6], traj=[("[0,0,0,3]", 10, 1e-8), ("[0,3,0,0]", 10, 1e-8),
-                                                          ("[2,0,0,0]", 10, 1e-8)],
+                                                          ("[2,0,0,0]", 10, 1e-8), ("[0,2,2,0]", 20, 1e-8)],
                        keep_inputs=True),
         # the 1-site benchmark shape: L=8, 1 mode, cutoff 8, D=32, 20 steps
         "l8c8d32": dict(chain=HolsteinChain(8, [1.0], [[1.0]] * 8, cutoff=8), D=32, seed=1234, ops_sites=[7],
@@ -74,19 +75,45 @@ def cases():
     }
 
 
+SA_SEED = 7  # seed of the SA stage's draws (oracle/shim/seeded_device.h)
+
+
 def trajectory(ch, work, out, stage, maxd, tol, dens):
     """Run the reference TDVP driver on work/in.mps, work/H.mpo and write
-    out/traj_<stage>.txt; returns the manifest entry."""
+    out/traj_<stage>.txt; returns the manifest entry.
+
+    A stage with SA-1TDVP sweeps runs the driver built with the seeded
+    random_device (kv_ref_tdvp_sa, KV_SA_SEED = SA_SEED) and the reference's
+    own fit script bin/nls.py on PATH, as total_start calls it; the singular-
+    value log it fits (SVS) and the widths it wrote (beta) are kept beside the
+    trajectory."""
     for f in os.listdir(os.path.join(work, "State")):
         os.remove(os.path.join(work, "State", f))
-    txt = run([os.path.join(REF_BIN, "kv_ref_tdvp"), "-w", "in.mps", "-o", "H.mpo", "-s", stage,
-               "-v", "0.05", "-D", str(maxd), "-t", str(tol), "-k", "11", "-e", "1e-8",
-               "-d", ",".join(os.path.basename(p) for p in dens)], work)
     tag = stage.strip("[]").replace(",", "_")
+    sa = int(stage.strip("[]").split(",")[2]) > 0
+    env = None
+    tool = "kv_ref_tdvp"
+    if sa:
+        tool = "kv_ref_tdvp_sa"
+        ref = os.environ.get("KYLINV_REFERENCE", "/root/reference")
+        wrap = os.path.join(work, "bin")
+        os.makedirs(wrap, exist_ok=True)
+        with open(os.path.join(wrap, "nls.py"), "w") as f:
+            f.write(f"#!/bin/sh\nexec {sys.executable} {os.path.join(ref, 'bin', 'nls.py')} \"$@\"\n")
+        os.chmod(os.path.join(wrap, "nls.py"), 0o755)
+        env = dict(os.environ, PATH=wrap + os.pathsep + os.environ["PATH"], KV_SA_SEED=str(SA_SEED))
+    txt = run([os.path.join(REF_BIN, tool), "-w", "in.mps", "-o", "H.mpo", "-s", stage,
+               "-v", "0.05", "-D", str(maxd), "-t", str(tol), "-k", "11", "-e", "1e-8",
+               "-d", ",".join(os.path.basename(p) for p in dens)], work, env)
     with open(os.path.join(out, f"traj_{tag}.txt"), "w") as f:
         f.write(f"# stage {stage} dt 0.05 maxD {maxd} tolSVD {tol} maxIter 11 tolExp 1e-8\n")
         f.write(txt)
-    return {"stage": stage, "maxD": maxd, "tol_svd": tol, "file": f"traj_{tag}.txt"}
+    entry = {"stage": stage, "maxD": maxd, "tol_svd": tol, "file": f"traj_{tag}.txt"}
+    if sa:
+        shutil.copy(os.path.join(work, "beta"), os.path.join(out, f"beta_{tag}.txt"))
+        shutil.copy(os.path.join(work, "SVS"), os.path.join(out, f"svs_{tag}.txt"))
+        entry.update({"sa_seed": SA_SEED, "beta": f"beta_{tag}.txt", "svs": f"svs_{tag}.txt"})
+    return entry
 
 
 def add_missing_trajectories():
@@ -127,8 +154,8 @@ def add_missing_trajectories():
         json.dump(manifest, f, indent=1)
 
 
-def run(cmd, cwd):
-    r = subprocess.run(cmd, cwd=cwd, capture_output=True, text=True)
+def run(cmd, cwd, env=None):
+    r = subprocess.run(cmd, cwd=cwd, capture_output=True, text=True, env=env)
     if r.returncode != 0:
         raise RuntimeError(f"{cmd}: {r.stdout}\n{r.stderr}")
     return r.stdout

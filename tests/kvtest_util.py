@@ -70,7 +70,24 @@ def read_traj(path):
 def stage_modes(stage: str) -> list:
     """Sweep modes of a total_start stage string [nK, n2TDVP, nSA, n1TDVP]
     (holstein/tdvp.h:297-385) in the order the driver runs them: 0 = one
-    global-Krylov step, 2 = two_site, 1 = one_site (the SA stage is not built)."""
+    global-Krylov step, 2 = two_site, 3 = sa_site, 1 = one_site."""
     nk, n2, nsa, n1 = (int(x) for x in stage.strip("[]").split(","))
-    assert nsa == 0, "the SA-1TDVP stage is not built"
-    return [0] * nk + [2] * n2 + [1] * n1
+    return [0] * nk + [2] * n2 + [3] * nsa + [1] * n1
+
+
+def sa_betas(case: str, tr: dict):
+    """betaSet of a golden SA trajectory (holstein/tdvp.h:343-358): 1 / the
+    value on every line longer than 3 characters of the beta file the
+    reference's fit wrote; None for a trajectory without an SA stage."""
+    if "beta" not in tr:
+        return None
+    with open(os.path.join(GOLDEN, case, tr["beta"])) as f:
+        return [1.0 / float(line) for line in f if len(line.rstrip("\n")) > 3]
+
+
+def prepare_sa(t, case: str, tr: dict):
+    """Give a TDVP handle (GPU or oracle) the widths and seed of a golden SA
+    trajectory; nothing for other trajectories."""
+    b = sa_betas(case, tr)
+    if b is not None:
+        t.set_sa(b, tr["sa_seed"])

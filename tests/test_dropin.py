@@ -63,3 +63,47 @@ def test_dropin_driver_matches_library(tmp_path):
         assert len(got) == len(want)
         for a, b in zip(got, want):
             assert U.tensor_diff(a, b) < 1e-12
+
+
+@pytest.mark.gpu
+def test_dropin_sa_stage(tmp_path):
+    """total_start with an SA-1TDVP stage through the C++ layer: the two-site
+    sweeps write the SVS log, `nls.py` on PATH (this package's restatement of
+    the reference's fit) writes beta, and the SA sweeps' checkpoints equal the
+    library's own SA sweeps with those widths and the same seed.  The fitted
+    widths match the ones the reference's fit wrote for the same chain."""
+    exe = tmp_path / "dropin_driver"
+    r = subprocess.run([_cxx(), "-std=c++17", "-O1", os.path.join(ROOT, "tests", "dropin_driver.cpp"),
+                        "-I" + os.path.join(ROOT, "include"), "-o", str(exe), "-L" + LIBDIR, "-lkvgpu",
+                        "-Wl,-rpath," + LIBDIR], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    import sys
+
+    bindir = tmp_path / "bin"
+    bindir.mkdir()
+    fit = bindir / "nls.py"
+    fit.write_text(f"#!/bin/sh\nexec {sys.executable} {os.path.join(ROOT, 'kylin-v_gb300', 'sa_fit.py')} \"$@\"\n")
+    fit.chmod(0o755)
+    g = U.GOLDEN
+    tr = [t for t in U.manifest()["tiny1"]["trajectories"] if t["stage"] == "[0,2,2,0]"][0]
+    mps_file, mpo_file = os.path.join(g, "tiny1", "in.mps"), os.path.join(g, "tiny1", "H.mpo")
+    env = dict(os.environ, PATH=str(bindir) + os.pathsep + os.environ["PATH"], KV_SA_SEED=str(tr["sa_seed"]))
+    r = subprocess.run([str(exe), mps_file, mpo_file, "[0,2,2,0]", str(tr["maxD"]), str(tr["tol_svd"])], cwd=tmp_path,
+                       capture_output=True, text=True, timeout=300, env=env)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    widths = [float(x) for x in (tmp_path / "beta").read_text().split()]
+    ref_widths = [float(x) for x in open(os.path.join(g, "tiny1", tr["beta"])).read().split()]
+    np.testing.assert_allclose(widths, ref_widths, rtol=1e-6)
+    from kylin_v_gb300 import kvgpu
+
+    kvgpu.init(0)
+    t = kvgpu.TDVP(kvio.read_mps(mps_file), kvio.read_mpo(mpo_file), tr["tol_svd"], 1e-8, tr["maxD"], 11, 0.05)
+    t.set_sa([1.0 / float("{:21.15f}".format(w)) for w in widths], tr["sa_seed"])
+    for k, mode in enumerate((2, 2, 3, 3)):
+        t.sweep(mode)
+        got = kvio.read_mps(str(tmp_path / "State" / f"T-{k}.mps"))
+        want = [s.to_host() for s in t.sites()]
+        assert len(got) == len(want)
+        for a, b in zip(got, want):
+            assert U.tensor_diff(a, b) < 1e-12
+    assert t.sa_added() > 0

@@ -53,6 +53,7 @@ def test_mixed_trajectory_within_population_gate(gpu, case, ti):
     dens = [[gpu.Tensor.from_host(x) for x in H.density_mpo(ch, j)] for j in ch.exciton_sites()]
     hmpo = [gpu.Tensor.from_host(x) for x in mpo]
     t = gpu.TDVP(mps, mpo, tr["tol_svd"], 1e-8, tr["maxD"], 11, 0.05, gpu.KV_MIXED_3M_DIGITS)
+    U.prepare_sa(t, case, tr)
     worst_p = worst_e = 0.0
     for k, mode in enumerate(U.stage_modes(tr["stage"])):
         t.sweep(mode)

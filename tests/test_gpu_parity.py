@@ -119,6 +119,7 @@ def test_tdvp_trajectory(gpu, case, ti):
     dens = [H.density_mpo(ch, j) for j in ch.exciton_sites()]
     ident = H.identity_mpo(ch)
     t = gpu.TDVP(mps, mpo, tr["tol_svd"], 1e-8, tr["maxD"], 11, 0.05)
+    U.prepare_sa(t, case, tr)
     dmpo = [[gpu.Tensor.from_host(x) for x in d] for d in dens]
     hmpo = [gpu.Tensor.from_host(x) for x in mpo]
     imp = [gpu.Tensor.from_host(x) for x in ident]

@@ -91,6 +91,7 @@ def test_tdvp_trajectory_matches_reference(case, ti):
         pytest.skip("D = 512: minutes per step on the CPU; the trajectory comes from the compiled reference and the "
                     "GPU gate test checks against it")
     t = O.Tdvp(mps, mpo, tr["tol_svd"], 1e-8, tr["maxD"], 11, 0.05)
+    U.prepare_sa(t, case, tr)
     modes = U.stage_modes(tr["stage"])
     if ent.get("mixed_only"):
         modes = modes[:2]  # the D = 128 case: its first two steps (about 15 s a step here)
