@@ -395,6 +395,212 @@ __device__ __forceinline__ int qrj_jacobi(float2 *sw, int ldw, int p, int r, flo
     return converged ? sweep : -sweep;
 }
 
+// Exchange slots of qrj_jacobi_reg: two parities x (16 warps + 1) slots, each
+// one group's column (GJ lanes x E elements) and its norm per lane.
+constexpr size_t kQrjXchBytes = 2 * 17 * (128 * sizeof(float2) + 32 * sizeof(float));
+
+// The same Jacobi with the columns held in registers for a whole sweep.
+// Ordering: odd-even transposition with every pair swapped after its
+// rotation, on the N = r + (r & 1) positions (column r is a zero column when r
+// is odd): even rounds pair positions (2g, 2g+1), odd rounds (2g+1, 2g+2);
+// such a network reverses the order in N rounds, so every pair of columns
+// meets exactly once per sweep.  Group g holds (X, Y) = positions (2g, 2g+1)
+// in even rounds and (2g+1, 2g+2) in odd ones (group n-1 idles in odd rounds
+// holding positions (2n-1, 0)); after each round one column per group moves
+// to a neighbouring group: even -> odd Y_g <- Y_{g+1 mod n}; odd -> even
+// X_g <- X_{g-1}, X_0 <- Y_{n-1}, Y_{n-1} <- X_{n-1}.  Moves inside a warp
+// are shuffles by GJ lanes; moves across warps go through a shared slot
+// (double buffered by round parity, so one barrier per round suffices).  The
+// streamed form reads and writes both columns of every pair through shared
+// memory each round; this moves one column per group.  On return column 2g
+// holds X and 2g+1 holds Y of group g (positions of the even layout): the
+// caller sorts all N columns.  xch: kQrjXchBytes of shared memory.
+template <int GJ, int E>
+__device__ __forceinline__ int qrj_jacobi_reg(float2 *sw, int ldw, int p, int r, unsigned char *xch, int *rotated,
+                                              int max_sweeps, float tol2, float zt) {
+    constexpr int NT = 512, NW = NT / 32, GPW = 32 / GJ, H = E / 2;
+    static_assert(GJ * E <= 128 && GJ <= 32 && E % 2 == 0, "exchange slot size");
+    // Each lane holds rows gjl + k GJ (k < E) of its two columns as H pairs of
+    // rows (2h, 2h+1), real and imaginary parts apart (XR[h] = (re, re), XI[h]
+    // = (im, im)), so the complex dot products and rotations are packed FP32
+    // pairs with no swapping of halves.
+    float2 *xd = reinterpret_cast<float2 *>(xch);                    // [2][NW + 1][128]
+    float *xn = reinterpret_cast<float *>(xd + 2 * (NW + 1) * 128);  // [2][NW + 1][32]
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int g = tid / GJ, gjl = tid % GJ, kw = g % GPW;  // group, lane in the group, group in the warp
+    const unsigned jmask = GJ == 32 ? 0xFFFFFFFFu : (((1u << GJ) - 1u) << (lane & ~(GJ - 1)));
+    const int qe = r + (r & 1), n = qe / 2;
+    const bool act = g < n;
+    float2 XR[H], XI[H], YR[H], YI[H];
+#pragma unroll
+    for (int h = 0; h < H; ++h) {
+        const int i0 = gjl + 2 * h * GJ, i1 = i0 + GJ;
+        const float2 z = make_float2(0.f, 0.f);
+        const float2 x0 = (act && i0 < p && 2 * g < r) ? sw[i0 * ldw + 2 * g] : z;
+        const float2 x1 = (act && i1 < p && 2 * g < r) ? sw[i1 * ldw + 2 * g] : z;
+        const float2 y0 = (act && i0 < p && 2 * g + 1 < r) ? sw[i0 * ldw + 2 * g + 1] : z;
+        const float2 y1 = (act && i1 < p && 2 * g + 1 < r) ? sw[i1 * ldw + 2 * g + 1] : z;
+        XR[h] = make_float2(x0.x, x1.x);
+        XI[h] = make_float2(x0.y, x1.y);
+        YR[h] = make_float2(y0.x, y1.x);
+        YI[h] = make_float2(y0.y, y1.y);
+    }
+    auto gsum = [&](float v) {
+#pragma unroll
+        for (int o = GJ / 2; o > 0; o >>= 1) v += __shfl_xor_sync(jmask, v, o, GJ);
+        return v;
+    };
+    auto shfl2 = [&](float2 v, bool down) {
+        return down ? make_float2(__shfl_down_sync(0xFFFFFFFFu, v.x, GJ), __shfl_down_sync(0xFFFFFFFFu, v.y, GJ))
+                    : make_float2(__shfl_up_sync(0xFFFFFFFFu, v.x, GJ), __shfl_up_sync(0xFFFFFFFFu, v.y, GJ));
+    };
+    float nx = 0.f, ny = 0.f;
+    int sweep = 0;
+    bool converged = r < 2;
+    for (; sweep < max_sweeps && !converged; ++sweep) {
+        {
+            float2 a = make_float2(0.f, 0.f), b = a;
+#pragma unroll
+            for (int h = 0; h < H; ++h) {
+                a = __ffma2_rn(XR[h], XR[h], a);
+                a = __ffma2_rn(XI[h], XI[h], a);
+                b = __ffma2_rn(YR[h], YR[h], b);
+                b = __ffma2_rn(YI[h], YI[h], b);
+            }
+            nx = gsum(a.x + a.y);
+            ny = gsum(b.x + b.y);
+        }
+        if (tid == 0) *rotated = 0;
+        __syncthreads();
+        for (int t = 0; t < qe; ++t) {
+            const bool odd = t & 1;
+            // ---- rotate this group's pair: c = <X, Y> = sum conj(x) y
+            if (act && !(odd && g == n - 1) && nx > zt && ny > zt) {
+                float2 ar = make_float2(0.f, 0.f), ai = ar, bi = ar;
+#pragma unroll
+                for (int h = 0; h < H; ++h) {
+                    ar = __ffma2_rn(XR[h], YR[h], ar);
+                    ar = __ffma2_rn(XI[h], YI[h], ar);
+                    ai = __ffma2_rn(XR[h], YI[h], ai);
+                    bi = __ffma2_rn(XI[h], YR[h], bi);
+                }
+                const float cr = gsum(ar.x + ar.y);
+                const float ci = gsum((ai.x + ai.y) - (bi.x + bi.y));
+                const float ac2 = cr * cr + ci * ci;
+                if (ac2 > tol2 * nx * ny) {  // group-uniform
+                    const float rac = rsqrtf(ac2);
+                    const float ac = ac2 * rac;
+                    const float z = fminf(fmaxf(0.5f * (ny - nx) * rac, -1e18f), 1e18f);
+                    const float w = fmaf(z, z, 1.f);
+                    const float tn = copysignf(__fdividef(1.f, fabsf(z) + w * rsqrtf(w)), z);
+                    const float cs = rsqrtf(fmaf(tn, tn, 1.f));
+                    const float sn = tn * cs;
+                    const float s_re = sn * cr * rac, s_im = sn * ci * rac;
+                    if (gjl == 0) *rotated = 1;
+                    nx = nx - tn * ac;
+                    ny = ny + tn * ac;
+                    // x' = cs x - conj(s) y, y' = cs y + s x, s = s_re + i s_im
+                    const float2 cs2 = make_float2(cs, cs), sr2 = make_float2(s_re, s_re), si2 = make_float2(s_im, s_im);
+                    const float2 msr2 = make_float2(-s_re, -s_re), msi2 = make_float2(-s_im, -s_im);
+#pragma unroll
+                    for (int h = 0; h < H; ++h) {
+                        const float2 xr = XR[h], xi = XI[h], yr = YR[h], yi = YI[h];
+                        XR[h] = __ffma2_rn(msi2, yi, __ffma2_rn(msr2, yr, __fmul2_rn(cs2, xr)));
+                        XI[h] = __ffma2_rn(si2, yr, __ffma2_rn(msr2, yi, __fmul2_rn(cs2, xi)));
+                        YR[h] = __ffma2_rn(msi2, xi, __ffma2_rn(sr2, xr, __fmul2_rn(cs2, yr)));
+                        YI[h] = __ffma2_rn(si2, xr, __ffma2_rn(sr2, xi, __fmul2_rn(cs2, yi)));
+                    }
+                }
+            }
+            // ---- move one column per group (every lane of a warp runs the shuffles)
+            float2 *sd = xd + (t & 1) * (NW + 1) * 128;
+            float *sn_ = xn + (t & 1) * (NW + 1) * 32;
+            if (!odd) {
+                // Y_g <- Y_{(g+1) mod n}: group 0 of every warp publishes its Y
+                if (act && kw == 0) {
+#pragma unroll
+                    for (int h = 0; h < H; ++h) {
+                        sd[warp * 128 + gjl + 2 * h * GJ] = YR[h];
+                        sd[warp * 128 + gjl + (2 * h + 1) * GJ] = YI[h];
+                    }
+                    sn_[warp * 32 + gjl] = ny;
+                }
+                __syncthreads();
+                const bool by_shfl = g + 1 < n && kw < GPW - 1;
+                const int ws = g + 1 < n ? (g + 1) / GPW : 0;  // else: the source is group 0 of warp ws
+#pragma unroll
+                for (int h = 0; h < H; ++h) {
+                    const float2 vr = shfl2(YR[h], true), vi = shfl2(YI[h], true);
+                    if (act) {
+                        YR[h] = by_shfl ? vr : sd[ws * 128 + gjl + 2 * h * GJ];
+                        YI[h] = by_shfl ? vi : sd[ws * 128 + gjl + (2 * h + 1) * GJ];
+                    }
+                }
+                const float nyn = __shfl_down_sync(0xFFFFFFFFu, ny, GJ);
+                if (act) ny = by_shfl ? nyn : sn_[ws * 32 + gjl];
+            } else {
+                // X_g <- X_{g-1}, X_0 <- Y_{n-1}, Y_{n-1} <- X_{n-1}: the last
+                // group of every warp publishes its X, group n-1 its Y (slot NW)
+                if (act && kw == GPW - 1) {
+#pragma unroll
+                    for (int h = 0; h < H; ++h) {
+                        sd[warp * 128 + gjl + 2 * h * GJ] = XR[h];
+                        sd[warp * 128 + gjl + (2 * h + 1) * GJ] = XI[h];
+                    }
+                    sn_[warp * 32 + gjl] = nx;
+                }
+                if (g == n - 1) {
+#pragma unroll
+                    for (int h = 0; h < H; ++h) {
+                        sd[NW * 128 + gjl + 2 * h * GJ] = YR[h];
+                        sd[NW * 128 + gjl + (2 * h + 1) * GJ] = YI[h];
+                    }
+                    sn_[NW * 32 + gjl] = ny;
+                }
+                __syncthreads();
+                const bool last = g == n - 1;  // Y_{n-1} <- X_{n-1} before X is replaced
+                const bool by_shfl = g > 0 && kw > 0;
+                const int src = g == 0 ? NW : warp - 1;  // slot when not by shuffle
+#pragma unroll
+                for (int h = 0; h < H; ++h) {
+                    const float2 vr = shfl2(XR[h], false), vi = shfl2(XI[h], false);
+                    if (act) {
+                        if (last) {
+                            YR[h] = XR[h];
+                            YI[h] = XI[h];
+                        }
+                        XR[h] = by_shfl ? vr : sd[src * 128 + gjl + 2 * h * GJ];
+                        XI[h] = by_shfl ? vi : sd[src * 128 + gjl + (2 * h + 1) * GJ];
+                    }
+                }
+                const float nxn = __shfl_up_sync(0xFFFFFFFFu, nx, GJ);
+                if (act) {
+                    if (last) ny = nx;
+                    nx = by_shfl ? nxn : sn_[src * 32 + gjl];
+                }
+            }
+        }
+        converged = (*rotated == 0);
+        __syncthreads();
+    }
+    if (act) {
+#pragma unroll
+        for (int h = 0; h < H; ++h) {
+            const int i0 = gjl + 2 * h * GJ, i1 = i0 + GJ;
+            if (i0 < p) {
+                sw[i0 * ldw + 2 * g] = make_float2(XR[h].x, XI[h].x);
+                sw[i0 * ldw + 2 * g + 1] = make_float2(YR[h].x, YI[h].x);
+            }
+            if (i1 < p) {
+                sw[i1 * ldw + 2 * g] = make_float2(XR[h].y, XI[h].y);
+                sw[i1 * ldw + 2 * g + 1] = make_float2(YR[h].y, YI[h].y);
+            }
+        }
+    }
+    __syncthreads();
+    return converged ? sweep : -sweep;
+}
+
 // QR-preconditioned one-sided Jacobi (mixed mode).  One CTA of 512 threads
 // per charge sector; the sector is held in shared memory in FP32 as p rows of
 // length q (row stride q + 1, so reads of one column by consecutive rows fall
@@ -428,7 +634,7 @@ template <int EPL>
 __global__ void __launch_bounds__(512, 1) k_svd_qrj(const SvdSector *__restrict__ secs,
                                                     const double2 *__restrict__ T64, float2 *__restrict__ Us,
                                                     double *__restrict__ S, int *status, int *ranks, int max_sweeps,
-                                                    float tol, float qr_floor) {
+                                                    float tol, float qr_floor, int use_reg) {
     constexpr int NT = 512, NW = NT / 32;
     constexpr int GQ = 16;                     // lanes per row in the QR phase (two rows at a time)
     extern __shared__ float2 sw[];
@@ -440,9 +646,12 @@ __global__ void __launch_bounds__(512, 1) k_svd_qrj(const SvdSector *__restrict_
     const SvdSector s = secs[blockIdx.x];
     const int p = s.p, q = s.q, ldw = q + 1, kmax = min(p, q);
     float2 *alph = sw + p * ldw;                          // [kmax] conj(alpha_k)
-    float *cn = reinterpret_cast<float *>(alph + kmax);   // [kmax] column norms^2 (Jacobi), then norms
-    int *piv = reinterpret_cast<int *>(cn + kmax);        // [kmax] pivot rows
+    float *cn = reinterpret_cast<float *>(alph + kmax);   // [kmax + 1] column norms^2 (Jacobi), then norms
+    int *piv = reinterpret_cast<int *>(cn + kmax + 1);    // [kmax] pivot rows
     int *done = piv + kmax;                               // [p] row already pivoted
+    // [kQrjXchBytes] exchange slots of the register-resident Jacobi (use_reg)
+    unsigned char *xch = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(done + p) + 15) & ~static_cast<uintptr_t>(15));
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
     // ---- load (FP64 column-major p x q -> FP32 rows) scaled by a power of two
@@ -554,6 +763,7 @@ __global__ void __launch_bounds__(512, 1) k_svd_qrj(const SvdSector *__restrict_
             float2 *wa = sw + iA * ldw, *wb = sw + (lB ? iB : iA) * ldw;
             // s = sum_c w_c v_c, v_c = conj(x_c) for c > k, v_k = v0
             float sar = 0.f, sai = 0.f, sbr = 0.f, sbi = 0.f;
+#pragma unroll 4
             for (int c = k + gql; c < q; c += GQ) {
                 const float2 xc = xr[c];
                 const float2 vc = c == k ? v0 : make_float2(xc.x, -xc.y);
@@ -573,6 +783,7 @@ __global__ void __launch_bounds__(512, 1) k_svd_qrj(const SvdSector *__restrict_
             const float far = lA ? beta * sar : 0.f, fai = lA ? beta * sai : 0.f;
             const float fbr = lB ? beta * sbr : 0.f, fbi = lB ? beta * sbi : 0.f;
             float ta = 0.f, tb = 0.f;
+#pragma unroll 4
             for (int c = k + gql; c < q; c += GQ) {
                 const float2 xc = xr[c];
                 const float2 cv = c == k ? make_float2(v0.x, -v0.y) : xc;  // conj(v_c)
@@ -617,16 +828,28 @@ __global__ void __launch_bounds__(512, 1) k_svd_qrj(const SvdSector *__restrict_
     const float zt = 1e-14f * fro2;  // (1e-7 ||T||_F)^2: numerically zero columns
     const float tol2 = tol * tol;
     int sweeps;
+    int ncol = r;  // columns holding the result (r + 1 when the register form ran on odd r)
     if constexpr (EPL > 0) {
-        if (r <= 32) sweeps = qrj_jacobi<32, (EPL >= 4 ? EPL / 4 : 1)>(sw, ldw, p, r, cn, &rotated, max_sweeps, tol2, zt);
-        else if (r <= 64) sweeps = qrj_jacobi<16, EPL / 2>(sw, ldw, p, r, cn, &rotated, max_sweeps, tol2, zt);
-        else sweeps = qrj_jacobi<8, EPL>(sw, ldw, p, r, cn, &rotated, max_sweeps, tol2, zt);
+        constexpr int E32 = EPL >= 4 ? EPL / 4 : 1;
+        if (use_reg && r <= 128 && (r > 32 || E32 >= 2)) {
+            ncol = r + (r & 1);
+            if (r <= 32) sweeps = qrj_jacobi_reg<32, (E32 >= 2 ? E32 : 2)>(sw, ldw, p, r, xch, &rotated, max_sweeps, tol2, zt);
+            else if (r <= 64) sweeps = qrj_jacobi_reg<16, EPL / 2>(sw, ldw, p, r, xch, &rotated, max_sweeps, tol2, zt);
+            else sweeps = qrj_jacobi_reg<8, EPL>(sw, ldw, p, r, xch, &rotated, max_sweeps, tol2, zt);
+        } else if (r <= 32) {
+            sweeps = qrj_jacobi<32, E32>(sw, ldw, p, r, cn, &rotated, max_sweeps, tol2, zt);
+        } else if (r <= 64) {
+            sweeps = qrj_jacobi<16, EPL / 2>(sw, ldw, p, r, cn, &rotated, max_sweeps, tol2, zt);
+        } else {
+            sweeps = qrj_jacobi<8, EPL>(sw, ldw, p, r, cn, &rotated, max_sweeps, tol2, zt);
+        }
     } else {
         sweeps = qrj_jacobi<8, 0>(sw, ldw, p, r, cn, &rotated, max_sweeps, tol2, zt);
     }
 
-    // ---- sorted singular values and normalised columns
-    for (int j = warp; j < r; j += NW) {
+    // ---- sorted singular values and normalised columns (of ncol columns the
+    // r largest: a zero column beyond r sorts last)
+    for (int j = warp; j < ncol; j += NW) {
         float a = 0.f;
         for (int i = lane; i < p; i += 32) {
             const float2 x = sw[i * ldw + j];
@@ -637,10 +860,11 @@ __global__ void __launch_bounds__(512, 1) k_svd_qrj(const SvdSector *__restrict_
         if (lane == 0) cn[j] = sqrtf(a);
     }
     __syncthreads();
-    for (int j = warp; j < r; j += NW) {
+    for (int j = warp; j < ncol; j += NW) {
         const float sj = cn[j];
         int rank = 0;
-        for (int i = 0; i < r; ++i) rank += (cn[i] > sj) || (cn[i] == sj && i < j);
+        for (int i = 0; i < ncol; ++i) rank += (cn[i] > sj) || (cn[i] == sj && i < j);
+        if (rank >= r) continue;  // warp-uniform
         const float inv = sj > 0.f ? 1.f / sj : 0.f;
         for (int i = lane; i < p; i += 32) {
             const float2 x = sw[i * ldw + j];
@@ -1056,7 +1280,7 @@ void svd_jacobi_f32(const SvdPlan &p, const double2 *T64, float2 *T, int *status
 // shared-memory bytes of k_svd_qrj for a p x q sector
 static size_t qrj_smem(int p, int q) {
     const size_t kmax = (size_t)std::min(p, q);
-    return sizeof(float2) * ((size_t)p * (q + 1) + kmax) + sizeof(float) * ((size_t)p + 2 * kmax);
+    return sizeof(float2) * ((size_t)p * (q + 1) + kmax) + sizeof(float) * ((size_t)p + 2 * kmax + 1);
 }
 
 bool svd_qrjacobi_f32(const SvdPlan &p, const double2 *T64, float2 *Us, double *S, int *status, int *ranks,
@@ -1070,9 +1294,12 @@ bool svd_qrjacobi_f32(const SvdPlan &p, const double2 *T64, float2 *Us, double *
         max_p = std::max(max_p, sc.p);
     }
     if (smem > (size_t)limit) return false;
+    // the register-resident Jacobi where its exchange slots also fit
+    const int use_reg = max_p <= 128 && smem + 16 + kQrjXchBytes <= (size_t)limit ? 1 : 0;
+    if (use_reg) smem += 16 + kQrjXchBytes;
     auto launch = [&](auto kernel) {
         kernel<<<(unsigned)p.secs.size(), 512, smem, ctx().stream>>>(p.d_secs.as<SvdSector>(), T64, Us, S, status,
-                                                                     ranks, max_sweeps, tol, qr_floor);
+                                                                     ranks, max_sweeps, tol, qr_floor, use_reg);
     };
     // elements per lane from the longest column of the launch (8 lanes a pair)
     if (max_p <= 32) launch(k_svd_qrj<4>);

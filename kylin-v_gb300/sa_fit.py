@@ -1,3 +1,4 @@
+#!/usr/bin/env python3
 """Widths of the SA-1TDVP stage's synthetic singular values, fitted from the
 two-site sweeps' singular-value log (a restatement of the reference's
 bin/nls.py, which total_start runs before the SA stage, holstein/tdvp.h:341-358).
