@@ -395,9 +395,14 @@ __device__ __forceinline__ int qrj_jacobi(float2 *sw, int ldw, int p, int r, flo
     return converged ? sweep : -sweep;
 }
 
-// Exchange slots of qrj_jacobi_reg: two parities x (16 warps + 1) slots, each
-// one group's column (GJ lanes x E elements) and its norm per lane.
-constexpr size_t kQrjXchBytes = 2 * 17 * (128 * sizeof(float2) + 32 * sizeof(float));
+// Exchange columns of qrj_jacobi_reg: r/2 + 1 columns of the GJ * E packed
+// elements a group holds (rows padded past p), the column stride 8 (mod 16)
+// float2 so that the four 8-lane pieces one warp moves at a time fall in two
+// shared-memory wavefronts, and their norms.  rows: the launch's 8 * EPL.
+__host__ __device__ constexpr int qrj_xch_stride(int rows) { return ((rows + 15) / 16) * 16 + 8; }
+__host__ __device__ constexpr size_t qrj_xch_bytes(int rows, int kmax) {
+    return (size_t)(kmax / 2 + 2) * ((size_t)qrj_xch_stride(rows) * sizeof(float2) + sizeof(float));
+}
 
 // The same Jacobi with the columns held in registers for a whole sweep.
 // Ordering: odd-even transposition with every pair swapped after its
@@ -408,28 +413,29 @@ constexpr size_t kQrjXchBytes = 2 * 17 * (128 * sizeof(float2) + 32 * sizeof(flo
 // in even rounds and (2g+1, 2g+2) in odd ones (group n-1 idles in odd rounds
 // holding positions (2n-1, 0)); after each round one column per group moves
 // to a neighbouring group: even -> odd Y_g <- Y_{g+1 mod n}; odd -> even
-// X_g <- X_{g-1}, X_0 <- Y_{n-1}, Y_{n-1} <- X_{n-1}.  Moves inside a warp
-// are shuffles by GJ lanes; moves across warps go through a shared slot
-// (double buffered by round parity, so one barrier per round suffices).  The
-// streamed form reads and writes both columns of every pair through shared
-// memory each round; this moves one column per group.  On return column 2g
-// holds X and 2g+1 holds Y of group g (positions of the even layout): the
-// caller sorts all N columns.  xch: kQrjXchBytes of shared memory.
+// X_g <- X_{g-1}, X_0 <- Y_{n-1}, Y_{n-1} <- X_{n-1}.  The moving columns go
+// through shared memory, one store and one load per element for every lane
+// (a warp moves four 8-row pieces at a time, two wavefronts).  The streamed
+// form reads and writes both columns of every pair each round; this moves
+// one.  On return column 2g holds X and 2g+1 holds Y of group g (positions of
+// the even layout): the caller sorts all N columns.  xch: qrj_xch_bytes(GJ E,
+// r) of shared memory.
 template <int GJ, int E>
 __device__ __forceinline__ int qrj_jacobi_reg(float2 *sw, int ldw, int p, int r, unsigned char *xch, int *rotated,
                                               int max_sweeps, float tol2, float zt) {
-    constexpr int NT = 512, NW = NT / 32, GPW = 32 / GJ, H = E / 2;
-    static_assert(GJ * E <= 128 && GJ <= 32 && E % 2 == 0, "exchange slot size");
+    constexpr int H = E / 2;
+    static_assert(GJ * E <= 128 && GJ <= 32 && E % 2 == 0, "row cover");
     // Each lane holds rows gjl + k GJ (k < E) of its two columns as H pairs of
     // rows (2h, 2h+1), real and imaginary parts apart (XR[h] = (re, re), XI[h]
     // = (im, im)), so the complex dot products and rotations are packed FP32
     // pairs with no swapping of halves.
-    float2 *xd = reinterpret_cast<float2 *>(xch);                    // [2][NW + 1][128]
-    float *xn = reinterpret_cast<float *>(xd + 2 * (NW + 1) * 128);  // [2][NW + 1][32]
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int g = tid / GJ, gjl = tid % GJ, kw = g % GPW;  // group, lane in the group, group in the warp
-    const unsigned jmask = GJ == 32 ? 0xFFFFFFFFu : (((1u << GJ) - 1u) << (lane & ~(GJ - 1)));
+    constexpr int ps = qrj_xch_stride(GJ * E);
+    float2 *xd = reinterpret_cast<float2 *>(xch);  // [n + 1] exchange columns of stride ps
     const int qe = r + (r & 1), n = qe / 2;
+    float *xn = reinterpret_cast<float *>(xd + (n + 1) * ps);  // [n + 1] their norms
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int g = tid / GJ, gjl = tid % GJ;  // group, lane in the group
+    const unsigned jmask = GJ == 32 ? 0xFFFFFFFFu : (((1u << GJ) - 1u) << (lane & ~(GJ - 1)));
     const bool act = g < n;
     float2 XR[H], XI[H], YR[H], YI[H];
 #pragma unroll
@@ -449,10 +455,6 @@ __device__ __forceinline__ int qrj_jacobi_reg(float2 *sw, int ldw, int p, int r,
 #pragma unroll
         for (int o = GJ / 2; o > 0; o >>= 1) v += __shfl_xor_sync(jmask, v, o, GJ);
         return v;
-    };
-    auto shfl2 = [&](float2 v, bool down) {
-        return down ? make_float2(__shfl_down_sync(0xFFFFFFFFu, v.x, GJ), __shfl_down_sync(0xFFFFFFFFu, v.y, GJ))
-                    : make_float2(__shfl_up_sync(0xFFFFFFFFu, v.x, GJ), __shfl_up_sync(0xFFFFFFFFu, v.y, GJ));
     };
     float nx = 0.f, ny = 0.f;
     int sweep = 0;
@@ -512,73 +514,74 @@ __device__ __forceinline__ int qrj_jacobi_reg(float2 *sw, int ldw, int p, int r,
                     }
                 }
             }
-            // ---- move one column per group (every lane of a warp runs the shuffles)
-            float2 *sd = xd + (t & 1) * (NW + 1) * 128;
-            float *sn_ = xn + (t & 1) * (NW + 1) * 32;
+            // ---- move one column per group through the exchange columns
+            // (column c at xd + c * ps, the lanes' packed pairs as they are held;
+            // norms at xn[c]): store, barrier, load, barrier (the next round's
+            // stores wait for every load)
+            float2 *mine = xd + g * ps + gjl;
             if (!odd) {
-                // Y_g <- Y_{(g+1) mod n}: group 0 of every warp publishes its Y
-                if (act && kw == 0) {
+                // Y_g <- Y_{(g+1) mod n}
+                if (act) {
 #pragma unroll
                     for (int h = 0; h < H; ++h) {
-                        sd[warp * 128 + gjl + 2 * h * GJ] = YR[h];
-                        sd[warp * 128 + gjl + (2 * h + 1) * GJ] = YI[h];
+                        mine[2 * h * GJ] = YR[h];
+                        mine[(2 * h + 1) * GJ] = YI[h];
                     }
-                    sn_[warp * 32 + gjl] = ny;
+                    if (gjl == 0) xn[g] = ny;
                 }
                 __syncthreads();
-                const bool by_shfl = g + 1 < n && kw < GPW - 1;
-                const int ws = g + 1 < n ? (g + 1) / GPW : 0;  // else: the source is group 0 of warp ws
+                if (act) {
+                    const int src = g + 1 < n ? g + 1 : 0;
+                    const float2 *from = xd + src * ps + gjl;
 #pragma unroll
-                for (int h = 0; h < H; ++h) {
-                    const float2 vr = shfl2(YR[h], true), vi = shfl2(YI[h], true);
-                    if (act) {
-                        YR[h] = by_shfl ? vr : sd[ws * 128 + gjl + 2 * h * GJ];
-                        YI[h] = by_shfl ? vi : sd[ws * 128 + gjl + (2 * h + 1) * GJ];
+                    for (int h = 0; h < H; ++h) {
+                        YR[h] = from[2 * h * GJ];
+                        YI[h] = from[(2 * h + 1) * GJ];
                     }
+                    ny = xn[src];
                 }
-                const float nyn = __shfl_down_sync(0xFFFFFFFFu, ny, GJ);
-                if (act) ny = by_shfl ? nyn : sn_[ws * 32 + gjl];
             } else {
-                // X_g <- X_{g-1}, X_0 <- Y_{n-1}, Y_{n-1} <- X_{n-1}: the last
-                // group of every warp publishes its X, group n-1 its Y (slot NW)
-                if (act && kw == GPW - 1) {
+                // X_g <- X_{g-1}, X_0 <- Y_{n-1} (column n), Y_{n-1} <- X_{n-1}
+                if (act) {
 #pragma unroll
                     for (int h = 0; h < H; ++h) {
-                        sd[warp * 128 + gjl + 2 * h * GJ] = XR[h];
-                        sd[warp * 128 + gjl + (2 * h + 1) * GJ] = XI[h];
+                        mine[2 * h * GJ] = XR[h];
+                        mine[(2 * h + 1) * GJ] = XI[h];
                     }
-                    sn_[warp * 32 + gjl] = nx;
-                }
-                if (g == n - 1) {
+                    if (g == n - 1) {
+                        float2 *tail = xd + n * ps + gjl;
 #pragma unroll
-                    for (int h = 0; h < H; ++h) {
-                        sd[NW * 128 + gjl + 2 * h * GJ] = YR[h];
-                        sd[NW * 128 + gjl + (2 * h + 1) * GJ] = YI[h];
+                        for (int h = 0; h < H; ++h) {
+                            tail[2 * h * GJ] = YR[h];
+                            tail[(2 * h + 1) * GJ] = YI[h];
+                        }
                     }
-                    sn_[NW * 32 + gjl] = ny;
+                    if (gjl == 0) {
+                        xn[g] = nx;
+                        if (g == n - 1) xn[n] = ny;
+                    }
                 }
                 __syncthreads();
-                const bool last = g == n - 1;  // Y_{n-1} <- X_{n-1} before X is replaced
-                const bool by_shfl = g > 0 && kw > 0;
-                const int src = g == 0 ? NW : warp - 1;  // slot when not by shuffle
+                if (act) {
+                    if (g == n - 1) {
 #pragma unroll
-                for (int h = 0; h < H; ++h) {
-                    const float2 vr = shfl2(XR[h], false), vi = shfl2(XI[h], false);
-                    if (act) {
-                        if (last) {
+                        for (int h = 0; h < H; ++h) {
                             YR[h] = XR[h];
                             YI[h] = XI[h];
                         }
-                        XR[h] = by_shfl ? vr : sd[src * 128 + gjl + 2 * h * GJ];
-                        XI[h] = by_shfl ? vi : sd[src * 128 + gjl + (2 * h + 1) * GJ];
+                        ny = nx;
                     }
-                }
-                const float nxn = __shfl_up_sync(0xFFFFFFFFu, nx, GJ);
-                if (act) {
-                    if (last) ny = nx;
-                    nx = by_shfl ? nxn : sn_[src * 32 + gjl];
+                    const int src = g == 0 ? n : g - 1;
+                    const float2 *from = xd + src * ps + gjl;
+#pragma unroll
+                    for (int h = 0; h < H; ++h) {
+                        XR[h] = from[2 * h * GJ];
+                        XI[h] = from[(2 * h + 1) * GJ];
+                    }
+                    nx = xn[src];
                 }
             }
+            __syncthreads();
         }
         converged = (*rotated == 0);
         __syncthreads();
@@ -649,7 +652,7 @@ __global__ void __launch_bounds__(512, 1) k_svd_qrj(const SvdSector *__restrict_
     float *cn = reinterpret_cast<float *>(alph + kmax);   // [kmax + 1] column norms^2 (Jacobi), then norms
     int *piv = reinterpret_cast<int *>(cn + kmax + 1);    // [kmax] pivot rows
     int *done = piv + kmax;                               // [p] row already pivoted
-    // [kQrjXchBytes] exchange slots of the register-resident Jacobi (use_reg)
+    // [qrj_xch_bytes(8 EPL, kmax)] exchange columns of the register-resident Jacobi (use_reg)
     unsigned char *xch = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(done + p) + 15) & ~static_cast<uintptr_t>(15));
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -1294,9 +1297,12 @@ bool svd_qrjacobi_f32(const SvdPlan &p, const double2 *T64, float2 *Us, double *
         max_p = std::max(max_p, sc.p);
     }
     if (smem > (size_t)limit) return false;
-    // the register-resident Jacobi where its exchange slots also fit
-    const int use_reg = max_p <= 128 && smem + 16 + kQrjXchBytes <= (size_t)limit ? 1 : 0;
-    if (use_reg) smem += 16 + kQrjXchBytes;
+    // the register-resident Jacobi where its exchange columns also fit
+    const int rows = max_p <= 32 ? 32 : max_p <= 64 ? 64 : 128;  // 8 EPL of the kernel launched below
+    size_t xch = 0;
+    for (auto &sc : p.secs) xch = std::max(xch, qrj_smem(sc.p, sc.q) + 16 + qrj_xch_bytes(rows, std::min(sc.p, sc.q)));
+    const int use_reg = max_p <= 128 && xch <= (size_t)limit ? 1 : 0;
+    if (use_reg) smem = xch;
     auto launch = [&](auto kernel) {
         kernel<<<(unsigned)p.secs.size(), 512, smem, ctx().stream>>>(p.d_secs.as<SvdSector>(), T64, Us, S, status,
                                                                      ranks, max_sweeps, tol, qr_floor, use_reg);
