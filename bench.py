@@ -33,6 +33,8 @@ cpu_baseline  the CPU oracle (restatement of the reference on OpenBLAS, all
            with a one-thread measurement of the same sample beside it.
 --config holstein-1site-batch64  the batched disordered ensemble instead
            (run_batched); under torchrun its chains are split across ranks.
+--config holstein-1site-L24-grad  the differentiation workload: gradients
+           through 10 one-site steps of the L = 24, D = 96 chain (run_gradient).
 N > 1 (torchrun): each rank evolves its own replica chain (a single chain's
 sweep is sequential), value = total flops / max time over ranks.
 """
@@ -576,12 +578,78 @@ def run_window(args):
     print(json.dumps(line), flush=True)
 
 
+GRAD_CONFIG = "holstein-1site-L24-grad"
+
+
+def run_gradient(args):
+    """The differentiation workload: L = 24, one mode (omega = 1, g = 1, J = 1),
+    cutoff 12, D = 96, one-site TDVP at dt = 0.05 without truncation, 10 steps.
+    Gradients of msd = sum_t sum_i i P_i(t) and of <H> with respect to (J,
+    omega, g): central differences with the 7 chains (theta, theta +- h e_k)
+    advanced together (gradient.fd_gradient), and the reverse-mode <H>
+    gradient through the parameter-linear MPO (gradient.energy_gradient_adjoint,
+    on the base chain's state).  value = wall seconds per gradient evaluation
+    (both quantities, all three parameters).  FP64 throughout: central
+    differences need a map that is smooth in theta, and the mixed SVD's
+    resolution floor (singular values below 1e-6 of a sector's largest read as
+    zero) is not."""
+    import numpy as np
+    import torch
+
+    import __graft_entry__ as ge
+
+    ge.load_package()
+    from kylin_v_gb300 import gradient as Gr
+    from kylin_v_gb300 import holstein as H
+    from kylin_v_gb300 import kvgpu as G
+
+    _, _, local = dist()
+    torch.cuda.set_device(local)
+    G.init(local)
+    prec = G.KV_FP64
+    n_mol, cutoff, D, steps = 24, 12, 96, 10
+    theta = {"J": 1.0, "omega": 1.0, "g": 1.0}
+    for _ in range(max(0, args.warmup)):
+        Gr.fd_gradient(n_mol, cutoff, D, theta, steps=1, precision=prec)
+    torch.cuda.synchronize()
+    walls, dev = [], []
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            r = Gr.fd_gradient(n_mol, cutoff, D, theta, steps=steps, precision=prec)
+            torch.cuda.synchronize()
+            walls.append(time.perf_counter() - t0)
+            dev.append(r["device_ms"])
+    # reverse mode for <H> on the base chain's state (energy_gradient_adjoint)
+    ch = Gr.holstein_chain(n_mol, cutoff, theta)
+    mps = [G.Tensor.from_host(x) for x in H.random_mps(ch, D, seed=1234)]
+    t0 = time.perf_counter()
+    adj = Gr.energy_gradient_adjoint(ch, mps, precision=prec)
+    torch.cuda.synchronize()
+    adj_s = time.perf_counter() - t0
+    fd_e = Gr.fd_gradient(n_mol, cutoff, D, theta, steps=0, precision=prec)["grad"]["energy"]
+    line = {"metric": "wall seconds per (msd, <H>) gradient w.r.t. (J, omega, g) through 10 1TDVP steps",
+            "value": float(np.median(walls)), "unit": "s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * float(np.median(walls)) / steps, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+            "data": "synthetic (seeded random right-canonical U(1) MPS, Holstein FSM MPO)",
+            "config": {"workload": GRAD_CONFIG, "n_mol": n_mol, "cutoff": cutoff, "D": D, "tdvp_steps": steps,
+                       "chains": 7, "h": 1e-5, "precision": "fp64"},
+            "device_ms_per_gradient": float(np.median(dev)),
+            "grad_fd": r["grad"], "value_fd": r["value"],
+            "adjoint_energy": {"seconds": adj_s, "grad": adj["grad"], "fd_grad_same_state": fd_e},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     elif args.config == BATCH_CONFIG:
         run_batched(args)
+    elif args.config == GRAD_CONFIG:
+        run_gradient(args)
     elif args.config in WINDOW_CONFIGS:
         run_window(args)
     else:

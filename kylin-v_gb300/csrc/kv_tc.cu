@@ -143,13 +143,26 @@ __device__ __forceinline__ __half2 digits2(int d0, int d1) {
 // that of B's row k.  A's column is scaled by 2^s, B's row by 2^-s, with
 // s = floor((E_B - E_A) / 2) from their binary exponents, so both reach about
 // sqrt(max_A max_B) and every digit product is resolved at the same scale.
-__device__ __forceinline__ double balance_factor(const unsigned long long *kmax, int64_t kscales, int64_t k,
-                                                 int b_side) {
+__device__ __forceinline__ int balance_shift(const unsigned long long *kmax, int64_t kscales, int64_t k, int b_side) {
     const int ea = (int)(kmax[k] >> 52), eb = (int)(kmax[kscales + k] >> 52);
-    if (ea == 0 || eb == 0) return 1.0;
-    int sh = (eb - ea) >> 1;
-    if (b_side) sh = -sh;
-    return __longlong_as_double((long long)(1023 + sh) << 52);
+    if (ea == 0 || eb == 0) return 0;
+    const int sh = (eb - ea) >> 1;
+    return b_side ? -sh : sh;
+}
+
+// x * 2^sh by the exponent field alone (no FP64 arithmetic): exact for
+// normal results; results below the normal range become +-0 and results
+// beyond it +-inf (as the product would round; a subnormal input stays as it
+// is, and fixq reads subnormals as 0 either way)
+__device__ __forceinline__ double scale_exp(double x, int sh) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    const int E = (int)((u >> 52) & 0x7FF);
+    if (sh == 0 || E == 0 || E == 0x7FF) return x;
+    const int En = E + sh;
+    const unsigned long long sign = u & 0x8000000000000000ull;
+    if (En <= 0) return __longlong_as_double((long long)sign);
+    if (En >= 0x7FF) return __longlong_as_double((long long)(sign | 0x7FF0000000000000ull));
+    return __longlong_as_double((long long)((u & ~(0x7FFull << 52)) | ((unsigned long long)En << 52)));
 }
 
 // Per-k maxima for balancing: one CTA per (view, 8 rows), one warp per row;
@@ -223,9 +236,9 @@ __device__ __forceinline__ void slice_item(const SliceJob *__restrict__ jobs, in
         if (scale) { v.x *= alpha; v.y *= alpha; }
         if (j.conj) v.y = -v.y;
         if (bal) {  // exact power-of-two balancing of the contracted index
-            const double f = balance_factor(kmax, kscales, j.ks_off + k, b_side);
-            v.x *= f;
-            v.y *= f;
+            const int sh = balance_shift(kmax, kscales, j.ks_off + k, b_side);
+            v.x = scale_exp(v.x, sh);
+            v.y = scale_exp(v.y, sh);
         }
         return v;
     };

@@ -86,3 +86,22 @@ def test_batched_errors(gpu):
         gpu.sweep_batched(ts, 1, -1)
     assert gpu.sweep_batched([], 1, 1) == 0.0
     assert gpu.sweep_batched(ts, 1, 0) == 0.0
+
+
+def test_batched_large_bond(gpu):
+    """Chains at the benchmark's bond dimension (D = 128, where the two-site
+    sectors reach 128 x 128 and the register-resident Jacobi runs) and D = 64,
+    two-site mixed steps: batched equals sequential bit for bit."""
+    chains = [(H.HolsteinChain(4, [1.0], [[1.0]] * 4, cutoff=8), 128),
+              (H.HolsteinChain(3, [0.6], [[0.8]] * 3, cutoff=8, eps=[0.2, -0.1, 0.0]), 64)]
+    host = [(H.random_mps(ch, D, seed=99 + i), H.hamiltonian_mpo(ch), D) for i, (ch, D) in enumerate(chains)]
+    make = lambda: [gpu.TDVP(m, w, 1e-8, 1e-8, D, 11, 0.05, gpu.KV_MIXED_3M_DIGITS) for m, w, D in host]  # noqa: E731
+    seq, bat = make(), make()
+    for t in seq:
+        for _ in range(2):
+            t.two_site()
+    gpu.sweep_batched(bat, 2, 2, max_streams=2)
+    assert max(sum(s.to_host().legs()[2].values()) for s in seq[0].sites()[:-1]) == 128
+    for i, (a, b) in enumerate(zip(seq, bat)):
+        for j in range(a.ns):
+            assert _same(a.site(j), b.site(j)), (i, j)
