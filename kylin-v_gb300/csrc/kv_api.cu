@@ -364,7 +364,7 @@ int kv_sweep_batched(int n_chains, const kv_tdvp *chains, int mode, int steps, i
     return guard([&] {
         kv::require_init();
         KV_REQUIRE(n_chains >= 0 && (n_chains == 0 || chains), KV_EINVAL, "null chain array");
-        KV_REQUIRE(mode >= 0 && mode <= 2, KV_EINVAL, "mode must be 0, 1 or 2");
+        KV_REQUIRE(mode >= 0 && mode <= 3, KV_EINVAL, "mode must be 0, 1, 2 or 3");
         KV_REQUIRE(steps >= 0, KV_EINVAL, "steps must be >= 0");
         std::set<const kv_tdvp_s *> seen;
         for (int i = 0; i < n_chains; ++i) {
@@ -427,6 +427,7 @@ int kv_sweep_batched(int n_chains, const kv_tdvp *chains, int mode, int steps, i
                     for (int s = 0; s < steps; ++s) {
                         if (mode == 0) t.global_krylov();
                         else if (mode == 1) t.one_site();
+                        else if (mode == 3) t.sa_site();
                         else t.two_site();
                     }
                 });

@@ -105,3 +105,24 @@ def test_batched_large_bond(gpu):
     for i, (a, b) in enumerate(zip(seq, bat)):
         for j in range(a.ns):
             assert _same(a.site(j), b.site(j)), (i, j)
+
+
+def test_batched_sa_equals_sequential(gpu):
+    """SA-1TDVP sweeps (mode 3) through kv_sweep_batched leave the tensors a
+    loop of single-chain SA sweeps leaves: each chain draws from its own seed
+    stream, whichever worker runs it."""
+    cs = _chains(4, seed=5)
+    def make():
+        ts = [gpu.TDVP(m, w, 1e-8, 1e-8, 2 * D, 11, 0.05, gpu.KV_MIXED_3M_DIGITS) for _, D, m, w in cs]
+        for i, (t, (ch, _, _, _)) in enumerate(zip(ts, cs)):
+            t.set_sa([4.0] * (ch.n_sites - 1), 11 + i)
+        return ts
+    seq, bat = make(), make()
+    for t in seq:
+        for _ in range(2):
+            t.sweep(3)
+    gpu.sweep_batched(bat, 3, 2, max_streams=3)
+    assert sum(t.sa_added() for t in seq) > 0
+    for i, (a, b) in enumerate(zip(seq, bat)):
+        for j in range(a.ns):
+            assert _same(a.site(j), b.site(j)), (i, j)
