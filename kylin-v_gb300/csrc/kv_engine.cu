@@ -944,9 +944,24 @@ SvdOut op_svd(const DTensor &A, int r1, bool l2r, double thres, int max_dim, int
         qr_ranks = svd_qrjacobi_f32(P, T.as<double2>(), Us.as<float2>(), S.as<double>(), status.as<int>(),
                                     status.as<int>() + P.secs.size(), 60, 1e-5f, kQrFloor);
         if (!qr_ranks) {
+            // sectors beyond shared memory: the same QR reduction on an
+            // L2-resident workspace, then the global-memory Jacobi on each
+            // sector's rank-r factor (its columns beyond r are zero)
             DevBuf T32(std::max<int64_t>(1, P.t_elems) * cb);
-            svd_jacobi_f32(P, T.as<double2>(), T32.as<float2>(), status.as<int>(), 60, 1e-5f);
+            int *rk_dev = status.as<int>() + P.secs.size();
+            svd_qr_global(P, T.as<double2>(), T32.as<float2>(), rk_dev, kQrFloor);
+            std::vector<int> rk(P.secs.size());
+            KV_CUDA(cudaMemcpyAsync(rk.data(), rk_dev, rk.size() * sizeof(int), cudaMemcpyDeviceToHost,
+                                    ctx().stream));
+            KV_CUDA(cudaStreamSynchronize(ctx().stream));
+            SvdPlan Pr;
+            Pr.secs = P.secs;
+            for (size_t i = 0; i < rk.size(); ++i) Pr.secs[i].q = std::max(0, std::min(rk[i], P.secs[i].q));
+            Pr.t_elems = P.t_elems;
+            Pr.upload();
+            svd_jacobi_f32(Pr, nullptr, T32.as<float2>(), status.as<int>(), 60, 1e-5f);
             svd_finalize_f32(P, T32.as<float2>(), Us.as<float2>(), S.as<double>());
+            qr_ranks = true;
         }
     } else {
         svd_jacobi(P, T.as<double2>(), V.as<double2>(), status.as<int>(), 60, 1e-15);

@@ -633,30 +633,23 @@ __device__ __forceinline__ int qrj_jacobi_reg(float2 *sw, int ldw, int p, int r,
 //     (column-major p x r at the sector's t_off), S = 0 in the sector's
 //     remaining slots up to q.
 // status[sector] = Jacobi sweeps used (negative: no convergence), ranks[sector] = r.
-template <int EPL>
-__global__ void __launch_bounds__(512, 1) k_svd_qrj(const SvdSector *__restrict__ secs,
-                                                    const double2 *__restrict__ T64, float2 *__restrict__ Us,
-                                                    double *__restrict__ S, int *status, int *ranks, int max_sweeps,
-                                                    float tol, float qr_floor, int use_reg) {
+// Load one sector into sw (p rows of stride ldw, in shared or global memory)
+// in FP32 scaled by a power of two (*up is the inverse factor), then the
+// pivoted Householder reduction of its rows to the numerical rank r (rows
+// below qr_floor ||T||_F dropped); on return M = sw's first r columns with
+// conj(alpha_k) at (piv[k], k) and zeros beyond.  Returns r, or -1 for a
+// sector holding Inf or NaN.  alph, piv: [min(p, q)]; done: [p].  512 threads.
+__device__ __forceinline__ int qrj_reduce(const SvdSector &s, const double2 *__restrict__ T64, float2 *sw, int ldw,
+                                          float2 *alph, int *piv, int *done, float qr_floor, double *up,
+                                          float *fro2_out) {
     constexpr int NT = 512, NW = NT / 32;
-    constexpr int GQ = 16;                     // lanes per row in the QR phase (two rows at a time)
-    extern __shared__ float2 sw[];
+    constexpr int GQ = 16;  // lanes per row (two rows at a time)
     __shared__ float wbest[2][NW];
     __shared__ int wbesti[2][NW];
     __shared__ float red[NW];
     __shared__ double dred[NW];
-    __shared__ int rotated;
-    const SvdSector s = secs[blockIdx.x];
-    const int p = s.p, q = s.q, ldw = q + 1, kmax = min(p, q);
-    float2 *alph = sw + p * ldw;                          // [kmax] conj(alpha_k)
-    float *cn = reinterpret_cast<float *>(alph + kmax);   // [kmax + 1] column norms^2 (Jacobi), then norms
-    int *piv = reinterpret_cast<int *>(cn + kmax + 1);    // [kmax] pivot rows
-    int *done = piv + kmax;                               // [p] row already pivoted
-    // [qrj_xch_bytes(8 EPL, kmax)] exchange columns of the register-resident Jacobi (use_reg)
-    unsigned char *xch = reinterpret_cast<unsigned char *>(
-        (reinterpret_cast<uintptr_t>(done + p) + 15) & ~static_cast<uintptr_t>(15));
+    const int p = s.p, q = s.q, kmax = min(p, q);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-
     // ---- load (FP64 column-major p x q -> FP32 rows) scaled by a power of two
     // that brings the largest element to [0.5, 1): sectors whose entries are
     // far below 1 would otherwise underflow FP32 in the squared norms
@@ -674,17 +667,11 @@ __global__ void __launch_bounds__(512, 1) k_svd_qrj(const SvdSector *__restrict_
     __syncthreads();
     amax = 0.0;
     for (int w = 0; w < NW; ++w) amax = fmax(amax, dred[w]);
-    if (!isfinite(amax)) {  // a non-finite sector: its singular values are NaN (reported by the host)
-        for (int j = tid; j < q; j += NT) S[s.s_off + j] = nan("");
-        if (tid == 0) {
-            status[blockIdx.x] = 0;
-            ranks[blockIdx.x] = 0;
-        }
-        return;
-    }
+    if (!isfinite(amax)) return -1;  // a non-finite sector (uniform over the CTA)
     int ex = 0;
     if (amax > 0.0) frexp(amax, &ex);
-    const double down = ldexp(1.0, -ex), up = ldexp(1.0, ex);  // exact powers of two
+    const double down = ldexp(1.0, -ex);  // exact powers of two
+    *up = ldexp(1.0, ex);
     for (int e = tid; e < pq; e += NT) {
         const int i = e % p, c = e / p;
         const double2 v = src[e];
@@ -725,6 +712,7 @@ __global__ void __launch_bounds__(512, 1) k_svd_qrj(const SvdSector *__restrict_
     float fro2 = 0.f;
     for (int w = 0; w < NW; ++w) fro2 += red[w];
     const float thr2 = qr_floor * qr_floor * fro2;
+    *fro2_out = fro2;
 
     // ---- pivoted Householder on the rows
     int r = 0;
@@ -825,6 +813,39 @@ __global__ void __launch_bounds__(512, 1) k_svd_qrj(const SvdSector *__restrict_
         if (c >= kk) sw[piv[kk] * ldw + c] = c == kk ? alph[kk] : make_float2(0.f, 0.f);
     }
     __syncthreads();
+    return r;
+}
+
+template <int EPL>
+__global__ void __launch_bounds__(512, 1) k_svd_qrj(const SvdSector *__restrict__ secs,
+                                                    const double2 *__restrict__ T64, float2 *__restrict__ Us,
+                                                    double *__restrict__ S, int *status, int *ranks, int max_sweeps,
+                                                    float tol, float qr_floor, int use_reg) {
+    constexpr int NT = 512, NW = NT / 32;
+    extern __shared__ float2 sw[];
+    __shared__ int rotated;
+    const SvdSector s = secs[blockIdx.x];
+    const int p = s.p, q = s.q, ldw = q + 1, kmax = min(p, q);
+    float2 *alph = sw + p * ldw;                          // [kmax] conj(alpha_k)
+    float *cn = reinterpret_cast<float *>(alph + kmax);   // [kmax + 1] column norms^2 (Jacobi), then norms
+    int *piv = reinterpret_cast<int *>(cn + kmax + 1);    // [kmax] pivot rows
+    int *done = piv + kmax;                               // [p] row already pivoted
+    // [qrj_xch_bytes(8 EPL, kmax)] exchange columns of the register-resident Jacobi (use_reg)
+    unsigned char *xch = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(done + p) + 15) & ~static_cast<uintptr_t>(15));
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+    double up = 1.0;
+    float fro2 = 0.f;
+    const int r = qrj_reduce(s, T64, sw, ldw, alph, piv, done, qr_floor, &up, &fro2);
+    if (r < 0) {  // a non-finite sector: its singular values are NaN (reported by the host)
+        for (int j = tid; j < q; j += NT) S[s.s_off + j] = nan("");
+        if (tid == 0) {
+            status[blockIdx.x] = 0;
+            ranks[blockIdx.x] = 0;
+        }
+        return;
+    }
 
     // ---- one-sided Jacobi on the r columns of M; the group width follows r
     // (r/2 pairs a round), the register capacity per lane follows EPL
@@ -880,6 +901,43 @@ __global__ void __launch_bounds__(512, 1) k_svd_qrj(const SvdSector *__restrict_
         status[blockIdx.x] = sweeps;
         ranks[blockIdx.x] = r;
     }
+}
+
+// Sectors too large for shared memory (mixed mode): the same load and
+// pivoted Householder reduction (qrj_reduce) on a global, L2-resident
+// workspace W (p rows of stride q + 1 at w_off[sector]), then M written
+// column-major into T32 (p x q at the sector's t_off, unscaled, columns r..q-1
+// zero) for the global-memory Jacobi, ranks[sector] = r.  A sector holding Inf
+// or NaN gets NaN in T32 and rank 0, so its singular values come out NaN.
+// Dynamic shared memory: alph [kmax] float2, piv [kmax] int, done [p] int.
+__global__ void __launch_bounds__(512, 1) k_svd_qr_g(const SvdSector *__restrict__ secs,
+                                                     const double2 *__restrict__ T64, float2 *__restrict__ W,
+                                                     const int64_t *__restrict__ w_off, float2 *__restrict__ T32,
+                                                     int *ranks, float qr_floor) {
+    extern __shared__ float2 sm_qr[];
+    const SvdSector s = secs[blockIdx.x];
+    const int p = s.p, q = s.q, ldw = q + 1, kmax = min(p, q);
+    float2 *sw = W + w_off[blockIdx.x];
+    float2 *alph = sm_qr;
+    int *piv = reinterpret_cast<int *>(alph + kmax);
+    int *done = piv + kmax;
+    double up = 1.0;
+    float fro2 = 0.f;
+    const int r = qrj_reduce(s, T64, sw, ldw, alph, piv, done, qr_floor, &up, &fro2);
+    float2 *out = T32 + s.t_off;
+    const int64_t pq = (int64_t)p * q;
+    if (r < 0) {
+        const float nanf_ = __int_as_float(0x7FC00000);
+        for (int64_t e = threadIdx.x; e < pq; e += blockDim.x) out[e] = make_float2(nanf_, nanf_);
+        if (threadIdx.x == 0) ranks[blockIdx.x] = 0;
+        return;
+    }
+    for (int64_t e = threadIdx.x; e < pq; e += blockDim.x) {
+        const int i = (int)(e % p), j = (int)(e / p);
+        const float2 v = j < r ? sw[(int64_t)i * ldw + j] : make_float2(0.f, 0.f);
+        out[e] = make_float2((float)((double)v.x * up), (float)((double)v.y * up));
+    }
+    if (threadIdx.x == 0) ranks[blockIdx.x] = r;
 }
 
 // singular values (as double), descending order, normalised U columns
@@ -1174,6 +1232,7 @@ int qrj_smem_limit(int dev) {
         KV_CUDA(cudaFuncSetAttribute(k_svd_qrj<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
         KV_CUDA(cudaFuncSetAttribute(k_svd_qrj<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
         KV_CUDA(cudaFuncSetAttribute(k_svd_qrj<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        KV_CUDA(cudaFuncSetAttribute(k_svd_qr_g, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
         g_qrj_smem[dev] = bytes;
         g_qrj_set[dev] = true;
     }
@@ -1251,6 +1310,28 @@ void sa_scatter(const std::vector<SaOut> &v, const double2 *X, double2 *out) {
     KV_CUDA(cudaGetLastError());
 }
 
+void svd_qr_global(const SvdPlan &p, const double2 *T64, float2 *T32, int *ranks, float qr_floor) {
+    if (p.secs.empty()) return;
+    std::vector<int64_t> w_off(p.secs.size());
+    int64_t w_elems = 0;
+    size_t smem = 0;
+    for (size_t i = 0; i < p.secs.size(); ++i) {
+        const SvdSector &sc = p.secs[i];
+        w_off[i] = w_elems;
+        w_elems += (int64_t)sc.p * (sc.q + 1);
+        const size_t kmax = (size_t)std::min(sc.p, sc.q);
+        smem = std::max(smem, kmax * (sizeof(float2) + sizeof(int)) + (size_t)sc.p * sizeof(int));
+    }
+    KV_REQUIRE(smem <= (size_t)qrj_smem_limit(ctx().device), KV_EINVAL,
+               "mixed-precision SVD: a sector has too many rows for the QR reduction");
+    DevBuf W(std::max<int64_t>(1, w_elems) * sizeof(float2));
+    DevBuf dw = upload_vec(w_off);
+    k_svd_qr_g<<<(unsigned)p.secs.size(), 512, smem, ctx().stream>>>(p.d_secs.as<SvdSector>(), T64, W.as<float2>(),
+                                                                      dw.as<int64_t>(), T32, ranks, qr_floor);
+    counted();
+    KV_CUDA(cudaGetLastError());
+}
+
 void svd_jacobi_f32(const SvdPlan &p, const double2 *T64, float2 *T, int *status, int max_sweeps, float tol) {
     if (p.secs.empty()) return;
     // dynamic shared memory: opt-in maximum less the static arrays and 4 KB,
@@ -1265,8 +1346,10 @@ void svd_jacobi_f32(const SvdPlan &p, const double2 *T64, float2 *T, int *status
     }
     const int cap = smem_bytes / (int)sizeof(float2);
     const int elems = (int)std::min<int64_t>(max_pq, cap);
-    k_to_f32<<<std::max(1, ctx().num_sms * 4), 256, 0, ctx().stream>>>(T64, T, p.t_elems);
-    counted();
+    if (T64) {
+        k_to_f32<<<std::max(1, ctx().num_sms * 4), 256, 0, ctx().stream>>>(T64, T, p.t_elems);
+        counted();
+    }
     // elements per lane from the longest column of the launch (16 lanes a pair)
     auto launch = [&](auto kernel) {
         kernel<<<(unsigned)p.secs.size(), 1024, (size_t)elems * sizeof(float2), ctx().stream>>>(

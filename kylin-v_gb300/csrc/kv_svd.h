@@ -71,6 +71,11 @@ constexpr int kJacobiMaxQ = 2048;
 // (T oriented so the wanted singular vectors are its columns), sorted
 // normalised columns and singular values, and the first k columns in FP64
 void svd_jacobi_f32(const SvdPlan &p, const double2 *T64, float2 *T, int *status, int max_sweeps, float tol);
+// (T64 == nullptr: T already holds the FP32 matrix)
+// mixed mode, sectors beyond shared memory: the QR reduction to numerical rank
+// (rows below qr_floor ||T||_F dropped) on an L2-resident workspace; T32 =
+// the rank-r factor, column-major, zero beyond column r; ranks[sector] = r
+void svd_qr_global(const SvdPlan &p, const double2 *T64, float2 *T32, int *ranks, float qr_floor);
 void svd_finalize_f32(const SvdPlan &p, const float2 *T, float2 *Us, double *S);
 // mixed mode, every sector in shared memory: pivoted Householder on T's rows
 // truncated where the remaining rows fall below qr_floor ||T||_F, one-sided
