@@ -1,12 +1,22 @@
-// Device block SVD for svd_impl (holstein/svd.h:296-440).
+// Device block SVD for svd_impl (holstein/svd.h:296-440) and the SA-1TDVP
+// split (holstein/svd.h:443-614).
 //
-// Each charge sector's dense matrix is gathered in tall orientation T (p x q,
-// p >= q, column-major; T = A or T = A^H), orthogonalised by one-sided
-// (Hestenes) Jacobi with round-robin ordering (one CTA per sector, each warp
-// rotates disjoint column pairs, rows split across lanes), and sorted by
-// descending singular value.  The host applies the reference's global
-// truncation and the scatter kernel writes the kept columns into the U and
-// S.V^H block tensors.
+// Each charge sector's dense matrix is gathered as T (p x q, column-major;
+// T = A or T = A^H) and factorised by one CTA:
+//  * FP64 mode: T tall (p >= q), one-sided (Hestenes) Jacobi with round-robin
+//    ordering and accumulated rotations (k_svd_jacobi), sorted by descending
+//    singular value (k_svd_finalize);
+//  * mixed mode: T oriented so the wanted singular vectors are its columns, a
+//    pivoted Householder reduction of its rows to the numerical rank, then
+//    FP32 one-sided Jacobi on the rank-r factor, all in shared memory
+//    (k_svd_qrj, the Jacobi with the columns in registers); sectors beyond
+//    shared memory take the same reduction on an L2-resident workspace
+//    (k_svd_qr_g) and the global-memory Jacobi (k_svd_jacobi_w).  The FP64
+//    rebuild of the kept factor (k_svd_extract, k_col_norm2, k_chol,
+//    k_trsm_rows with the FP64 GEMM) runs after the host's truncation.
+// The host applies the reference's global truncation and the scatter kernel
+// writes the kept columns into the U and S.V^H block tensors; the SA split's
+// new directions come from k_sa_basis / k_sa_subtract / k_sa_scatter.
 #include <mutex>
 #include "kv_internal.h"
 #include "kv_jacobi.cuh"
