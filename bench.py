@@ -288,6 +288,7 @@ def run_ours(args):
             plan_ms += hs["plan_ms"]
     barrier()
     prof = G.profile_read()
+    lz = G.profile_read_lanczos()
     G.profile(False)
     launches = G.launches() - n0
     svd = G.svd_stats(reset=True)
@@ -361,6 +362,7 @@ def run_ours(args):
                      "flops_per_launch": per_launch, "launches": prof["gemm_launches"],
                      "peak_source": f"dense FP16/BF16 tensor rate, {src} ({bf16:.1f} TFLOP/s bf16); "
                                     "achieved counts the reference's 8MNK flops of the block pairs"},
+        "roofline_lanczos": lanczos_roofline(lz, hbm, src),
         "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
         "svd_sectors": {"per_step": svd["sectors"] / args.steps, "mean_columns": svd["mean_columns"],
                         "mean_rank": svd["mean_rank"], "mean_jacobi_sweeps": svd["mean_sweeps"],
@@ -376,6 +378,21 @@ def run_ours(args):
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
         line["cpu_baseline"]["ms_per_step"] = cb["ms_per_step"]
     print(json.dumps(line), flush=True)
+
+
+def lanczos_roofline(lz, hbm, src):
+    """The Lanczos step (two overlaps, two subtractions, the norm and the
+    normalisation of one iteration, one cooperative launch): its algorithmic
+    bytes (16 B per complex element moved) over its event-timed duration,
+    against the measured HBM copy rate.  The step's vectors were written by
+    the H_eff apply just before it, so at this size much of it is served from
+    L2 and frac can pass 1."""
+    if not lz["launches"]:
+        return None
+    achieved = lz["bytes"] / (lz["ms"] / 1e3) / 1e9
+    return {"bound": "hbm", "kernel": "k_lanczos_step", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm, "bytes_per_launch": lz["bytes"] / lz["launches"], "launches": lz["launches"],
+            "us_per_launch": lz["ms"] * 1e3 / lz["launches"], "peak_source": f"HBM copy, {src}"}
 
 
 def compare_fp64(args, G):

@@ -228,6 +228,14 @@ int kv_sweep_batched(int n_chains, const kv_tdvp *chains, int mode, int steps, i
  * kv_counters returns the number of kernels launched since kv_init. */
 int kv_profile(int enable);
 int kv_profile_read(double *gemm_ms, double *gemm_ref_flops, long long *gemm_launches);
+/* With profiling on: the Lanczos steps (one per iteration after the H_eff
+ * apply) that ran since the last read, resolved at the end of each sweep:
+ * their device ms, their algorithmic bytes (16 B per complex element moved:
+ * 4 per element of v_{k-1}'s support, 4 per element of v_k's, 3 per element
+ * of v_{k+1}'s, for the two overlaps, the two subtractions, the norm and the
+ * normalisation) and their number; the counters are cleared.  No reference
+ * counterpart. */
+int kv_profile_read_lanczos(double *ms, double *bytes, long long *launches);
 int kv_counters(long long *launches);
 /* Charge sectors factorised by the block SVD on the calling thread's stream
  * since kv_init (or the last reset): their count, summed column counts, summed

@@ -510,6 +510,18 @@ int kv_profile(int enable) {
     });
 }
 
+int kv_profile_read_lanczos(double *ms, double *bytes, long long *launches) {
+    return guard([&] {
+        kv::require_init();
+        auto &c = kv::ctx();
+        if (ms) *ms = c.lz_ms;
+        if (bytes) *bytes = c.lz_bytes;
+        if (launches) *launches = c.lz_launches;
+        c.lz_ms = c.lz_bytes = 0.0;
+        c.lz_launches = 0;
+    });
+}
+
 int kv_profile_read(double *gemm_ms, double *gemm_ref_flops, long long *gemm_launches) {
     return guard([&] {
         kv::require_init();

@@ -385,9 +385,18 @@ void prof_resolve(int (*iters_of)(const KrylovState *, void *), void *arg) {
     for (auto &r : c.prof_pending) {
         float ms = 0.f;
         KV_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
-        c.prof_ms += ms;
-        c.prof_launches += 1;
-        if (!r.st || (iters_of && r.k < iters_of(r.st, arg))) c.prof_flops += r.flops;
+        const bool ran = !r.st || (iters_of && r.k < iters_of(r.st, arg));
+        if (r.lanczos) {
+            if (ran) {  // a step past the stop returns at once: neither its time nor bytes count
+                c.lz_ms += ms;
+                c.lz_bytes += r.flops;
+                c.lz_launches += 1;
+            }
+        } else {
+            c.prof_ms += ms;
+            c.prof_launches += 1;
+            if (ran) c.prof_flops += r.flops;
+        }
         c.ev_free.push_back(r.a);
         c.ev_free.push_back(r.b);
     }
@@ -751,8 +760,24 @@ TensorP op_lanczos(int nsite, const DTensor &L, const DTensor &psi, const DTenso
             if (*reinterpret_cast<volatile int *>(c.stop_host)) break;
         }
         run_heff(H, w, L, V + voff[k], W1, W2, R, hv.as<double2>(), dt * 0.5, precision, skip, st_dev, k);
+        ProfRec rec{};
+        if (c.prof) {
+            // algorithmic bytes, 16 B per element: overlap with v_{k-1} (hv,
+            // v_{k-1} on its support), subtract it and overlap with v_k (hv, v_k;
+            // v_{k-1} read and hv written on v_{k-1}'s support), subtract v_k
+            // and take the norm (hv; v_k read and hv written on v_k's support),
+            // normalise (hv read, v_{k+1} written)
+            const double n_prev = k > 0 ? (double)nl.n[k - 1] : 0.0;
+            rec = {prof_event(), prof_event(), 16.0 * (4 * n_prev + 4 * (double)nl.n[k] + 3 * (double)nl.n[k + 1]),
+                   st_dev, k, 1};
+            KV_CUDA(cudaEventRecord(rec.a, c.stream));
+        }
         krylov_step(st_dev, k, hv.as<double2>(), k > 0 ? V + voff[k - 1] : nullptr, V + voff[k], V + voff[k + 1], nl,
                     parts.as<double2>(), tol, max_iter, c.stop_dev);
+        if (c.prof) {
+            KV_CUDA(cudaEventRecord(rec.b, c.stream));
+            c.prof_pending.push_back(rec);
+        }
         KV_CUDA(cudaEventRecord(c.iter_ev[k], c.stream));
         ++c.krylov_issued;
     }

@@ -42,14 +42,16 @@ struct Error : std::runtime_error {
 // ------------------------------------------------------------------ context
 struct KrylovState;
 
-// One profiled grouped-GEMM launch: its events, the reference flops of the
-// block pairs it multiplies, and (for Lanczos applies) the Krylov state and
-// iteration whose stop flag may have skipped it.
+// One profiled launch: its events, the reference flops of the block pairs a
+// grouped GEMM multiplies (or the algorithmic bytes of a Lanczos step), and
+// (for Lanczos iterations) the Krylov state and iteration whose stop flag may
+// have skipped it.
 struct ProfRec {
     cudaEvent_t a, b;
     double flops;
     const KrylovState *st;
     int k;
+    int lanczos = 0;  // 1: a Lanczos step (flops holds bytes)
 };
 
 struct PlanCache;  // H_eff plans keyed by block structure (kv_engine.cu)
@@ -68,6 +70,9 @@ struct Context {
     std::vector<cudaEvent_t> ev_free;
     double prof_ms = 0.0, prof_flops = 0.0;
     long long prof_launches = 0;
+    // profiled Lanczos steps that ran: device ms, algorithmic bytes, launches
+    double lz_ms = 0.0, lz_bytes = 0.0;
+    long long lz_launches = 0;
     // pinned staging ring for plan uploads: kRingChunks chunks of kRingChunk bytes
     static constexpr int kRingChunks = 16;
     static constexpr size_t kRingChunk = 4u << 20;

@@ -33,7 +33,7 @@ EXPORTS = (
     "kv_expectation", "kv_profile", "kv_profile_read", "kv_counters", "kv_expectation_noalloc",
     "kv_tdvp_host_stats", "kv_canonicalize", "kv_sweep_batched", "kv_adjoint_heff", "kv_adjoint_env",
     "kv_debug_gemm_stall", "kv_debug_pool_usage", "kv_svd_stats", "kv_krylov_stats", "kv_tdvp_set_sa",
-    "kv_tdvp_svs", "kv_tdvp_window", "kv_local_expectations",
+    "kv_tdvp_svs", "kv_profile_read_lanczos", "kv_tdvp_window", "kv_local_expectations",
 )
 
 
@@ -79,6 +79,7 @@ def lib():
         L.kv_tdvp_host_stats.argtypes = [vp, dp, dp, ctypes.POINTER(ctypes.c_longlong), dp]
         L.kv_profile.argtypes = [ctypes.c_int]
         L.kv_profile_read.argtypes = [dp, dp, ctypes.POINTER(ctypes.c_longlong)]
+        L.kv_profile_read_lanczos.argtypes = [dp, dp, ctypes.POINTER(ctypes.c_longlong)]
         L.kv_counters.argtypes = [ctypes.POINTER(ctypes.c_longlong)]
         L.kv_tdvp_free.argtypes = [vp]
         L.kv_expectation.argtypes = [ctypes.c_int, pvp, pvp, pvp, dp, dp]
@@ -274,6 +275,13 @@ def canonicalize(mps, tol_svd=0.0, max_dim=1000, precision=KV_FP64) -> list:
 def profile(enable: bool):
     """Bracket every grouped-GEMM launch with CUDA events (instrumentation)."""
     check(lib().kv_profile(int(enable)))
+
+
+def profile_read_lanczos() -> dict:
+    """Profiled Lanczos steps since the last read: device ms, algorithmic bytes, launches."""
+    ms, b, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
+    check(lib().kv_profile_read_lanczos(ctypes.byref(ms), ctypes.byref(b), ctypes.byref(n)))
+    return {"ms": ms.value, "bytes": b.value, "launches": n.value}
 
 
 def profile_read() -> dict:
