@@ -105,7 +105,13 @@ __global__ void __launch_bounds__(256) k_gemm_fp64(const GemmTile *__restrict__ 
 
 // ------------------------------------------------------------------ mix
 // out[k, k2, r, n] = sum_terms sum_kk W[k2, kk, r] in[k, kk, n]; one CTA per
-// (job, 1024-element chunk).
+// (job, 1024-element chunk).  The FP64 unit (two thread-operations per clock
+// per SM on GB300) bounds this kernel, and an MPO's local operators are
+// mostly zeros and real: a zero W entry adds nothing and is skipped, a real
+// one takes two fused multiply-adds instead of four.  Consecutive threads
+// share (k2, r), so the branch is uniform across a warp where n spans it;
+// for finite inputs the sums equal the four-FMA product's (up to the sign
+// of a zero sum).
 constexpr int MIX_CHUNK = 1024;
 
 __global__ void __launch_bounds__(256) k_mix(const MixItem *__restrict__ items, const MixJob *__restrict__ jobs,
@@ -133,7 +139,17 @@ __global__ void __launch_bounds__(256) k_mix(const MixItem *__restrict__ items, 
             if (tm.entry > step) continue;
             const double2 *w = W + tm.w_off + (k2 * tm.K) * jb.wr + r;
             const double2 *x = in + tm.in_off + (k * tm.K) * jb.rest + n;
-            for (int kk = 0; kk < tm.K; ++kk) cfma(acc, w[(int64_t)kk * jb.wr], x[(int64_t)kk * jb.rest]);
+            for (int kk = 0; kk < tm.K; ++kk) {
+                const double2 wv = w[(int64_t)kk * jb.wr];
+                if (wv.y == 0.0) {
+                    if (wv.x == 0.0) continue;
+                    const double2 xv = x[(int64_t)kk * jb.rest];
+                    acc.x = fma(wv.x, xv.x, acc.x);
+                    acc.y = fma(wv.x, xv.y, acc.y);
+                } else {
+                    cfma(acc, wv, x[(int64_t)kk * jb.rest]);
+                }
+            }
         }
         out[jb.out_off + e] = acc;
     }

@@ -20,41 +20,84 @@ constexpr double kMaxTridiagNorm = 1e5;  // largest ||T||_1 the Taylor sub-stepp
 
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 
-// conj(x) * y
-__device__ __forceinline__ double2 cdotc(double2 x, double2 y) {
-    return make_double2(x.x * y.x + x.y * y.y, x.x * y.y - x.y * y.x);
+// GB300's FP64 unit issues two thread-operations per clock per SM, so the
+// vector kernels below are bound by their FP64 operation count: products are
+// accumulated with fused multiply-adds, and reductions add only where a sum
+// is used.
+
+// s + conj(x) y, two fused multiply-adds a component
+__device__ __forceinline__ double2 cdotc_acc(double2 s, double2 x, double2 y) {
+    s.x = fma(x.x, y.x, fma(x.y, y.y, s.x));
+    s.y = fma(x.x, y.y, fma(-x.y, y.x, s.y));
+    return s;
 }
 
-__device__ double2 block_sum(double2 v) {
-    __shared__ double2 red[KT / 32];
-    for (int o = 16; o > 0; o >>= 1) {
-        v.x += __shfl_down_sync(0xffffffffu, v.x, o);
-        v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+// h - c x
+__device__ __forceinline__ double2 csub_mul(double2 h, double2 c, double2 x) {
+    h.x = fma(-c.x, x.x, fma(c.y, x.y, h.x));
+    h.y = fma(-c.x, x.y, fma(-c.y, x.x, h.y));
+    return h;
+}
+
+// s + c x
+__device__ __forceinline__ double2 cmul_acc(double2 s, double2 c, double2 x) {
+    s.x = fma(c.x, x.x, fma(-c.y, x.y, s.x));
+    s.y = fma(c.x, x.y, fma(c.y, x.x, s.y));
+    return s;
+}
+
+// s + |h|^2
+__device__ __forceinline__ double norm2_acc(double s, double2 h) { return fma(h.x, h.x, fma(h.y, h.y, s)); }
+
+// lane 0 receives the sum of the warp's values (a tree in which, at each
+// level, only the lanes whose sums reach lane 0 add)
+template <int W = 32>
+__device__ __forceinline__ double2 warp_sum0(double2 v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = W / 2; o > 0; o >>= 1) {
+        const double tx = __shfl_down_sync(0xffffffffu, v.x, o);
+        const double ty = __shfl_down_sync(0xffffffffu, v.y, o);
+        if (lane < o) {
+            v.x += tx;
+            v.y += ty;
+        }
     }
+    return v;
+}
+
+// the block's sum, returned to every thread; a fixed order of adds
+__device__ double2 block_sum(double2 v) {
+    constexpr int NW = KT / 32;
+    static_assert(NW <= 32 && (NW & (NW - 1)) == 0, "warp count a power of two");
+    __shared__ double2 red[NW];
+    __shared__ double2 out;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    __syncthreads();
+    v = warp_sum0(v);
+    __syncthreads();  // a previous call's readers of red are done
     if (lane == 0) red[w] = v;
     __syncthreads();
-    double2 s = make_double2(0.0, 0.0);
-    if (threadIdx.x == 0)
-        for (int i = 0; i < KT / 32; ++i) s = cadd(s, red[i]);
-    __shared__ double2 out;
-    if (threadIdx.x == 0) out = s;
+    if (w == 0) {
+        double2 s = lane < NW ? red[lane] : make_double2(0.0, 0.0);
+        s = warp_sum0<NW>(s);
+        if (lane == 0) out = s;
+    }
     __syncthreads();
     return out;
 }
 
 // every CTA reduces the same partial array in the same order
 __device__ double2 reduce_partials(const double2 *parts, int nparts) {
-    double2 v = make_double2(0.0, 0.0);
-    for (int i = threadIdx.x; i < nparts; i += KT) v = cadd(v, parts[i]);
+    int i = threadIdx.x;
+    double2 v = i < nparts ? parts[i] : make_double2(0.0, 0.0);
+    for (i += KT; i < nparts; i += KT) v = cadd(v, parts[i]);
     return block_sum(v);
 }
 
 __global__ void __launch_bounds__(KT) k_norm_part(const double2 *x, int64_t n, double2 *parts) {
     double s = 0.0;
     for (int64_t i = blockIdx.x * (int64_t)KT + threadIdx.x; i < n; i += (int64_t)gridDim.x * KT)
-        s += x[i].x * x[i].x + x[i].y * x[i].y;
+        s = norm2_acc(s, x[i]);
     double2 r = block_sum(make_double2(s, 0.0));
     if (threadIdx.x == 0) parts[blockIdx.x] = r;
 }
@@ -90,7 +133,7 @@ __global__ void __launch_bounds__(KT) k_dot_part(const KrylovState *st, const do
     if (st->done) return;
     double2 s = make_double2(0.0, 0.0);
     for (int64_t i = blockIdx.x * (int64_t)KT + threadIdx.x; i < n; i += (int64_t)gridDim.x * KT)
-        s = cadd(s, cdotc(x[i], y[i]));
+        s = cdotc_acc(s, x[i], y[i]);
     double2 r = block_sum(s);
     if (threadIdx.x == 0) parts[blockIdx.x] = r;
 }
@@ -108,13 +151,11 @@ __global__ void __launch_bounds__(KT) k_sub(KrylovState *st, double2 *hv, const 
     for (int64_t i = blockIdx.x * (int64_t)KT + threadIdx.x; i < n_dot; i += (int64_t)gridDim.x * KT) {
         double2 h = hv[i];
         if (i < n_sub) {
-            const double2 x = v[i];
-            h.x -= c.x * x.x - c.y * x.y;
-            h.y -= c.x * x.y + c.y * x.x;
+            h = csub_mul(h, c, v[i]);
             hv[i] = h;
         }
-        if (w) s = cadd(s, cdotc(h, w[i]));
-        else s.x += h.x * h.x + h.y * h.y;
+        if (w) s = cdotc_acc(s, h, w[i]);
+        else s.x = norm2_acc(s.x, h);
     }
     double2 r = block_sum(s);
     if (threadIdx.x == 0) pout[blockIdx.x] = r;
@@ -167,7 +208,7 @@ __global__ void __launch_bounds__(KT) k_lanczos_step(KrylovState *st, int k, dou
     const int64_t i0 = blockIdx.x * (int64_t)KT + threadIdx.x, di = (int64_t)gridDim.x * KT;
     if (k > 0) {
         double2 s = make_double2(0.0, 0.0);
-        for (int64_t i = i0; i < n_prev; i += di) s = cadd(s, cdotc(hv[i], vprev[i]));
+        for (int64_t i = i0; i < n_prev; i += di) s = cdotc_acc(s, hv[i], vprev[i]);
         double2 r = block_sum(s);
         if (threadIdx.x == 0) P0[blockIdx.x] = r;
         grid.sync();
@@ -177,18 +218,16 @@ __global__ void __launch_bounds__(KT) k_lanczos_step(KrylovState *st, int k, dou
         for (int64_t i = i0; i < n_k; i += di) {
             double2 h = hv[i];
             if (i < n_prev) {
-                const double2 x = vprev[i];
-                h.x -= c.x * x.x - c.y * x.y;
-                h.y -= c.x * x.y + c.y * x.x;
+                h = csub_mul(h, c, vprev[i]);
                 hv[i] = h;
             }
-            s = cadd(s, cdotc(h, vk[i]));
+            s = cdotc_acc(s, h, vk[i]);
         }
         r = block_sum(s);
         if (threadIdx.x == 0) P1[blockIdx.x] = r;
     } else {
         double2 s = make_double2(0.0, 0.0);
-        for (int64_t i = i0; i < n_k; i += di) s = cadd(s, cdotc(hv[i], vk[i]));
+        for (int64_t i = i0; i < n_k; i += di) s = cdotc_acc(s, hv[i], vk[i]);
         const double2 r = block_sum(s);
         if (threadIdx.x == 0) P1[blockIdx.x] = r;
     }
@@ -200,12 +239,10 @@ __global__ void __launch_bounds__(KT) k_lanczos_step(KrylovState *st, int k, dou
         for (int64_t i = i0; i < n_next; i += di) {
             double2 h = hv[i];
             if (i < n_k) {
-                const double2 x = vk[i];
-                h.x -= c.x * x.x - c.y * x.y;
-                h.y -= c.x * x.y + c.y * x.x;
+                h = csub_mul(h, c, vk[i]);
                 hv[i] = h;
             }
-            s.x += h.x * h.x + h.y * h.y;
+            s.x = norm2_acc(s.x, h);
         }
         const double2 r = block_sum(s);
         if (threadIdx.x == 0) P0[blockIdx.x] = r;
@@ -292,9 +329,7 @@ __global__ void __launch_bounds__(KT) k_combine(const KrylovState *st, double2 *
         double2 acc = make_double2(0.0, 0.0);
         for (int j = 0; j < m; ++j) {
             if (i >= nl.n[j]) continue;
-            const double2 c = st->coef[j], v = V[j][i];
-            acc.x += c.x * v.x - c.y * v.y;
-            acc.y += c.x * v.y + c.y * v.x;
+            acc = cmul_acc(acc, st->coef[j], V[j][i]);
         }
         out[i] = acc;
     }
