@@ -360,7 +360,7 @@ MixPlanFull plan_mix(const Meta &lm, const Meta &W, int lead, const std::vector<
         j.term_end = start[b + 1];
         const int job = (int)R.mix.jobs.size();
         R.mix.jobs.push_back(j);
-        for (int64_t s = 0; s < j.count; s += 1024) R.mix.items.push_back({job, s});
+        for (int64_t s = 0; s < j.count; s += kMixChunk) R.mix.items.push_back({job, s});
     }
     return R;
 }

@@ -358,6 +358,9 @@ struct MixJob {
     int nk_unused, so, wr, rest;
     int term_begin, term_end;
 };
+// elements of one job handled by one CTA of the mixing kernel (256 threads,
+// one element each): small jobs still spread over many SMs
+constexpr int kMixChunk = 256;
 struct MixItem {  // a chunk of one job handled by one CTA
     int job;
     int64_t start;

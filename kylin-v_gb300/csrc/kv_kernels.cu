@@ -105,14 +105,13 @@ __global__ void __launch_bounds__(256) k_gemm_fp64(const GemmTile *__restrict__ 
 
 // ------------------------------------------------------------------ mix
 // out[k, k2, r, n] = sum_terms sum_kk W[k2, kk, r] in[k, kk, n]; one CTA per
-// (job, 1024-element chunk).  The FP64 unit (two thread-operations per clock
+// (job, kMixChunk-element chunk).  The FP64 unit (two thread-operations per clock
 // per SM on GB300) bounds this kernel, and an MPO's local operators are
 // mostly zeros and real: a zero W entry adds nothing and is skipped, a real
 // one takes two fused multiply-adds instead of four.  Consecutive threads
 // share (k2, r), so the branch is uniform across a warp where n spans it;
 // for finite inputs the sums equal the four-FMA product's (up to the sign
 // of a zero sum).
-constexpr int MIX_CHUNK = 1024;
 
 __global__ void __launch_bounds__(256) k_mix(const MixItem *__restrict__ items, const MixJob *__restrict__ jobs,
                                              const MixTerm *__restrict__ terms, const double2 *__restrict__ in,
@@ -126,7 +125,7 @@ __global__ void __launch_bounds__(256) k_mix(const MixItem *__restrict__ items, 
         for (int ti = jb.term_begin; ti < jb.term_end; ++ti) any = any || terms[ti].entry <= step;
         if (!any) return;
     }
-    for (int j = threadIdx.x; j < MIX_CHUNK; j += blockDim.x) {
+    for (int j = threadIdx.x; j < kMixChunk; j += blockDim.x) {
         int64_t e = it.start + j;
         if (e >= jb.count) break;
         int64_t n = e % jb.rest;

@@ -21,9 +21,9 @@ constexpr double kMaxTridiagNorm = 1e5;  // largest ||T||_1 the Taylor sub-stepp
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 
 // GB300's FP64 unit issues two thread-operations per clock per SM, so the
-// vector kernels below are bound by their FP64 operation count: products are
-// accumulated with fused multiply-adds, and reductions add only where a sum
-// is used.
+// vector kernels below are bound by their FP64 operation count and latency:
+// products are accumulated with fused multiply-adds (two a component), and a
+// block's warp sums are combined by a shuffle tree instead of one thread.
 
 // s + conj(x) y, two fused multiply-adds a component
 __device__ __forceinline__ double2 cdotc_acc(double2 s, double2 x, double2 y) {
@@ -49,19 +49,13 @@ __device__ __forceinline__ double2 cmul_acc(double2 s, double2 c, double2 x) {
 // s + |h|^2
 __device__ __forceinline__ double norm2_acc(double s, double2 h) { return fma(h.x, h.x, fma(h.y, h.y, s)); }
 
-// lane 0 receives the sum of the warp's values (a tree in which, at each
-// level, only the lanes whose sums reach lane 0 add)
+// lane 0 receives the sum of the warp's first W values (a shuffle tree)
 template <int W = 32>
 __device__ __forceinline__ double2 warp_sum0(double2 v) {
-    const int lane = threadIdx.x & 31;
 #pragma unroll
     for (int o = W / 2; o > 0; o >>= 1) {
-        const double tx = __shfl_down_sync(0xffffffffu, v.x, o);
-        const double ty = __shfl_down_sync(0xffffffffu, v.y, o);
-        if (lane < o) {
-            v.x += tx;
-            v.y += ty;
-        }
+        v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_down_sync(0xffffffffu, v.y, o);
     }
     return v;
 }
