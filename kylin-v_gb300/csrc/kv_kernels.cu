@@ -105,13 +105,13 @@ __global__ void __launch_bounds__(256) k_gemm_fp64(const GemmTile *__restrict__ 
 
 // ------------------------------------------------------------------ mix
 // out[k, k2, r, n] = sum_terms sum_kk W[k2, kk, r] in[k, kk, n]; one CTA per
-// (job, kMixChunk-element chunk).  The FP64 unit (two thread-operations per clock
-// per SM on GB300) bounds this kernel, and an MPO's local operators are
-// mostly zeros and real: a zero W entry adds nothing and is skipped, a real
-// one takes two fused multiply-adds instead of four.  Consecutive threads
-// share (k2, r), so the branch is uniform across a warp where n spans it;
-// for finite inputs the sums equal the four-FMA product's (up to the sign
-// of a zero sum).
+// (job, chunk of kMixChunk elements).  The FP64 unit (two thread-operations
+// per clock per SM on GB300) bounds this kernel, and an MPO's local operators
+// are mostly zeros and real: a zero W entry adds nothing and is skipped, a
+// real one takes two fused multiply-adds instead of four.  Consecutive
+// threads share (k2, r), so the branch is uniform across a warp where n spans
+// it; for finite inputs the sums equal the four-FMA product's (up to the
+// sign of a zero sum).
 
 __global__ void __launch_bounds__(256) k_mix(const MixItem *__restrict__ items, const MixJob *__restrict__ jobs,
                                              const MixTerm *__restrict__ terms, const double2 *__restrict__ in,
