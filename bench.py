@@ -21,6 +21,9 @@ roofline   the grouped block-sparse GEMM on the tensor cores: reference flops
            of its block pairs / its event-timed duration, against the
            measured dense FP16/BF16 tensor peak (the digit GEMM runs on the
            FP16 pipe); traffic from the committed ncu summary.
+roofline_lanczos, roofline_mix  the Lanczos step and the MPO mixing kernels:
+           algorithmic bytes / event-timed duration against the measured HBM
+           copy rate (bytes_roofline).
 fp64_compare  the mixed path against the plain FP64 GPU path on the same
            chain over --compare-steps steps (default 1): time per step and the
            largest site-population and energy differences.
@@ -289,6 +292,7 @@ def run_ours(args):
     barrier()
     prof = G.profile_read()
     lz = G.profile_read_lanczos()
+    mx = G.profile_read_mix()
     G.profile(False)
     launches = G.launches() - n0
     svd = G.svd_stats(reset=True)
@@ -362,7 +366,8 @@ def run_ours(args):
                      "flops_per_launch": per_launch, "launches": prof["gemm_launches"],
                      "peak_source": f"dense FP16/BF16 tensor rate, {src} ({bf16:.1f} TFLOP/s bf16); "
                                     "achieved counts the reference's 8MNK flops of the block pairs"},
-        "roofline_lanczos": lanczos_roofline(lz, hbm, src),
+        "roofline_lanczos": bytes_roofline(lz, "k_lanczos_step", hbm, src),
+        "roofline_mix": bytes_roofline(mx, "k_mix", hbm, src),
         "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
         "svd_sectors": {"per_step": svd["sectors"] / args.steps, "mean_columns": svd["mean_columns"],
                         "mean_rank": svd["mean_rank"], "mean_jacobi_sweeps": svd["mean_sweeps"],
@@ -380,19 +385,21 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
 
 
-def lanczos_roofline(lz, hbm, src):
-    """The Lanczos step (two overlaps, two subtractions, the norm and the
-    normalisation of one iteration, one cooperative launch): its algorithmic
-    bytes (16 B per complex element moved) over its event-timed duration,
-    against the measured HBM copy rate.  The step's vectors were written by
-    the H_eff apply just before it, so at this size much of it is served from
-    L2 and frac can pass 1."""
-    if not lz["launches"]:
+def bytes_roofline(rec, kernel, hbm, src):
+    """A streaming kernel's algorithmic bytes over its event-timed duration,
+    against the measured HBM copy rate.  k_lanczos_step: the two overlaps,
+    two subtractions, norm and normalisation of one Lanczos iteration (16 B
+    per complex element moved); k_mix: the MPO mixings of the H_eff applies
+    and environment updates (per output element 16 B written and 16 B read
+    per contracted index of each active term).  Their inputs were written by
+    the launch just before, so at these sizes much of the traffic is served
+    from L2 and frac can pass 1."""
+    if not rec["launches"] or rec["ms"] <= 0.0:
         return None
-    achieved = lz["bytes"] / (lz["ms"] / 1e3) / 1e9
-    return {"bound": "hbm", "kernel": "k_lanczos_step", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-            "frac": achieved / hbm, "bytes_per_launch": lz["bytes"] / lz["launches"], "launches": lz["launches"],
-            "us_per_launch": lz["ms"] * 1e3 / lz["launches"], "peak_source": f"HBM copy, {src}"}
+    achieved = rec["bytes"] / (rec["ms"] / 1e3) / 1e9
+    return {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm, "bytes_per_launch": rec["bytes"] / rec["launches"], "launches": rec["launches"],
+            "us_per_launch": rec["ms"] * 1e3 / rec["launches"], "peak_source": f"HBM copy, {src}"}
 
 
 def compare_fp64(args, G):

@@ -236,6 +236,10 @@ int kv_profile_read(double *gemm_ms, double *gemm_ref_flops, long long *gemm_lau
  * normalisation) and their number; the counters are cleared.  No reference
  * counterpart. */
 int kv_profile_read_lanczos(double *ms, double *bytes, long long *launches);
+/* The same for the MPO mixings of the sweep (inside the H_eff applies and
+ * the environment updates): algorithmic bytes = per output element 16 B
+ * written plus 16 B read per contracted index of every active term. */
+int kv_profile_read_mix(double *ms, double *bytes, long long *launches);
 int kv_counters(long long *launches);
 /* Charge sectors factorised by the block SVD on the calling thread's stream
  * since kv_init (or the last reset): their count, summed column counts, summed

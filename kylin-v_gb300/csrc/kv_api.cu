@@ -510,16 +510,24 @@ int kv_profile(int enable) {
     });
 }
 
-int kv_profile_read_lanczos(double *ms, double *bytes, long long *launches) {
+static int profile_read_bytes(int kind, double *ms, double *bytes, long long *launches) {
     return guard([&] {
         kv::require_init();
         auto &c = kv::ctx();
-        if (ms) *ms = c.lz_ms;
-        if (bytes) *bytes = c.lz_bytes;
-        if (launches) *launches = c.lz_launches;
-        c.lz_ms = c.lz_bytes = 0.0;
-        c.lz_launches = 0;
+        if (ms) *ms = c.bw_ms[kind];
+        if (bytes) *bytes = c.bw_bytes[kind];
+        if (launches) *launches = c.bw_launches[kind];
+        c.bw_ms[kind] = c.bw_bytes[kind] = 0.0;
+        c.bw_launches[kind] = 0;
     });
+}
+
+int kv_profile_read_lanczos(double *ms, double *bytes, long long *launches) {
+    return profile_read_bytes(kv::kProfLanczos, ms, bytes, launches);
+}
+
+int kv_profile_read_mix(double *ms, double *bytes, long long *launches) {
+    return profile_read_bytes(kv::kProfMix, ms, bytes, launches);
 }
 
 int kv_profile_read(double *gemm_ms, double *gemm_ref_flops, long long *gemm_launches) {

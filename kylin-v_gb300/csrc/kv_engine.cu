@@ -386,11 +386,11 @@ void prof_resolve(int (*iters_of)(const KrylovState *, void *), void *arg) {
         float ms = 0.f;
         KV_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
         const bool ran = !r.st || (iters_of && r.k < iters_of(r.st, arg));
-        if (r.lanczos) {
-            if (ran) {  // a step past the stop returns at once: neither its time nor bytes count
-                c.lz_ms += ms;
-                c.lz_bytes += r.flops;
-                c.lz_launches += 1;
+        if (r.kind != kProfGemm) {
+            if (ran) {  // a launch past the stop returns at once: neither its time nor bytes count
+                c.bw_ms[r.kind] += ms;
+                c.bw_bytes[r.kind] += r.flops;
+                c.bw_launches[r.kind] += 1;
             }
         } else {
             c.prof_ms += ms;
@@ -417,6 +417,42 @@ void run_gemm(const GemmPlan &g, const double2 *A, const double2 *B, double2 *C,
     if (precision == KV_FP64) launch_gemm_fp64(g, A, B, C, alpha, skip, step);
     else if (precision == KV_MIXED_TF32) launch_gemm_mixed(g, A, B, C, alpha, skip, step);
     else throw Error(KV_EINVAL, "unknown precision mode");
+    if (c.prof) {
+        KV_CUDA(cudaEventRecord(rec.b, c.stream));
+        c.prof_pending.push_back(rec);
+    }
+}
+
+// Algorithmic bytes of one mixing launch at Lanczos step `step`: each output
+// element reads 16 B of input per contracted index of every active term and
+// writes 16 B (the MPO blocks, a few KB, are left out).  A block with no
+// active term is written as zeros only where the plan writes inactive blocks.
+static double mix_bytes(const MixPlan &p, int step) {
+    double b = 0.0;
+    for (const MixJob &j : p.jobs) {
+        double per = 0.0;
+        bool any = false;
+        for (int t = j.term_begin; t < j.term_end; ++t)
+            if (p.terms[t].entry <= step) {
+                per += 16.0 * p.terms[t].K;
+                any = true;
+            }
+        if (any || p.write_inactive) b += (per + 16.0) * (double)j.count;
+    }
+    return b;
+}
+
+// launch_mix, event-timed with its algorithmic bytes when profiling is on
+static void run_mix(const MixPlan &p, const double2 *in, const double2 *W, double2 *out, const int *skip, int step,
+             const KrylovState *st, int k) {
+    if (p.items.empty()) return;
+    auto &c = ctx();
+    ProfRec rec{};
+    if (c.prof) {
+        rec = {prof_event(), prof_event(), mix_bytes(p, step), st, k, kProfMix};
+        KV_CUDA(cudaEventRecord(rec.a, c.stream));
+    }
+    launch_mix(p, in, W, out, skip, step);
     if (c.prof) {
         KV_CUDA(cudaEventRecord(rec.b, c.stream));
         c.prof_pending.push_back(rec);
@@ -672,11 +708,11 @@ void run_heff(const HeffPlan &H, HeffWork &w, const DTensor &L, const double2 *v
     const double2 *last = w.t1.as<double2>();
     const int step = k >= 0 ? k : kAllSteps;
     if (H.nsite >= 1) {
-        launch_mix(H.m1.mix, last, W1->data(), w.t2.as<double2>(), skip, step);
+        run_mix(H.m1.mix, last, W1->data(), w.t2.as<double2>(), skip, step, st, k);
         last = w.t2.as<double2>();
     }
     if (H.nsite == 2) {
-        launch_mix(H.m2.mix, last, W2->data(), w.t3.as<double2>(), skip, step);
+        run_mix(H.m2.mix, last, W2->data(), w.t3.as<double2>(), skip, step, st, k);
         last = w.t3.as<double2>();
     }
     run_gemm(H.p2.gemm, last, R.data(), out, scale, precision, skip, st, k, credit >= 0.0 ? 0.0 : -1.0);
@@ -769,7 +805,7 @@ TensorP op_lanczos(int nsite, const DTensor &L, const DTensor &psi, const DTenso
             // normalise (hv read, v_{k+1} written)
             const double n_prev = k > 0 ? (double)nl.n[k - 1] : 0.0;
             rec = {prof_event(), prof_event(), 16.0 * (4 * n_prev + 4 * (double)nl.n[k] + 3 * (double)nl.n[k + 1]),
-                   st_dev, k, 1};
+                   st_dev, k, kProfLanczos};
             KV_CUDA(cudaEventRecord(rec.a, c.stream));
         }
         krylov_step(st_dev, k, hv.as<double2>(), k > 0 ? V + voff[k - 1] : nullptr, V + voff[k], V + voff[k + 1], nl,
@@ -1421,7 +1457,7 @@ TensorP op_env(bool l2r, const DTensor &env, const DTensor &A, const DTensor &W,
     MixPlanFull M = plan_mix(t1->meta, W.meta, 1);
     M.mix.upload();
     auto t2 = DTensor::make(M.out, false);
-    launch_mix(M.mix, t1->data(), W.data(), t2->data(), nullptr);
+    run_mix(M.mix, t1->data(), W.data(), t2->data(), nullptr, kAllSteps, nullptr, -1);
     ProductPlan P2 = plan_product(A.meta, t2->meta, 2, KV_OP_C, KV_OP_N);
     // A's blocks pair with every (reference-unmerged) copy of each mixed block
     const double f2 = ref_product_flops(A.meta, M.out, 2, KV_OP_C, KV_OP_N, nullptr, &M.mult);

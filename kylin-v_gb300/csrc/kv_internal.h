@@ -43,15 +43,16 @@ struct Error : std::runtime_error {
 struct KrylovState;
 
 // One profiled launch: its events, the reference flops of the block pairs a
-// grouped GEMM multiplies (or the algorithmic bytes of a Lanczos step), and
-// (for Lanczos iterations) the Krylov state and iteration whose stop flag may
-// have skipped it.
+// grouped GEMM multiplies (or the algorithmic bytes of a Lanczos step or an
+// MPO mixing), and (for Lanczos iterations) the Krylov state and iteration
+// whose stop flag may have skipped it.
+enum ProfKind { kProfGemm = 0, kProfLanczos = 1, kProfMix = 2 };
 struct ProfRec {
     cudaEvent_t a, b;
     double flops;
     const KrylovState *st;
     int k;
-    int lanczos = 0;  // 1: a Lanczos step (flops holds bytes)
+    int kind = kProfGemm;  // kProfLanczos / kProfMix: flops holds bytes
 };
 
 struct PlanCache;  // H_eff plans keyed by block structure (kv_engine.cu)
@@ -70,9 +71,10 @@ struct Context {
     std::vector<cudaEvent_t> ev_free;
     double prof_ms = 0.0, prof_flops = 0.0;
     long long prof_launches = 0;
-    // profiled Lanczos steps that ran: device ms, algorithmic bytes, launches
-    double lz_ms = 0.0, lz_bytes = 0.0;
-    long long lz_launches = 0;
+    // profiled Lanczos steps and MPO mixings that ran, per ProfKind: device
+    // ms, algorithmic bytes, launches
+    double bw_ms[3] = {}, bw_bytes[3] = {};
+    long long bw_launches[3] = {};
     // pinned staging ring for plan uploads: kRingChunks chunks of kRingChunk bytes
     static constexpr int kRingChunks = 16;
     static constexpr size_t kRingChunk = 4u << 20;

@@ -33,7 +33,7 @@ EXPORTS = (
     "kv_expectation", "kv_profile", "kv_profile_read", "kv_counters", "kv_expectation_noalloc",
     "kv_tdvp_host_stats", "kv_canonicalize", "kv_sweep_batched", "kv_adjoint_heff", "kv_adjoint_env",
     "kv_debug_gemm_stall", "kv_debug_pool_usage", "kv_svd_stats", "kv_krylov_stats", "kv_tdvp_set_sa",
-    "kv_tdvp_svs", "kv_profile_read_lanczos", "kv_tdvp_window", "kv_local_expectations",
+    "kv_tdvp_svs", "kv_profile_read_lanczos", "kv_profile_read_mix", "kv_tdvp_window", "kv_local_expectations",
 )
 
 
@@ -80,6 +80,7 @@ def lib():
         L.kv_profile.argtypes = [ctypes.c_int]
         L.kv_profile_read.argtypes = [dp, dp, ctypes.POINTER(ctypes.c_longlong)]
         L.kv_profile_read_lanczos.argtypes = [dp, dp, ctypes.POINTER(ctypes.c_longlong)]
+        L.kv_profile_read_mix.argtypes = [dp, dp, ctypes.POINTER(ctypes.c_longlong)]
         L.kv_counters.argtypes = [ctypes.POINTER(ctypes.c_longlong)]
         L.kv_tdvp_free.argtypes = [vp]
         L.kv_expectation.argtypes = [ctypes.c_int, pvp, pvp, pvp, dp, dp]
@@ -277,11 +278,20 @@ def profile(enable: bool):
     check(lib().kv_profile(int(enable)))
 
 
+def _profile_read_bytes(fn) -> dict:
+    ms, b, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
+    check(fn(ctypes.byref(ms), ctypes.byref(b), ctypes.byref(n)))
+    return {"ms": ms.value, "bytes": b.value, "launches": n.value}
+
+
 def profile_read_lanczos() -> dict:
     """Profiled Lanczos steps since the last read: device ms, algorithmic bytes, launches."""
-    ms, b, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
-    check(lib().kv_profile_read_lanczos(ctypes.byref(ms), ctypes.byref(b), ctypes.byref(n)))
-    return {"ms": ms.value, "bytes": b.value, "launches": n.value}
+    return _profile_read_bytes(lib().kv_profile_read_lanczos)
+
+
+def profile_read_mix() -> dict:
+    """Profiled MPO mixings of the sweep since the last read: device ms, algorithmic bytes, launches."""
+    return _profile_read_bytes(lib().kv_profile_read_mix)
 
 
 def profile_read() -> dict:
