@@ -18,7 +18,8 @@ e2e        the same metric through the public C ABI with host buffers: every
            step uploads the MPS and MPO from pinned host memory, builds the
            environments, sweeps and downloads the MPS.
 roofline   the grouped block-sparse GEMM on the tensor cores: reference flops
-           of its block pairs / its event-timed duration, against the
+           of its block pairs / the event-timed duration of the GEMM calls
+           (operand slicing launch and GEMM launch together), against the
            measured dense FP16/BF16 tensor peak (the digit GEMM runs on the
            FP16 pipe); traffic from the committed ncu summary.
 roofline_lanczos, roofline_mix  the Lanczos step and the MPO mixing kernels:

@@ -427,19 +427,30 @@ void run_gemm(const GemmPlan &g, const double2 *A, const double2 *B, double2 *C,
 // element reads 16 B of input per contracted index of every active term and
 // writes 16 B (the MPO blocks, a few KB, are left out).  A block with no
 // active term is written as zeros only where the plan writes inactive blocks.
+// The figure changes only at the terms' entry steps (Lanczos iterations, so
+// small), so it is tabulated once per plan for steps 0 .. the last entry.
 static double mix_bytes(const MixPlan &p, int step) {
-    double b = 0.0;
-    for (const MixJob &j : p.jobs) {
-        double per = 0.0;
-        bool any = false;
-        for (int t = j.term_begin; t < j.term_end; ++t)
-            if (p.terms[t].entry <= step) {
-                per += 16.0 * p.terms[t].K;
-                any = true;
+    if (p.prof_bytes.empty()) {
+        constexpr int kMaxTabulated = 63;
+        int last = 0;
+        for (const MixTerm &t : p.terms) last = std::max(last, std::min(t.entry, kMaxTabulated));
+        p.prof_bytes.assign((size_t)last + 1, 0.0);
+        for (int s = 0; s <= last; ++s) {
+            double b = 0.0;
+            for (const MixJob &j : p.jobs) {
+                double per = 0.0;
+                bool any = false;
+                for (int t = j.term_begin; t < j.term_end; ++t)
+                    if (p.terms[t].entry <= s) {
+                        per += 16.0 * p.terms[t].K;
+                        any = true;
+                    }
+                if (any || p.write_inactive) b += (per + 16.0) * (double)j.count;
             }
-        if (any || p.write_inactive) b += (per + 16.0) * (double)j.count;
+            p.prof_bytes[s] = b;
+        }
     }
-    return b;
+    return p.prof_bytes[(size_t)std::min<int>(std::max(step, 0), (int)p.prof_bytes.size() - 1)];
 }
 
 // launch_mix, event-timed with its algorithmic bytes when profiling is on

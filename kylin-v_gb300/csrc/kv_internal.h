@@ -373,6 +373,9 @@ struct MixPlan {
     std::vector<MixItem> items;
     DevBuf d_terms, d_jobs, d_items;
     bool write_inactive = true;  // as GemmPlan::write_inactive, per output block
+    // profiling: algorithmic bytes of a launch at Lanczos step s (s clamped to
+    // the last entry step), filled on first use
+    mutable std::vector<double> prof_bytes;
     void upload() { d_terms = upload_vec(terms); d_jobs = upload_vec(jobs); d_items = upload_vec(items); }
 };
 
