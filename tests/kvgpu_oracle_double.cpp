@@ -1,0 +1,144 @@
+// Test double of libkvgpu's C ABI for host-side tests of the C++ layer
+// (include/holstein/kv_ops.h): the entry points that layer calls, with the
+// same signatures and argument meaning as include/kvgpu.h, answered by the
+// CPU oracle (oracle/_build/libkvoracle.so) instead of the GPU.  Built by
+// tests/test_ops_layer.py into a temporary libkvgpu.so; it never ships and
+// is never loaded by the product path.
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "kvgpu.h"
+
+extern "C" {
+const char *kvo_last_error();
+int kvo_tensor_new(int rank, const int *dirs, int nblocks, const int *shapes, const int *qns, const double *data,
+                   void **out);
+int kvo_tensor_info(void *h, int *rank, int *nblocks, long long *nelem);
+int kvo_tensor_get(void *h, int *dirs, int *shapes, int *qns, double *data);
+void kvo_tensor_free(void *h);
+int kvo_product(void *a, void *b, int nc, int ta, int tb, void **out);
+int kvo_apply(int nsite, void *L, void *psi, void *W1, void *W2, void *R, void **out);
+int kvo_env_sweep(void *env, void *A, void *W, int l2r, void **out);
+int kvo_local_krylov(int nsite, void *L, void *psi, void *W1, void *W2, void *R, double dt, int max_iter, double tol,
+                     int reverse, int *iters, void **out);
+int kvo_svd(void *A, int r1, int l2r, double tol, int max_dim, void **U, void **V, double *svals, int *nkept,
+            int *ntotal);
+}
+
+namespace {
+
+std::string g_err;
+long long g_calls = 0;  // operations answered (tensor I/O excluded)
+
+void *H(kv_tensor t) { return static_cast<void *>(t); }
+kv_tensor T(void *p) { return static_cast<kv_tensor>(p); }
+
+int status(int rc) {
+    if (rc == 0) return KV_OK;
+    g_err = kvo_last_error();
+    return KV_EINVAL;
+}
+
+}  // namespace
+
+extern "C" {
+
+int kv_init(int) { return KV_OK; }
+int kv_shutdown(void) { return KV_OK; }
+const char *kv_last_error(void) { return g_err.c_str(); }
+long long kv_double_calls(void) { return g_calls; }
+
+int kv_tensor_create(int rank, const int *dirs, int nblocks, const int *shapes, const int *qns, const double *data,
+                     kv_tensor *out) {
+    std::vector<double> zeros;
+    if (!data) {
+        long long n = 0;
+        for (int b = 0; b < nblocks; ++b) {
+            long long s = 1;
+            for (int i = 0; i < rank; ++i) s *= shapes[b * rank + i];
+            n += s;
+        }
+        zeros.assign(2 * (size_t)n + 2, 0.0);
+        data = zeros.data();
+    }
+    void *h = nullptr;
+    const int rc = kvo_tensor_new(rank, dirs, nblocks, shapes, qns, data, &h);
+    *out = T(h);
+    return status(rc);
+}
+
+int kv_tensor_info(kv_tensor t, int *rank, int *nblocks, long long *nelem) {
+    return status(kvo_tensor_info(H(t), rank, nblocks, nelem));
+}
+
+int kv_tensor_download(kv_tensor t, int *dirs, int *shapes, int *qns, double *data) {
+    return status(kvo_tensor_get(H(t), dirs, shapes, qns, data));
+}
+
+int kv_tensor_free(kv_tensor t) {
+    kvo_tensor_free(H(t));
+    return KV_OK;
+}
+
+int kv_product(kv_tensor A, kv_tensor B, int nc, int opA, int opB, int, kv_tensor *out) {
+    ++g_calls;
+    void *h = nullptr;
+    const int rc = kvo_product(H(A), H(B), nc, opA, opB, &h);
+    *out = T(h);
+    return status(rc);
+}
+
+int kv_heff_apply(int nsite, kv_tensor L, kv_tensor psi, kv_tensor W1, kv_tensor W2, kv_tensor R, double scale, int,
+                  kv_tensor *out) {
+    ++g_calls;
+    void *h = nullptr;
+    int rc = kvo_apply(nsite, H(L), H(psi), H(W1), H(W2), H(R), &h);
+    if (rc == 0 && scale != 1.0) {  // the oracle applies H_eff unscaled
+        int rank = 0, nb = 0;
+        long long ne = 0;
+        kvo_tensor_info(h, &rank, &nb, &ne);
+        std::vector<int> dirs(rank), sh((size_t)nb * rank), qn((size_t)nb * rank);
+        std::vector<double> d(2 * (size_t)ne + 2);
+        kvo_tensor_get(h, dirs.data(), sh.data(), qn.data(), d.data());
+        for (auto &x : d) x *= scale;
+        kvo_tensor_free(h);
+        rc = kvo_tensor_new(rank, dirs.data(), nb, sh.data(), qn.data(), d.data(), &h);
+    }
+    *out = T(h);
+    return status(rc);
+}
+
+int kv_env_update(int l2r, kv_tensor env, kv_tensor A, kv_tensor W, int, kv_tensor *out) {
+    ++g_calls;
+    void *h = nullptr;
+    const int rc = kvo_env_sweep(H(env), H(A), H(W), l2r, &h);
+    *out = T(h);
+    return status(rc);
+}
+
+int kv_lanczos_expm(int nsite, kv_tensor L, kv_tensor psi, kv_tensor W1, kv_tensor W2, kv_tensor R, double dt,
+                    int max_iter, double tol, int reverse, int, kv_tensor *out, int *iters) {
+    ++g_calls;
+    void *h = nullptr;
+    int it = 0;
+    const int rc = kvo_local_krylov(nsite, H(L), H(psi), H(W1), H(W2), H(R), dt, max_iter, tol, reverse, &it, &h);
+    *out = T(h);
+    if (iters) *iters = it;
+    return status(rc);
+}
+
+int kv_svd_truncate(kv_tensor A, int r1, int l2r, double tol, int max_dim, int, kv_tensor *U, kv_tensor *V,
+                    int *n_kept, int *n_total) {
+    ++g_calls;
+    void *u = nullptr, *v = nullptr;
+    int nk = 0, nt = 0;
+    const int rc = kvo_svd(H(A), r1, l2r, tol, max_dim, &u, &v, nullptr, &nk, &nt);
+    *U = T(u);
+    *V = T(v);
+    if (n_kept) *n_kept = nk;
+    if (n_total) *n_total = nt;
+    return status(rc);
+}
+
+}  // extern "C"
