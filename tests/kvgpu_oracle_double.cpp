@@ -1,9 +1,11 @@
 // Test double of libkvgpu's C ABI for host-side tests of the C++ layer
-// (include/holstein/kv_ops.h): the entry points that layer calls, with the
-// same signatures and argument meaning as include/kvgpu.h, answered by the
-// CPU oracle (oracle/_build/libkvoracle.so) instead of the GPU.  Built by
-// tests/test_ops_layer.py into a temporary libkvgpu.so; it never ships and
-// is never loaded by the product path.
+// (include/holstein/: kv_ops.h and the TDVP driver layer of kv_holstein.h):
+// the entry points that layer calls, with the same signatures and argument
+// meaning as include/kvgpu.h, answered by the CPU oracle
+// (oracle/_build/libkvoracle.so) instead of the GPU.  The sweep timings it
+// reports are zeros and it keeps no singular-value record.  Built by the
+// tests (kvtest_util.build_abi_double) into a temporary libkvgpu.so; it never
+// ships and is never loaded by the product path.
 #include <cstring>
 #include <string>
 #include <vector>
@@ -24,6 +26,12 @@ int kvo_local_krylov(int nsite, void *L, void *psi, void *W1, void *W2, void *R,
                      int reverse, int *iters, void **out);
 int kvo_svd(void *A, int r1, int l2r, double tol, int max_dim, void **U, void **V, double *svals, int *nkept,
             int *ntotal);
+int kvo_tdvp_new(int ns, void **mps, void **mpo, double tol_svd, double tol_exp, int max_dim, int max_iter,
+                 double dt, void **out);
+int kvo_tdvp_sweep(void *h, int mode);
+int kvo_tdvp_set_sa(void *h, const double *beta, int nbeta, unsigned long long seed);
+int kvo_tdvp_site(void *h, int i, void **out);
+void kvo_tdvp_free(void *h);
 }
 
 namespace {
@@ -139,6 +147,52 @@ int kv_svd_truncate(kv_tensor A, int r1, int l2r, double tol, int max_dim, int, 
     if (n_kept) *n_kept = nk;
     if (n_total) *n_total = nt;
     return status(rc);
+}
+
+int kv_tdvp_create(int nsites, const kv_tensor *mps, const kv_tensor *mpo, double tol_svd, double tol_exp,
+                   int max_dim, int max_iter, double dt, int, kv_tdvp *out) {
+    std::vector<void *> m(mps, mps + nsites), w(mpo, mpo + nsites);
+    void *h = nullptr;
+    const int rc = kvo_tdvp_new(nsites, m.data(), w.data(), tol_svd, tol_exp, max_dim, max_iter, dt, &h);
+    *out = static_cast<kv_tdvp>(h);
+    return status(rc);
+}
+
+int kv_tdvp_sweep(kv_tdvp s, int mode) {
+    ++g_calls;
+    return status(kvo_tdvp_sweep(static_cast<void *>(s), mode));
+}
+
+int kv_tdvp_set_sa(kv_tdvp s, const double *beta, int nbeta, unsigned long long seed, long long *added_last) {
+    if (added_last) *added_last = 0;
+    return status(kvo_tdvp_set_sa(static_cast<void *>(s), beta, nbeta, seed));
+}
+
+int kv_tdvp_svs(kv_tdvp, int *n_records, long long *n_values, int *, double *) {
+    if (n_records) *n_records = 0;
+    if (n_values) *n_values = 0;
+    return KV_OK;
+}
+
+int kv_tdvp_site(kv_tdvp s, int i, kv_tensor *out) {
+    void *h = nullptr;
+    const int rc = kvo_tdvp_site(static_cast<void *>(s), i, &h);
+    *out = T(h);
+    return status(rc);
+}
+
+int kv_tdvp_stats(kv_tdvp, double *module_ms, double *sweep_ms, double *ref_flops, double *gemm_ref_flops) {
+    if (module_ms)
+        for (int i = 0; i < 6; ++i) module_ms[i] = 0.0;
+    if (sweep_ms) *sweep_ms = 0.0;
+    if (ref_flops) *ref_flops = 0.0;
+    if (gemm_ref_flops) *gemm_ref_flops = 0.0;
+    return KV_OK;
+}
+
+int kv_tdvp_free(kv_tdvp s) {
+    kvo_tdvp_free(static_cast<void *>(s));
+    return KV_OK;
 }
 
 }  // extern "C"

@@ -31,6 +31,20 @@ def load_oracle():
     return oracle
 
 
+def build_abi_double(dest) -> str:
+    """Compile tests/kvgpu_oracle_double.cpp (the C ABI answered by the CPU
+    oracle, for host-side tests of the C++ layer) into dest/libkvgpu.so."""
+    import subprocess
+
+    oracle_dir = os.path.dirname(load_oracle().build())
+    os.makedirs(dest, exist_ok=True)
+    so = os.path.join(str(dest), "libkvgpu.so")
+    subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-fPIC", "-shared", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "kvgpu_oracle_double.cpp"), "-o", so, f"-L{oracle_dir}", "-lkvoracle",
+                    f"-Wl,-rpath,{oracle_dir}"], check=True)
+    return so
+
+
 def manifest():
     with open(os.path.join(GOLDEN, "manifest.json")) as f:
         return json.load(f)

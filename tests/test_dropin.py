@@ -1,7 +1,9 @@
 """The drop-in C++ layer (include/holstein/): the reference's own driver
-src/kln-tdvp.cpp compiles unchanged against it (CPU, where the reference tree
-is present), and a driver using the same calls reproduces the library's TDVP
-sweep on the GPU, checkpoint file included."""
+src/kln-tdvp.cpp compiles unchanged against it and, on a CPU test double of
+the C ABI, runs the same trajectory as the reference built with its own
+headers (CPU, where the reference tree is present); a driver using the same
+calls reproduces the library's TDVP sweep on the GPU, checkpoint file
+included."""
 import os
 import shutil
 import subprocess
@@ -36,6 +38,68 @@ def test_reference_driver_compiles_unchanged(tmp_path):
     r = subprocess.run([_cxx(), "-std=c++17", str(tmp_path / "src" / "kln-tdvp.cpp"), "-o", str(tmp_path / "kln-tdvp"),
                         "-L" + LIBDIR, "-lkvgpu", "-Wl,-rpath," + LIBDIR], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-2000:]
+
+
+REF_BIN = os.path.join(ROOT, "oracle", "_ref", "kln-tdvp")
+
+
+def _observables(case):
+    """Norm, energy and site populations of an MPS on a golden case's chain."""
+    import sys
+
+    sys.path.insert(0, U.GOLDEN)
+    import make_golden as MG  # noqa: E402
+
+    from kylin_v_gb300 import holstein as H
+
+    O = U.load_oracle()
+    ch = MG.cases()[case]["chain"]
+    mpo = kvio.read_mpo(os.path.join(U.GOLDEN, case, "H.mpo"))
+    ident = H.identity_mpo(ch)
+    dens = [H.density_mpo(ch, j) for j in ch.exciton_sites()]
+
+    def obs(s):
+        return np.array([O.join(s, ident, s).real, O.join(s, mpo, s).real] + [O.join(s, d, s).real for d in dens])
+
+    return obs
+
+
+@pytest.mark.skipif(not os.path.exists(REF_DRIVER) or not os.path.exists(REF_BIN) or _cxx() is None,
+                    reason="reference tree, its compiled driver or g++ absent")
+def test_reference_driver_runs_on_the_layer(tmp_path):
+    """The reference's own src/kln-tdvp.cpp, unchanged, compiled against
+    include/holstein/ and run on a CPU test double of the C ABI
+    (tests/kvgpu_oracle_double.cpp), against the same driver compiled with
+    the reference's own headers (oracle/_ref/kln-tdvp): two two-site and two
+    one-site sweeps; every checkpoint has the same norm, energy, site
+    populations and largest bond."""
+    libdir = tmp_path / "lib"
+    U.build_abi_double(libdir)
+    (tmp_path / "src").mkdir()
+    os.symlink(REF_DRIVER, tmp_path / "src" / "kln-tdvp.cpp")
+    os.symlink(os.path.join(ROOT, "include", "holstein"), tmp_path / "holstein")
+    exe = tmp_path / "kln-tdvp"
+    r = subprocess.run([_cxx(), "-std=c++17", "-O1", str(tmp_path / "src" / "kln-tdvp.cpp"), "-o", str(exe),
+                        f"-L{libdir}", "-lkvgpu", f"-Wl,-rpath,{libdir}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    case = "tiny1"
+    g = os.path.join(U.GOLDEN, case)
+    D = U.manifest()[case]["D"]
+    args = ["-w", os.path.join(g, "in.mps"), "-o", os.path.join(g, "H.mpo"), "-s", "[0,2,0,2]", "-v", "0.05",
+            "-D", str(D), "-t", "1e-8"]
+    runs = {}
+    for name, prog in (("layer", str(exe)), ("reference", REF_BIN)):
+        wd = tmp_path / name
+        (wd / "State").mkdir(parents=True)  # the reference writes its checkpoints there, it does not create it
+        r = subprocess.run([prog] + args, cwd=wd, capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, name + ": " + r.stdout[-2000:] + r.stderr[-2000:]
+        runs[name] = wd
+    obs = _observables(case)
+    for k in range(4):
+        a = kvio.read_mps(str(runs["layer"] / "State" / f"T-{k}.mps"))
+        b = kvio.read_mps(str(runs["reference"] / "State" / f"T-{k}.mps"))
+        assert np.abs(obs(a) - obs(b)).max() < 1e-12, k
+        assert [sum(t.legs()[2].values()) for t in a] == [sum(t.legs()[2].values()) for t in b], k
 
 
 @pytest.mark.gpu

@@ -38,10 +38,7 @@ CXX = ["g++", "-std=c++17", "-O1", "-Wall", "-Wno-unused-function"]
 def double_driver(tmp_path_factory):
     """The driver linked against the oracle-backed test double of libkvgpu."""
     d = tmp_path_factory.mktemp("ops_layer")
-    oracle_dir = os.path.dirname(O.build())
-    subprocess.run(CXX + ["-fPIC", "-shared", "-I", os.path.join(ROOT, "include"),
-                          os.path.join(ROOT, "tests", "kvgpu_oracle_double.cpp"), "-o", str(d / "libkvgpu.so"),
-                          f"-L{oracle_dir}", "-lkvoracle", f"-Wl,-rpath,{oracle_dir}"], check=True)
+    U.build_abi_double(d)
     subprocess.run(CXX + ["-I", os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "ops_layer_driver.cpp"),
                           "-o", str(d / "ops_layer_driver"), f"-L{d}", "-lkvgpu", f"-Wl,-rpath,{d}"], check=True)
     return d / "ops_layer_driver"
