@@ -33,6 +33,10 @@ cpu_baseline  the CPU oracle (restatement of the reference on OpenBLAS, all
            updates (sites 20-24) timed after the pass is advanced there, the
            full step extrapolated (2 x 159 updates).
 
+batched    (N = 1, default config) the 64-chain disordered ensemble of
+           --config holstein-1site-batch64 advanced by kv_sweep_batched: one
+           untimed and one timed one-site step (batched_leg); --no-batched
+           skips it.
 --impl reference  runs only the CPU oracle sample (rank 0) and prints its line,
            with a one-thread measurement of the same sample beside it.
 --config holstein-1site-batch64  the batched disordered ensemble instead
@@ -57,6 +61,7 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 METRIC = "TDVP sweep s & H_eff TFLOP/s, mixed vs plain FP64 on GB300 at <=1e-6 pop err"
+DEFAULT_CONFIG = "holstein-2site-L32"
 
 
 def parse():
@@ -65,10 +70,13 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="holstein-2site-L32")
+    ap.add_argument("--config", default=DEFAULT_CONFIG)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-compare", action="store_true", help="skip the mixed-vs-FP64 comparison leg")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the batched-ensemble leg of the default run (its own config: --config "
+                         "holstein-1site-batch64)")
     ap.add_argument("--compare-steps", type=int, default=1,
                     help="time steps of the mixed-vs-FP64 comparison leg (on the benchmark chain itself)")
     ap.add_argument("--compare-against", default="fp64", choices=["fp64", "fp64-contractions"],
@@ -377,6 +385,8 @@ def run_ours(args):
                    "mean_dimension": kry["mean_dimension"]},
         "gpu_launches_per_step": launches / args.steps,
     }
+    if ws == 1 and not args.no_batched and args.molecules is None and args.config == DEFAULT_CONFIG:
+        line["batched"] = batched_leg(G, prec, max_streams=args.max_streams)
     if not args.no_compare:
         line["fp64_compare"] = compare_fp64(args, G)
     if not args.no_cpu:
@@ -448,6 +458,39 @@ def compare_fp64(args, G):
             "fp64_modules_ms_per_step": modules[ref],
             "max_pop_err": perr, "max_energy_err": eerr, "pop_err_by_step": per_step,
             "energy_fp64": float(obs[ref][1])}
+
+
+def batched_leg(G, prec, chains: int = 64, steps: int = 1, warmup: int = 1, max_streams: int = 0) -> dict:
+    """The batched ensemble (run_batched's workload, 64 disordered chains,
+    one-site TDVP) measured inside the default run at N = 1: `warmup` untimed
+    and `steps` timed time steps of all chains advanced together by
+    kv_sweep_batched (device ms).  Returns its figures, or the error that
+    stopped it; the headline line is printed either way."""
+    try:
+        import __graft_entry__ as ge
+
+        ge.load_package()
+        from kylin_v_gb300 import holstein as H
+
+        members = [H.disordered_chain(i) for i in range(chains)]
+        host = [(H.random_mps(ch, D, seed=1234 + i), H.hamiltonian_mpo(ch), D) for i, (ch, D) in enumerate(members)]
+        bat = [G.TDVP([G.Tensor.from_host(x) for x in m], [G.Tensor.from_host(x) for x in w], 1e-8, 1e-8, D, 11,
+                      0.05, prec) for m, w, D in host]
+        G.sweep_batched(bat, 1, warmup, max_streams)
+        n0 = G.launches()
+        ms, flops = 0.0, 0.0
+        for _ in range(steps):
+            ms += G.sweep_batched(bat, 1, 1, max_streams)
+            flops += sum(t.stats()["ref_flops"] for t in bat)
+        launches = G.launches() - n0
+        del bat
+        return {"workload": BATCH_CONFIG, "chains": chains, "mode": "1-site TDVP", "steps": steps,
+                "warmup": warmup, "ms_per_step": ms / steps, "value": flops / (ms / 1e3) / 1e12, "unit": "TFLOP/s",
+                "sites": sum(ch.n_sites for ch, _ in members), "gpu_launches_per_step": launches / steps,
+                "note": f"device time of kv_sweep_batched; the full leg with the one-after-another timing is "
+                        f"bench.py --config {BATCH_CONFIG}"}
+    except Exception as e:  # the leg must not cost the headline line
+        return {"workload": BATCH_CONFIG, "error": f"{type(e).__name__}: {e}"}
 
 
 def run_batched(args):
