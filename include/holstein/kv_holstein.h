@@ -194,6 +194,36 @@ class State {
     HostTensor<3> &operator[](INT i) { return tt_[i]; }
     const HostTensor<3> &at(INT i) const { return tt_[i]; }
 
+    // the scalar multiplies site 0 (holstein/state.h:66-85)
+    State &operator*=(double val) {
+        for (auto &b : tt_.at(0).data)
+            for (auto &x : b) x *= val;
+        return *this;
+    }
+    State operator*(const Complex &val) const {
+        State res(*this);
+        for (auto &b : res.tt_.at(0).data)
+            for (auto &x : b) x *= val;
+        return res;
+    }
+    State operator*(double val) const { return (*this) * Complex(val, 0.0); }
+
+    // an L->R then an R->L SVD sweep on the device, the orthogonality centre
+    // left on site 0 (holstein/state.h:166-185)
+    void canonicalize(double tolS = 0.0, INT mD = 1000) {
+        detail::ensure_init();
+        const INT ns = nsite();
+        vector<kv_tensor> in(ns), out(ns, nullptr);
+        for (INT i = 0; i < ns; ++i) in[i] = tt_[i].upload();
+        const int rc = kv_canonicalize(ns, in.data(), tolS, mD, detail::precision(), out.data());
+        for (auto t : in) kv_tensor_free(t);
+        detail::check(rc, "canonicalize");
+        for (INT i = 0; i < ns; ++i) {
+            tt_[i] = HostTensor<3>::download(out[i]);
+            kv_tensor_free(out[i]);
+        }
+    }
+
     // largest right bond dimension and its position (holstein/state.h:187-200)
     void max_bond() const {
         INT mb = 0, mbp = 0;
@@ -250,6 +280,38 @@ class Operator {
     INT nsite() const { return (INT)tt_.size(); }
     HostTensor<4> &operator[](INT i) { return tt_[i]; }
     const HostTensor<4> &at(INT i) const { return tt_[i]; }
+
+    // the scalar multiplies site 0 (holstein/operator.h:66-70)
+    Operator &operator*=(double val) {
+        for (auto &b : tt_.at(0).data)
+            for (auto &x : b) x *= val;
+        return *this;
+    }
+
+    // <s1|this|s2> on the device (holstein/operator.h:178-198)
+    Complex join(const State &s1, const State &s2) const {
+        detail::ensure_init();
+        const INT ns = nsite();
+        if (s1.nsite() != ns || s2.nsite() != ns) {
+            cout << "join: the states and the operator differ in length" << endl;
+            exit(1);
+        }
+        vector<kv_tensor> a(ns), w(ns), b(ns);
+        for (INT i = 0; i < ns; ++i) {
+            a[i] = s1.at(i).upload();
+            w[i] = tt_[i].upload();
+            b[i] = s2.at(i).upload();
+        }
+        double re = 0.0, im = 0.0;
+        const int rc = kv_expectation(ns, a.data(), w.data(), b.data(), &re, &im);
+        for (INT i = 0; i < ns; ++i) {
+            kv_tensor_free(a[i]);
+            kv_tensor_free(w[i]);
+            kv_tensor_free(b[i]);
+        }
+        detail::check(rc, "join");
+        return Complex(re, im);
+    }
 
   private:
     vector<HostTensor<4>> tt_;

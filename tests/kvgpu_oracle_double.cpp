@@ -26,6 +26,7 @@ int kvo_local_krylov(int nsite, void *L, void *psi, void *W1, void *W2, void *R,
                      int reverse, int *iters, void **out);
 int kvo_svd(void *A, int r1, int l2r, double tol, int max_dim, void **U, void **V, double *svals, int *nkept,
             int *ntotal);
+int kvo_join(int ns, void **a, void **w, void **b, double *re, double *im);
 int kvo_tdvp_new(int ns, void **mps, void **mpo, double tol_svd, double tol_exp, int max_dim, int max_iter,
                  double dt, void **out);
 int kvo_tdvp_sweep(void *h, int mode);
@@ -147,6 +148,59 @@ int kv_svd_truncate(kv_tensor A, int r1, int l2r, double tol, int max_dim, int, 
     if (n_kept) *n_kept = nk;
     if (n_total) *n_total = nt;
     return status(rc);
+}
+
+// State::canonicalize by the reference's sequence of SVDs and products
+// (holstein/state.h:166-185) on the oracle's primitives
+int kv_canonicalize(int nsites, const kv_tensor *mps, double tol_svd, int max_dim, int, kv_tensor *out) {
+    ++g_calls;
+    std::vector<void *> t(nsites);
+    auto copy = [](void *h) {  // a fresh oracle tensor equal to h
+        int rank = 0, nb = 0;
+        long long ne = 0;
+        kvo_tensor_info(h, &rank, &nb, &ne);
+        std::vector<int> dirs(rank), sh((size_t)nb * rank), qn((size_t)nb * rank);
+        std::vector<double> d(2 * (size_t)ne + 2);
+        kvo_tensor_get(h, dirs.data(), sh.data(), qn.data(), d.data());
+        void *c = nullptr;
+        kvo_tensor_new(rank, dirs.data(), nb, sh.data(), qn.data(), d.data(), &c);
+        return c;
+    };
+    for (int i = 0; i < nsites; ++i) t[i] = copy(H(mps[i]));
+    int rc = 0;
+    for (int i = 0; i + 1 < nsites && rc == 0; ++i) {
+        void *u = nullptr, *v = nullptr, *nx = nullptr;
+        int nk = 0, nt = 0;
+        rc = kvo_svd(t[i], 2, 1, tol_svd, max_dim, &u, &v, nullptr, &nk, &nt);
+        if (rc == 0) rc = kvo_product(v, t[i + 1], 1, KV_OP_N, KV_OP_N, &nx);
+        if (rc != 0) break;
+        kvo_tensor_free(t[i]);
+        kvo_tensor_free(t[i + 1]);
+        kvo_tensor_free(v);
+        t[i] = u;
+        t[i + 1] = nx;
+    }
+    for (int i = nsites - 1; i > 0 && rc == 0; --i) {
+        void *u = nullptr, *v = nullptr, *pv = nullptr;
+        int nk = 0, nt = 0;
+        rc = kvo_svd(t[i], 1, 0, tol_svd, max_dim, &u, &v, nullptr, &nk, &nt);
+        if (rc == 0) rc = kvo_product(t[i - 1], u, 1, KV_OP_N, KV_OP_N, &pv);
+        if (rc != 0) break;
+        kvo_tensor_free(t[i]);
+        kvo_tensor_free(t[i - 1]);
+        kvo_tensor_free(u);
+        t[i] = v;
+        t[i - 1] = pv;
+    }
+    for (int i = 0; i < nsites; ++i) out[i] = T(t[i]);
+    return status(rc);
+}
+
+int kv_expectation(int nsites, const kv_tensor *bra, const kv_tensor *mpo, const kv_tensor *ket, double *re,
+                   double *im) {
+    ++g_calls;
+    std::vector<void *> a(bra, bra + nsites), w(mpo, mpo + nsites), b(ket, ket + nsites);
+    return status(kvo_join(nsites, a.data(), w.data(), b.data(), re, im));
 }
 
 int kv_tdvp_create(int nsites, const kv_tensor *mps, const kv_tensor *mpo, double tol_svd, double tol_exp,

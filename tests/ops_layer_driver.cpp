@@ -1,8 +1,10 @@
 // A program written against the reference's tensor-level headers
-// (holstein/tensor.h, product.h, exponential.h, svd.h), compiled against
-// include/holstein/ and linked with -lkvgpu.  It runs the hot-path
-// primitives on one site of a golden case and writes every result as a .kvt
-// file for tests/test_ops_layer.py to compare with the reference's dumps.
+// (holstein/tensor.h, product.h, exponential.h, svd.h) and its State /
+// Operator classes, compiled against include/holstein/ and linked with
+// -lkvgpu.  It runs the hot-path primitives on one site of a golden case,
+// canonicalises the case's MPS and evaluates <psi|H|psi>, and writes every
+// result as a .kvt file (or in its one JSON line) for tests/test_ops_layer.py
+// to compare with the reference's dumps and the oracle.
 //
 //   ops_layer_driver <case dir> <ops dir> <out dir> <site> <max D>
 #include <cstdio>
@@ -147,9 +149,21 @@ int main(int argc, char **argv) {
     }
     write_kvt(out + "env2_l2r.kvt", env_sweep(e2l, A, a3, true));
 
+    // State / Operator level (holstein/state.h, holstein/operator.h)
+    const Complex j0 = mpo.join(mps, mps);
+    State c = mps;
+    c.canonicalize();
+    const Complex j1 = mpo.join(c, c);
+    Operator half = mpo;
+    half *= 0.5;
+    const Complex j2 = half.join(c * 2.0, c);  // 0.5 * 2 <c|H|c>
+    for (INT k = 0; k < c.nsite(); ++k) write_kvt(out + "canon_" + to_string(k) + ".kvt", to_tensor(c.at(k)));
+
     printf("{\"k1_iters\": %d, \"k2_iters\": %d, \"k0_iters\": %d, \"k1_loss\": %.17g, \"k1_maxitr\": %d, "
-           "\"norm_A\": %.17g, \"overlap_re\": %.17g, \"overlap_im\": %.17g}\n",
+           "\"norm_A\": %.17g, \"overlap_re\": %.17g, \"overlap_im\": %.17g, \"join\": [%.17g, %.17g, %.17g, "
+           "%.17g, %.17g, %.17g]}\n",
            e1.RealIter, e2.RealIter, e0.RealIter, e1.LossNorm,
-           e1.reason == KrylovExitReason::AchMaxItr ? 1 : 0, norm(A), ov.real(), ov.imag());
+           e1.reason == KrylovExitReason::AchMaxItr ? 1 : 0, norm(A), ov.real(), ov.imag(), j0.real(), j0.imag(),
+           j1.real(), j1.imag(), j2.real(), j2.imag());
     return 0;
 }

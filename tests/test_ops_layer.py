@@ -1,6 +1,7 @@
 """The reference's tensor-level C++ surface (include/holstein/kv_ops.h:
-Tensor, Block, product, apply_*, env_sweep, local_krylov, svd_impl) on the
-host side, without a GPU.
+Tensor, Block, product, apply_*, env_sweep, local_krylov, svd_impl; and
+State::canonicalize, Operator::join in kv_holstein.h) on the host side,
+without a GPU.
 
 tests/ops_layer_driver.cpp is written against the reference's header names.
 It is compiled twice:
@@ -124,6 +125,22 @@ def test_layer_matches_reference(double_driver, tmp_path, case, d):
                             [(tuple(reversed(q)), np.transpose(a, (2, 1, 0))) for q, a in A.blocks])
     assert got("A_t210").dirs == t210.dirs
     assert U.tensor_diff(got("A_t210"), t210) == 0.0
+    # State::canonicalize and Operator::join: the canonical form holds the same
+    # state (energy unchanged), every site right of the centre is
+    # right-orthonormal, and the scalar products scale site 0
+    j0, j1, j2 = (complex(info["join"][2 * k], info["join"][2 * k + 1]) for k in range(3))
+    assert abs(j0 - O.join(mps, mpo, mps)) < 1e-12
+    assert abs(j1 - j0) < 1e-10 * max(1.0, abs(j0))
+    assert abs(j2 - j1) < 1e-12 * max(1.0, abs(j1))
+    canon = [got(f"canon_{k}") for k in range(len(mps))]
+    assert abs(O.join(canon, mpo, canon) - j1) < 1e-12
+    for t in canon[1:]:
+        rows = {}
+        for q, a in t.blocks:
+            rows.setdefault(q[0], []).append(a.reshape(a.shape[0], -1))
+        for q, ms in rows.items():
+            m = np.concatenate(ms, axis=1)
+            np.testing.assert_allclose(m @ m.conj().T, np.eye(m.shape[0]), atol=1e-12)
     # the two-leg bra/ket environment: identity on the first block's left sector
     q0, a0 = A.blocks[0]
     e = kvio.BlockTensor((1, -1), [((q0[0], q0[0]), np.eye(a0.shape[0], dtype=complex))])
