@@ -387,12 +387,19 @@ def run_ours(args):
     }
     if ws == 1 and not args.no_batched and args.molecules is None and args.config == DEFAULT_CONFIG:
         line["batched"] = batched_leg(G, prec, max_streams=args.max_streams)
+    # the side legs report their own failure instead of losing the line
     if not args.no_compare:
-        line["fp64_compare"] = compare_fp64(args, G)
+        try:
+            line["fp64_compare"] = compare_fp64(args, G)
+        except Exception as e:
+            line["fp64_compare"] = {"error": f"{type(e).__name__}: {e}"}
     if not args.no_cpu:
-        cb = cpu_baseline(args.config)
-        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
-        line["cpu_baseline"]["ms_per_step"] = cb["ms_per_step"]
+        try:
+            cb = cpu_baseline(args.config)
+            line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+            line["cpu_baseline"]["ms_per_step"] = cb["ms_per_step"]
+        except Exception as e:
+            line["cpu_baseline"] = {"error": f"{type(e).__name__}: {e}"}
     print(json.dumps(line), flush=True)
 
 
