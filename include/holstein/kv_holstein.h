@@ -6,6 +6,9 @@
  * `#include "../holstein/tdvp.h"` resolve here, so the driver compiles
  * unchanged and its sweeps run on the GPU.
  *
+ * Also provided: State::canonicalize and Operator::join (on the device), the
+ * scalar products and the direct sums State += / Operator +=
+ * (holstein/state.h:54-85, holstein/operator.h:54-70).
  * Reference behaviour kept: the binary .mps / .mpo formats
  * (holstein/state.h:107-157, holstein/operator.h:117-143), parse_stage
  * (holstein/tdvp.h:19-32), the TDVP constructor's arguments
@@ -35,6 +38,7 @@
 #include <fstream>
 #include <iomanip>
 #include <iostream>
+#include <map>
 #include <random>
 #include <sstream>
 #include <string>
@@ -155,6 +159,77 @@ struct HostTensor {
     }
 };
 
+namespace detail {
+
+// b added into a as a direct sum along the legs `axes` (holstein/tensor.h
+// stack, :263-320): on each such leg a charge sector's dimension becomes the
+// sum of the two tensors' dimensions, a's entries first and b's after them;
+// every block is zero-padded to its combined shape, then blocks of equal
+// shape and charges are added.  Host-side, like the reference's.
+template <int R>
+void stack_into(HostTensor<R> &a, const HostTensor<R> &b, const vector<int> &axes) {
+    auto legs = [](const HostTensor<R> &t) {
+        array<map<INT, INT>, R> l;
+        for (INT j = 0; j < t.num_blocks(); ++j)
+            for (int i = 0; i < R; ++i) l[i][t.qn[j][i]] = t.shape[j][i];
+        return l;
+    };
+    const array<map<INT, INT>, R> lb = legs(b);
+    array<map<INT, INT>, R> comb = legs(a);
+    for (int ax : axes)
+        for (const auto &kv : lb[ax]) comb[ax][kv.first] += kv.second;
+    // src (shape sp) placed at offset pos of a zero block of shape full, row-major
+    auto embed = [](const vector<Complex> &src, const array<INT, R> &sp, const array<INT, R> &full,
+                    const array<INT, R> &pos) {
+        size_t n = 1;
+        for (INT x : full) n *= (size_t)x;
+        vector<Complex> out(n);
+        for (size_t e = 0; e < src.size(); ++e) {
+            size_t rem = e, dst = 0, stride = 1;
+            array<size_t, R> idx{};
+            for (int i = R - 1; i >= 0; --i) {
+                idx[i] = rem % (size_t)sp[i];
+                rem /= (size_t)sp[i];
+            }
+            for (int i = R - 1; i >= 0; --i) {
+                dst += (idx[i] + (size_t)pos[i]) * stride;
+                stride *= (size_t)full[i];
+            }
+            out[dst] = src[e];
+        }
+        return out;
+    };
+    for (INT j = 0; j < a.num_blocks(); ++j) {
+        array<INT, R> full = a.shape[j], pos{};
+        for (int ax : axes) full[ax] = comb[ax][a.qn[j][ax]];
+        if (full != a.shape[j]) {
+            a.data[j] = embed(a.data[j], a.shape[j], full, pos);
+            a.shape[j] = full;
+        }
+    }
+    for (INT j = 0; j < b.num_blocks(); ++j) {
+        array<INT, R> full = b.shape[j], pos{};
+        for (int ax : axes) {
+            full[ax] = comb[ax][b.qn[j][ax]];
+            pos[ax] = full[ax] - b.shape[j][ax];
+        }
+        vector<Complex> blk = full == b.shape[j] ? b.data[j] : embed(b.data[j], b.shape[j], full, pos);
+        bool added = false;
+        for (INT k = 0; k < a.num_blocks() && !added; ++k)
+            if (a.shape[k] == full && a.qn[k] == b.qn[j]) {
+                for (size_t e = 0; e < blk.size(); ++e) a.data[k][e] += blk[e];
+                added = true;
+            }
+        if (!added) {
+            a.shape.push_back(full);
+            a.qn.push_back(b.qn[j]);
+            a.data.push_back(move(blk));
+        }
+    }
+}
+
+}  // namespace detail
+
 // Holstein::State: an MPS, legs (left bond, phys, right bond), dirs {1, 1, -1}
 class State {
   public:
@@ -193,6 +268,20 @@ class State {
     INT nsite() const { return (INT)tt_.size(); }
     HostTensor<3> &operator[](INT i) { return tt_[i]; }
     const HostTensor<3> &at(INT i) const { return tt_[i]; }
+
+    // direct sum: the MPS of this + r, bond dimensions added
+    // (holstein/state.h:54-64)
+    State &operator+=(const State &r) {
+        const INT ns = nsite();
+        if (r.nsite() != ns || ns < 2) {
+            cout << "State += : the states differ in length" << endl;
+            exit(1);
+        }
+        detail::stack_into(tt_[0], r.tt_[0], {2});
+        for (INT i = 1; i < ns - 1; ++i) detail::stack_into(tt_[i], r.tt_[i], {0, 2});
+        detail::stack_into(tt_[ns - 1], r.tt_[ns - 1], {0});
+        return *this;
+    }
 
     // the scalar multiplies site 0 (holstein/state.h:66-85)
     State &operator*=(double val) {
@@ -280,6 +369,20 @@ class Operator {
     INT nsite() const { return (INT)tt_.size(); }
     HostTensor<4> &operator[](INT i) { return tt_[i]; }
     const HostTensor<4> &at(INT i) const { return tt_[i]; }
+
+    // direct sum: the MPO of this + r, MPO bond dimensions added
+    // (holstein/operator.h:54-64)
+    Operator &operator+=(const Operator &r) {
+        const INT ns = nsite();
+        if (r.nsite() != ns || ns < 2) {
+            cout << "Operator += : the operators differ in length" << endl;
+            exit(1);
+        }
+        detail::stack_into(tt_[0], r.tt_[0], {3});
+        for (INT i = 1; i < ns - 1; ++i) detail::stack_into(tt_[i], r.tt_[i], {1, 3});
+        detail::stack_into(tt_[ns - 1], r.tt_[ns - 1], {1});
+        return *this;
+    }
 
     // the scalar multiplies site 0 (holstein/operator.h:66-70)
     Operator &operator*=(double val) {

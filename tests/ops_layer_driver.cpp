@@ -158,12 +158,22 @@ int main(int argc, char **argv) {
     half *= 0.5;
     const Complex j2 = half.join(c * 2.0, c);  // 0.5 * 2 <c|H|c>
     for (INT k = 0; k < c.nsite(); ++k) write_kvt(out + "canon_" + to_string(k) + ".kvt", to_tensor(c.at(k)));
+    // direct sums: H + 2H represents 3H, psi + psi represents 2 psi
+    Operator h3 = mpo, two = mpo;
+    two *= 2.0;
+    h3 += two;
+    const Complex j3 = h3.join(mps, mps);
+    State s2 = mps;
+    s2 += mps;
+    const Complex j4 = mpo.join(s2, s2);
+    write_kvt(out + "sum_state_1.kvt", to_tensor(s2.at(1)));
+    write_kvt(out + "sum_mpo_1.kvt", to_tensor(h3.at(1)));
 
     printf("{\"k1_iters\": %d, \"k2_iters\": %d, \"k0_iters\": %d, \"k1_loss\": %.17g, \"k1_maxitr\": %d, "
            "\"norm_A\": %.17g, \"overlap_re\": %.17g, \"overlap_im\": %.17g, \"join\": [%.17g, %.17g, %.17g, "
-           "%.17g, %.17g, %.17g]}\n",
+           "%.17g, %.17g, %.17g, %.17g, %.17g, %.17g, %.17g]}\n",
            e1.RealIter, e2.RealIter, e0.RealIter, e1.LossNorm,
            e1.reason == KrylovExitReason::AchMaxItr ? 1 : 0, norm(A), ov.real(), ov.imag(), j0.real(), j0.imag(),
-           j1.real(), j1.imag(), j2.real(), j2.imag());
+           j1.real(), j1.imag(), j2.real(), j2.imag(), j3.real(), j3.imag(), j4.real(), j4.imag());
     return 0;
 }

@@ -141,6 +141,16 @@ def test_layer_matches_reference(double_driver, tmp_path, case, d):
         for q, ms in rows.items():
             m = np.concatenate(ms, axis=1)
             np.testing.assert_allclose(m @ m.conj().T, np.eye(m.shape[0]), atol=1e-12)
+    # State += and Operator += (direct sums): H + 2H is 3H, psi + psi is 2 psi,
+    # and the summed legs carry both parts' dimensions per charge
+    j3, j4 = (complex(info["join"][2 * k], info["join"][2 * k + 1]) for k in (3, 4))
+    assert abs(j3 - 3 * j0) < 1e-10 * max(1.0, abs(j0))
+    assert abs(j4 - 4 * j0) < 1e-10 * max(1.0, abs(j0))
+    s1, m1 = got("sum_state_1"), got("sum_mpo_1")
+    for leg in (0, 2):
+        assert s1.legs()[leg] == {q: 2 * n for q, n in mps[1].legs()[leg].items()}
+    for leg in (1, 3):
+        assert m1.legs()[leg] == {q: 2 * n for q, n in mpo[1].legs()[leg].items()}
     # the two-leg bra/ket environment: identity on the first block's left sector
     q0, a0 = A.blocks[0]
     e = kvio.BlockTensor((1, -1), [((q0[0], q0[0]), np.eye(a0.shape[0], dtype=complex))])
