@@ -1,5 +1,5 @@
 /* The reference's tensor-level C++ surface on libkvgpu: Block<Rank> and
- * Tensor<Rank> with norm / overlap / transpose (holstein/block.h,
+ * Tensor<Rank> with norm / overlap / transpose / stack (holstein/block.h,
  * holstein/tensor.h), product<N1,N2,nc>, apply_zero / apply_single /
  * apply_double and env_sweep (holstein/product.h), local_krylov<Rank> with
  * KrylovConfig / KrylovExit (holstein/exponential.h) and svd_impl<R1,R2> with
@@ -311,6 +311,29 @@ Tensor<Rank> to_tensor(const HostTensor<Rank> &h) {
     }
     t.check_legs();
     return t;
+}
+
+// the host blocks of a tensor in the drop-in State / Operator form
+template <INT Rank>
+HostTensor<Rank> to_host(const Tensor<Rank> &t) {
+    HostTensor<Rank> h;
+    h.dirs = t.dirs();
+    for (INT j = 0; j < t.num_blocks(); ++j) {
+        const Block<Rank> &b = t.at(j);
+        h.shape.push_back(b.shape());
+        h.qn.push_back(b.qn());
+        h.data.emplace_back(b.cptr(), b.cptr() + b.size());
+    }
+    return h;
+}
+
+// om2 added into om1 as a direct sum along the legs ax (holstein/tensor.h
+// stack, :263-320); om2 is left unchanged
+template <INT Rank>
+void stack(Tensor<Rank> &om1, const Tensor<Rank> &om2, Brace ax) {
+    HostTensor<Rank> h = to_host(om1);
+    detail::stack_into(h, to_host(om2), vector<int>(ax.begin(), ax.end()));
+    om1 = to_tensor(h);
 }
 
 // sqrt of the summed squared block norms (holstein/tensor.h:214-223)

@@ -168,6 +168,9 @@ int main(int argc, char **argv) {
     const Complex j4 = mpo.join(s2, s2);
     write_kvt(out + "sum_state_1.kvt", to_tensor(s2.at(1)));
     write_kvt(out + "sum_mpo_1.kvt", to_tensor(h3.at(1)));
+    Tensor<3> x = to_tensor(mps.at(1));
+    stack<3>(x, to_tensor(mps.at(1)), {0, 2});
+    write_kvt(out + "stack_1.kvt", x);
 
     printf("{\"k1_iters\": %d, \"k2_iters\": %d, \"k0_iters\": %d, \"k1_loss\": %.17g, \"k1_maxitr\": %d, "
            "\"norm_A\": %.17g, \"overlap_re\": %.17g, \"overlap_im\": %.17g, \"join\": [%.17g, %.17g, %.17g, "

@@ -151,6 +151,7 @@ def test_layer_matches_reference(double_driver, tmp_path, case, d):
         assert s1.legs()[leg] == {q: 2 * n for q, n in mps[1].legs()[leg].items()}
     for leg in (1, 3):
         assert m1.legs()[leg] == {q: 2 * n for q, n in mpo[1].legs()[leg].items()}
+    assert U.tensor_diff(got("stack_1"), s1) == 0.0  # the tensor-level stack is the same direct sum
     # the two-leg bra/ket environment: identity on the first block's left sector
     q0, a0 = A.blocks[0]
     e = kvio.BlockTensor((1, -1), [((q0[0], q0[0]), np.eye(a0.shape[0], dtype=complex))])
